@@ -1,0 +1,239 @@
+/*
+ * lpgpu.h -- C ABI of the GB300-native label-propagation (km1) refinement path.
+ *
+ * The reference (Mt-KaHyPar) exposes this phase only in C++, through
+ *   IRefiner::initialize / IRefiner::refine
+ *     (mt-kahypar/partition/refinement/i_refiner.h:45-53),
+ *   created by LabelPropagationFactory
+ *     (mt-kahypar/partition/factories.h:60-61,
+ *      mt-kahypar/partition/registries/register_refinement_algorithms.cpp:35-40),
+ * and operates on PartitionedHypergraph
+ *     (mt-kahypar/datastructures/partitioned_hypergraph.h:44-1201).
+ * Its public C API (include/libkahypar.h:58-86) has no refine-only entry point,
+ * so the entry points below are what an FFI binding of that phase binds. Each
+ * declaration names the reference interface it replaces.
+ *
+ * Conventions
+ *   - All ids are int32 (vertices, nets, blocks); CSR offsets are int64.
+ *   - Host pointers are caller-owned and only read/written during the call.
+ *   - Device state lives in an opaque session; every call returns a status.
+ *   - There is no CPU fallback: without a usable CUDA device every call that
+ *     needs one returns LPGPU_ERR_NO_DEVICE.
+ *   - A session is not reentrant: calls on one session must not overlap.
+ *     Distinct sessions may be used from distinct threads.
+ */
+#ifndef LPGPU_H_
+#define LPGPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define LPGPU_API __attribute__((visibility("default")))
+#else
+#define LPGPU_API
+#endif
+
+typedef enum {
+  LPGPU_OK = 0,
+  LPGPU_ERR_INVALID_ARG = 1,   /* malformed CSR, ids out of range, k too large ... */
+  LPGPU_ERR_OOM = 2,           /* device allocation failed */
+  LPGPU_ERR_ADMISSION = 3,     /* request does not fit the configured memory budget */
+  LPGPU_ERR_TIMEOUT = 4,       /* a bounded device wait gave up */
+  LPGPU_ERR_CUDA = 5,          /* any other CUDA runtime error */
+  LPGPU_ERR_NO_DEVICE = 6,     /* no CUDA device, or the library was not built for it */
+  LPGPU_ERR_STATE = 7          /* call order violated (e.g. refine before set_partition) */
+} lpgpu_status;
+
+/* Largest number of blocks the device path supports. */
+#define LPGPU_MAX_K 1024
+
+/* LP parameters. Mirrors Context::refinement.label_propagation
+ * (mt-kahypar/partition/context.h:119-125) plus the synchronous-round knobs.
+ * lpgpu_config_default() fills the fast_preset.ini values
+ * (config/fast_preset.ini:57-61): 5 rounds, rebalancing on, activation
+ * threshold 100. */
+typedef struct {
+  int32_t rounds;               /* maximum_iterations */
+  int32_t activation_threshold; /* hyperedge_size_activation_threshold; <= 0 means no limit */
+  int32_t rebalancing;          /* 1: all vertices start active and zero-gain rebalancing
+                                   moves are allowed; 0: border vertices start active */
+  int32_t subrounds;            /* sub-rounds per round (>= 1) */
+  int32_t revert;               /* 1: undo moves whose reverse now strictly improves km1 */
+  int32_t rollback;             /* 1: undo a sub-round whose summed delta is positive */
+  int32_t reserved0;
+  int32_t reserved1;
+} lpgpu_config;
+
+/* Result of one refine call. Mirrors the kahypar::Metrics update done in
+ * LabelPropagationRefiner::refineImpl (label_propagation_refiner.cpp:48-67). */
+typedef struct {
+  int64_t km1_before;
+  int64_t km1_after;      /* recomputed from the device connectivity sets */
+  int64_t delta;          /* sum of attributed objective deltas (km1_after - km1_before) */
+  int64_t moves;          /* committed moves kept at the end */
+  int64_t pins_processed; /* sum over rounds of sum of degrees of swept vertices */
+  int32_t rounds;         /* rounds executed */
+  int32_t improved;       /* IRefiner::refine return value: delta < 0 */
+  double imbalance;       /* metrics::imbalance after refinement */
+} lpgpu_result;
+
+/* Per-round statistics. */
+typedef struct {
+  int64_t active;
+  int64_t pins;
+  int64_t candidates;
+  int64_t moved;
+  int64_t reverted;
+  int64_t delta;
+} lpgpu_round_stats;
+
+typedef struct lpgpu_session_s lpgpu_session;
+
+/* ---------------------------------------------------------------- config */
+
+/* Fills *cfg with the preset values (see lpgpu_config). */
+LPGPU_API void lpgpu_config_default(lpgpu_config* cfg);
+
+/* Human-readable name of a status code. */
+LPGPU_API const char* lpgpu_status_string(lpgpu_status s);
+
+/* Text of the last error on this thread (empty string if none). */
+LPGPU_API const char* lpgpu_last_error(void);
+
+/* ------------------------------------------------------------- one-shot */
+
+/* Refine a partition in place: upload, initializePartition, LP rounds,
+ * download. Replaces the pair LabelPropagationFactory::createObject +
+ * IRefiner::refine on a PartitionedHypergraph built by
+ * HypergraphFactory::construct (lib/libkahypar.cc:168-190) for this phase.
+ * Max block weight follows Context::setupPartWeights (context.cpp:237-250):
+ * perfect = ceil(W/k), max = (int)((1 + eps) * perfect). */
+LPGPU_API lpgpu_status lpgpu_refine_km1(int64_t num_vertices, int64_t num_nets,
+                                        const int64_t* net_offsets, const int32_t* pins,
+                                        const int32_t* vertex_weights, /* NULL: unit */
+                                        const int32_t* net_weights,    /* NULL: unit */
+                                        int32_t k, double epsilon,
+                                        int32_t* partition_inout,
+                                        const lpgpu_config* cfg, /* NULL: defaults */
+                                        lpgpu_result* result);
+
+/* ----------------------------------------------------------- sessions */
+
+/* Creates a session on CUDA device `device`. */
+LPGPU_API lpgpu_status lpgpu_session_create(int32_t device, lpgpu_session** out);
+LPGPU_API lpgpu_status lpgpu_session_destroy(lpgpu_session* s);
+
+/* Uploads the hypergraph (net -> pins CSR) and builds the vertex -> incident
+ * nets arrays on the device. Replaces StaticHypergraphFactory::construct
+ * (static_hypergraph_factory.cpp:32-166). Incident-net order per vertex is
+ * unspecified; nothing computed depends on it. Single-pin nets are kept. */
+LPGPU_API lpgpu_status lpgpu_session_upload(lpgpu_session* s, int64_t num_vertices,
+                                            int64_t num_nets, const int64_t* net_offsets,
+                                            const int32_t* pins,
+                                            const int32_t* vertex_weights, /* NULL: unit */
+                                            const int32_t* net_weights);   /* NULL: unit */
+
+/* Sets the block of every vertex and rebuilds block weights, pin counts and
+ * connectivity sets. Replaces setOnlyNodePart for all vertices followed by
+ * PartitionedHypergraph::initializePartition (partitioned_hypergraph.h:522-526,
+ * 693-698, 1067-1110). max_part_weights / perfect_part_weights may be NULL, in
+ * which case they are derived from epsilon as in lpgpu_refine_km1. */
+LPGPU_API lpgpu_status lpgpu_session_set_partition(lpgpu_session* s, int32_t k, double epsilon,
+                                                   const int32_t* partition,
+                                                   const int64_t* max_part_weights,
+                                                   const int64_t* perfect_part_weights);
+
+/* Runs the LP refinement on the device-resident state. Replaces
+ * IRefiner::refine of LabelPropagationRefiner<Km1Policy>
+ * (label_propagation_refiner.cpp:34-68). refinement_nodes (may be NULL with
+ * count 0, meaning all vertices) restricts the initial active set
+ * (label_propagation_refiner.cpp:200-230). */
+LPGPU_API lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg,
+                                            const int32_t* refinement_nodes,
+                                            int64_t num_refinement_nodes,
+                                            lpgpu_result* result);
+
+/* Statistics of the last refine: up to max_rounds records, returns the count in *rounds. */
+LPGPU_API lpgpu_status lpgpu_session_round_stats(lpgpu_session* s, lpgpu_round_stats* out,
+                                                 int32_t max_rounds, int32_t* rounds);
+
+/* Downloads partID for all vertices (PartitionedHypergraph::partID, h:517). */
+LPGPU_API lpgpu_status lpgpu_session_get_partition(lpgpu_session* s, int32_t* partition);
+
+/* metrics::km1 and metrics::hyperedgeCut (metrics.cpp:29-65) on the device state,
+ * plus metrics::imbalance (metrics.cpp:114-128). Any output pointer may be NULL. */
+LPGPU_API lpgpu_status lpgpu_session_metrics(lpgpu_session* s, int64_t* km1, int64_t* cut,
+                                             double* imbalance);
+
+/* Block weights c(V_b) (partWeight, h:599), k values. */
+LPGPU_API lpgpu_status lpgpu_session_get_block_weights(lpgpu_session* s, int64_t* weights);
+
+/* Pin counts Φ(e,b) (pinCountInPart, h:640) as a dense num_nets x k int32 array. */
+LPGPU_API lpgpu_status lpgpu_session_get_pin_counts(lpgpu_session* s, int32_t* pin_counts);
+
+/* Connectivity sets Λ(e) (connectivitySet, connectivity_set.h:53-221) as
+ * num_nets x ceil(k/32) uint32 words; bit b%32 of word b/32 is block b. */
+LPGPU_API lpgpu_status lpgpu_session_get_connectivity(lpgpu_session* s, uint32_t* words);
+
+/* Vertex -> incident nets arrays built by upload (vertex_offsets: n+1 int64,
+ * incident_nets: P int32). */
+LPGPU_API lpgpu_status lpgpu_session_get_incidence(lpgpu_session* s, int64_t* vertex_offsets,
+                                                   int32_t* incident_nets);
+
+/* Per-vertex best move under Km1Policy::computeMaxGainMoveImpl with
+ * disable_randomization = true (gain_policy.h:108-167), guarded by
+ * isBorderNode (partitioned_hypergraph.h:605-620). to[v] == partID(v) and
+ * gain[v] == 0 when no strictly improving feasible move exists; border[v] is
+ * isBorderNode(v). Any output may be NULL. */
+LPGPU_API lpgpu_status lpgpu_session_best_moves(lpgpu_session* s, int32_t* to, int32_t* gain,
+                                                uint8_t* border);
+
+/* Gain cache (initializeGainCache, partitioned_hypergraph.h:707-809):
+ * benefit[v] = moveFromBenefit(v), penalty[v*k+b] = moveToPenalty(v,b), so
+ * km1Gain(v,from,to) = benefit[v] - penalty[v*k+to] (h:682-688). */
+LPGPU_API lpgpu_status lpgpu_session_gain_cache(lpgpu_session* s, int32_t* benefit,
+                                                int32_t* penalty);
+
+/* Applies `count` moves concurrently on the device without balance checks,
+ * the curried PartitionedHypergraph::changeNodePart (h:566-572) with its
+ * updatePinCountOfHyperedge / km1Delta attribution (h:1133-1167,
+ * hypergraph_common.h:133-140). The vertices must be distinct and from[i]
+ * must be the current block of vertices[i] (else LPGPU_ERR_INVALID_ARG and
+ * nothing is applied). *delta receives the summed attributed objective delta. */
+LPGPU_API lpgpu_status lpgpu_session_apply_moves(lpgpu_session* s, int64_t count,
+                                                 const int32_t* vertices, const int32_t* from,
+                                                 const int32_t* to, int64_t* delta);
+
+/* Device memory held by the session, in bytes. */
+LPGPU_API lpgpu_status lpgpu_session_footprint(lpgpu_session* s, int64_t* bytes);
+
+/* Device bytes a session would need for (n, m, pins, k): the admission
+ * estimate used by the refine server. */
+LPGPU_API int64_t lpgpu_estimate_footprint(int64_t num_vertices, int64_t num_nets,
+                                           int64_t num_pins, int32_t k, int32_t subrounds);
+
+/* ------------------------------------------------------------- timing */
+
+/* Kernel-phase timing with CUDA events on the session stream. When enabled,
+ * every refine records, per named phase, the summed device time and launch
+ * count; lpgpu_session_phase_times returns up to max entries. */
+typedef struct {
+  char name[24];
+  int64_t launches;
+  double ms;
+} lpgpu_phase_time;
+
+LPGPU_API lpgpu_status lpgpu_session_enable_timing(lpgpu_session* s, int32_t enable);
+LPGPU_API lpgpu_status lpgpu_session_phase_times(lpgpu_session* s, lpgpu_phase_time* out,
+                                                 int32_t max, int32_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LPGPU_H_ */

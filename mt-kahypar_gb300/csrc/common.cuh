@@ -1,0 +1,157 @@
+// Internal declarations shared by the device translation units of liblpgpu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "lpgpu.h"
+
+namespace lpgpu {
+
+// Thread-local last-error text (lpgpu_last_error).
+void set_error(const std::string& msg);
+
+// Vertices of degree above this threshold are never border vertices
+// (PartitionedHypergraph::HIGH_DEGREE_THRESHOLD, partitioned_hypergraph.h:67).
+constexpr int64_t kHighDegree = 100000;
+
+// Sub-rounds are assigned per aligned chunk of 32 consecutive vertex ids.
+constexpr int kChunkShift = 5;
+constexpr int kMaxSubrounds = 64;
+
+// Sub-round of vertex v in round r: mix32((v >> 5) ^ (0x9E3779B9 * (r + 1))) % S.
+__host__ __device__ inline uint32_t mix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+__host__ __device__ inline int subround_of(int64_t v, int round, int S) {
+  if (S <= 1) return 0;
+  return (int)(mix32((uint32_t)(v >> kChunkShift) ^ (0x9E3779B9u * (uint32_t)(round + 1))) %
+               (uint32_t)S);
+}
+
+// Candidate ordering key: (gain, vertex) as one unsigned 64-bit integer.
+__host__ __device__ inline uint64_t move_key(int32_t gain, int32_t v) {
+  return ((uint64_t)((uint32_t)gain ^ 0x80000000u) << 32) | (uint32_t)v;
+}
+
+// Indices into the device scalar block.
+enum Scalar : int {
+  kDeltaSub = 0,   // summed attributed delta of the current sub-round
+  kAnyOverTo = 1,  // some target block overflows
+  kAnyOverFrom = 2,
+  kKm1 = 3,        // km1 accumulator (metrics)
+  kCut = 4,        // cut accumulator (metrics)
+  kError = 5,      // device-side error flag
+  kApplyDelta = 6, // apply_moves delta
+  kDeltaRb = 7,    // delta of a sub-round rollback
+  kScalars = 8
+};
+
+// Per-round statistics slots (lpgpu_round_stats order).
+enum Stat : int { kStActive = 0, kStPins, kStCands, kStMoved, kStReverted, kStDelta, kStats = 8 };
+
+// Device pointers of the round kernels.
+struct RoundCtx {
+  int64_t n, m;
+  int32_t k, W;
+  const int64_t* net_off;
+  const int32_t* pins;
+  const int64_t* vtx_off;
+  const int32_t* inets;
+  const int32_t* w_v;
+  const int32_t* w_e;
+  int32_t* part;
+  int32_t* phi;
+  uint32_t* conn;
+  int64_t* bw;
+  const int64_t* lmax;
+  const int64_t* perfect;
+  // active lists
+  int32_t* list;
+  int64_t* sub_off;      // S + 1 offsets into list
+  uint8_t* next_flag;    // n
+  int32_t* net_epoch;    // m
+  // per list position
+  int2* rec;             // (to, gain); to < 0: no candidate
+  uint8_t* status;       // 0 none, 1 moved, 2 reverted, 3 rolled back
+  // per block scratch
+  int64_t* in_w;         // candidate weight by target block (sweep)
+  int64_t* in_cnt;       // candidate count by target block (sweep)
+  int64_t* cand_out;     // candidate weight by source block (sweep)
+  int64_t* acc_w;        // target-accepted weight by source block
+  int64_t* acc_cnt;      // target-accepted count by source block
+  int64_t* seg_off;      // k + 1
+  int64_t* cursor;
+  uint64_t* thr_to;
+  uint64_t* thr_from;
+  uint8_t* over_to;
+  uint8_t* over_from;
+  uint64_t* seg_key;     // n
+  int32_t* seg_w;        // n
+  int64_t* scal;         // kScalars
+  int64_t* stats;        // rounds x kStats
+  // parameters
+  int32_t zero_gain, revert, rollback;
+  int64_t act_threshold;
+};
+
+// Launch helpers (lp_kernels.cu). All launch on `st`; none synchronizes.
+struct Launch {
+  cudaStream_t st;
+  int num_sms;
+};
+
+cudaError_t scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t count, int64_t* tmp,
+                               int64_t tmp_elems, cudaStream_t st);
+int64_t scan_tmp_elems(int64_t count);
+
+cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const int64_t* net_off,
+                                   const int32_t* pins, int64_t* vtx_off, int32_t* inets,
+                                   int64_t* cursor, int64_t* scan_tmp, int64_t scan_tmp_elems);
+cudaError_t launch_init_partition(const Launch& L, const RoundCtx& c);
+cudaError_t launch_metrics(const Launch& L, const RoundCtx& c);
+cudaError_t launch_best_moves(const Launch& L, const RoundCtx& c, int32_t* to, int32_t* gain,
+                              uint8_t* border);
+cudaError_t launch_gain_cache(const Launch& L, const RoundCtx& c, int32_t* benefit,
+                              int32_t* penalty);
+cudaError_t launch_apply_moves(const Launch& L, const RoundCtx& c, int64_t count,
+                               const int32_t* v, const int32_t* from, const int32_t* to);
+
+// Round phases (the sub-round pipeline). `timer` may be null.
+struct PhaseTimer;
+cudaError_t launch_mark_all(const Launch& L, const RoundCtx& c, int rebalancing);
+cudaError_t launch_mark_list(const Launch& L, const RoundCtx& c, const int32_t* nodes,
+                             int64_t count);
+cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int S,
+                              int64_t* tile_cnt, int64_t* tile_off, int64_t* scan_tmp,
+                              int64_t scan_tmp_elems, PhaseTimer* timer);
+cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int sub, int epoch,
+                            PhaseTimer* timer);
+
+// Optional per-phase CUDA-event timing.
+struct PhaseTimer {
+  struct Rec {
+    int phase;
+    cudaEvent_t a, b;
+  };
+  std::vector<std::string> names;
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  cudaStream_t st = nullptr;
+  int phase_id(const char* name);
+  void begin(int phase, cudaEvent_t* a);
+  void end(int phase, cudaEvent_t a);
+  void reset();
+  ~PhaseTimer();
+};
+
+}  // namespace lpgpu

@@ -1,0 +1,1178 @@
+// Device kernels of the label-propagation (km1) refinement path, sm_103a.
+//
+// All work is integer and memory bound; no tensor cores are involved. Kernels
+// use grid-stride loops over persistent grids sized to the SM count, read their
+// element counts from device memory (so a whole refine needs no host sync),
+// and privatize per-block accumulators in shared memory.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace lpgpu {
+
+#define FULLMASK 0xffffffffu
+
+using ull = unsigned long long;
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULLMASK, v, o);
+  return v;
+}
+
+// Block-wide sum of an int64 (any blockDim multiple of 32, <= 1024). All threads get the total.
+__device__ int64_t block_sum_i64(int64_t v) {
+  __shared__ int64_t ws[32];
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane_id() == 0) ws[w] = v;
+  __syncthreads();
+  int64_t t = lane_id() < nw ? ws[lane_id()] : 0;
+  t = warp_sum(t);
+  return t;
+}
+
+// Block-wide exclusive scan of an int64 (blockDim multiple of 32, <= 1024).
+__device__ int64_t block_scan_excl_i64(int64_t v, int64_t* total) {
+  __shared__ int64_t ws[32];
+  const int lane = lane_id(), w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  int64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(FULLMASK, x, o);
+    if (lane >= o) x += y;
+  }
+  __syncthreads();
+  if (lane == 31) ws[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int64_t s = lane < nw ? ws[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(FULLMASK, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < nw) ws[lane] = s;
+  }
+  __syncthreads();
+  const int64_t prefix = w > 0 ? ws[w - 1] : 0;
+  *total = ws[nw - 1];
+  return prefix + x - v;
+}
+
+static int blocks_per_sm_hint = 4;
+
+static int grid_for(const Launch& L, int64_t work_items, int threads, int per_sm = 0) {
+  const int64_t cap = (int64_t)L.num_sms * (per_sm > 0 ? per_sm : blocks_per_sm_hint);
+  const int64_t need = (work_items + threads - 1) / threads;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(cap, need));
+}
+
+// =================================================================== scan
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int64_t kScanTile = kScanThreads * kScanItems;
+
+__global__ void k_tile_sums(const int64_t* __restrict__ in, int64_t count, int64_t* __restrict__ sums) {
+  const int64_t base = blockIdx.x * kScanTile;
+  int64_t s = 0;
+  for (int i = threadIdx.x; i < kScanTile; i += kScanThreads) {
+    const int64_t g = base + i;
+    if (g < count) s += in[g];
+  }
+  s = block_sum_i64(s);
+  if (threadIdx.x == 0) sums[blockIdx.x] = s;
+}
+
+__global__ void k_scan_tiles(const int64_t* in, int64_t* out, int64_t count,
+                             const int64_t* __restrict__ tile_prefix) {
+  const int64_t base = blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  int64_t v[kScanItems];
+  int64_t s = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    v[j] = (base + j < count) ? in[base + j] : 0;
+    s += v[j];
+  }
+  int64_t total;
+  int64_t run = block_scan_excl_i64(s, &total) + (tile_prefix ? tile_prefix[blockIdx.x] : 0);
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    if (base + j < count) out[base + j] = run;
+    run += v[j];
+  }
+}
+
+int64_t scan_tmp_elems(int64_t count) {
+  const int64_t tiles = (count + kScanTile - 1) / kScanTile;
+  if (tiles <= 1) return 0;
+  return tiles + scan_tmp_elems(tiles);
+}
+
+cudaError_t scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t count, int64_t* tmp,
+                               int64_t tmp_elems, cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  const int64_t tiles = (count + kScanTile - 1) / kScanTile;
+  if (tiles == 1) {
+    k_scan_tiles<<<1, kScanThreads, 0, st>>>(in, out, count, nullptr);
+    return cudaGetLastError();
+  }
+  if (tmp_elems < scan_tmp_elems(count)) return cudaErrorInvalidValue;
+  int64_t* sums = tmp;
+  k_tile_sums<<<(unsigned)tiles, kScanThreads, 0, st>>>(in, count, sums);
+  cudaError_t e = scan_exclusive_i64(sums, sums, tiles, tmp + tiles, tmp_elems - tiles, st);
+  if (e != cudaSuccess) return e;
+  k_scan_tiles<<<(unsigned)tiles, kScanThreads, 0, st>>>(in, out, count, sums);
+  return cudaGetLastError();
+}
+
+// ============================================================ incidence
+
+__global__ void k_count_pins(const int32_t* __restrict__ pins, int64_t P, int64_t* __restrict__ cnt) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P;
+       i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(reinterpret_cast<ull*>(&cnt[pins[i]]), 1ull);
+}
+
+// Warp per net: every pin appends the net id to its vertex's incident-net list.
+__global__ void k_scatter_incidence(int64_t m, const int64_t* __restrict__ net_off,
+                                    const int32_t* __restrict__ pins, int64_t* __restrict__ cursor,
+                                    int32_t* __restrict__ inets) {
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < m; e += warps) {
+    const int64_t b = net_off[e], en = net_off[e + 1];
+    for (int64_t i = b + lane_id(); i < en; i += 32) {
+      const int64_t pos = (int64_t)atomicAdd(reinterpret_cast<ull*>(&cursor[pins[i]]), 1ull);
+      inets[pos] = (int32_t)e;
+    }
+  }
+}
+
+cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const int64_t* net_off,
+                                   const int32_t* pins, int64_t* vtx_off, int32_t* inets,
+                                   int64_t* cursor, int64_t* scan_tmp, int64_t scan_tmp_elems) {
+  int64_t P = 0;
+  cudaError_t e = cudaMemcpyAsync(&P, net_off + m, sizeof(int64_t), cudaMemcpyDeviceToHost, L.st);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(L.st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(vtx_off, 0, sizeof(int64_t) * (n + 1), L.st)) != cudaSuccess) return e;
+  if (P > 0) k_count_pins<<<grid_for(L, P, 256, 8), 256, 0, L.st>>>(pins, P, vtx_off);
+  if ((e = scan_exclusive_i64(vtx_off, vtx_off, n + 1, scan_tmp, scan_tmp_elems, L.st)) != cudaSuccess)
+    return e;
+  if ((e = cudaMemcpyAsync(cursor, vtx_off, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, L.st)) !=
+      cudaSuccess)
+    return e;
+  if (m > 0) k_scatter_incidence<<<grid_for(L, m * 32, 256, 8), 256, 0, L.st>>>(m, net_off, pins, cursor, inets);
+  return cudaGetLastError();
+}
+
+// ======================================================== partition init
+
+// c(V_b) = sum of w(v) over v in block b (initializeBlockWeights, h:1067-1084).
+__global__ void k_block_weights(RoundCtx c) {
+  extern __shared__ ull s_w[];
+  for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_w[b] = 0;
+  __syncthreads();
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < c.n;
+       v += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&s_w[c.part[v]], (ull)(int64_t)c.w_v[v]);
+  __syncthreads();
+  for (int b = threadIdx.x; b < c.k; b += blockDim.x)
+    if (s_w[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_w[b]);
+}
+
+// Φ and Λ from scratch, warp per net with a per-warp k-bin shared histogram
+// (initializePinCountInPart, h:1086-1110), fused with the km1 / cut sums.
+__global__ void k_pin_counts(RoundCtx c) {
+  extern __shared__ int s_hist[];
+  const int k = c.k, W = c.W;
+  int* hist = s_hist + (threadIdx.x >> 5) * k;
+  const int lane = lane_id();
+  for (int b = lane; b < k; b += 32) hist[b] = 0;
+  __syncwarp();
+  int64_t km1 = 0, cut = 0;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < c.m; e += warps) {
+    const int64_t b0 = c.net_off[e], b1 = c.net_off[e + 1];
+    for (int64_t i = b0 + lane; i < b1; i += 32) atomicAdd(&hist[c.part[c.pins[i]]], 1);
+    __syncwarp();
+    int lam = 0;
+    for (int w = 0; w < W; ++w) {
+      const int b = w * 32 + lane;
+      int cnt = 0;
+      if (b < k) {
+        cnt = hist[b];
+        hist[b] = 0;
+        c.phi[e * k + b] = cnt;
+      }
+      const unsigned bits = __ballot_sync(FULLMASK, cnt > 0);
+      if (lane == 0) c.conn[e * W + w] = bits;
+      lam += __popc(bits);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      const int64_t we = c.w_e[e];
+      km1 += (int64_t)(lam > 1 ? lam - 1 : 0) * we;
+      cut += lam > 1 ? we : 0;
+    }
+  }
+  km1 = block_sum_i64(km1);
+  cut = block_sum_i64(cut);
+  if (threadIdx.x == 0) {
+    atomicAdd(reinterpret_cast<ull*>(&c.scal[kKm1]), (ull)km1);
+    atomicAdd(reinterpret_cast<ull*>(&c.scal[kCut]), (ull)cut);
+  }
+}
+
+cudaError_t launch_init_partition(const Launch& L, const RoundCtx& c) {
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(c.bw, 0, sizeof(int64_t) * c.k, L.st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(c.scal, 0, sizeof(int64_t) * kScalars, L.st)) != cudaSuccess) return e;
+  if (c.n > 0)
+    k_block_weights<<<grid_for(L, c.n, 256), 256, sizeof(ull) * c.k, L.st>>>(c);
+  if (c.m > 0) {
+    const size_t smem = sizeof(int) * c.k * 8;
+    k_pin_counts<<<grid_for(L, c.m * 32, 256), 256, smem, L.st>>>(c);
+  }
+  return cudaGetLastError();
+}
+
+// metrics::km1 / hyperedgeCut (metrics.cpp:29-65): thread per net.
+__global__ void k_metrics(RoundCtx c) {
+  int64_t km1 = 0, cut = 0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < c.m;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int lam = 0;
+    for (int w = 0; w < c.W; ++w) lam += __popc(c.conn[e * c.W + w]);
+    const int64_t we = c.w_e[e];
+    km1 += (int64_t)(lam > 1 ? lam - 1 : 0) * we;
+    cut += lam > 1 ? we : 0;
+  }
+  km1 = block_sum_i64(km1);
+  cut = block_sum_i64(cut);
+  if (threadIdx.x == 0) {
+    atomicAdd(reinterpret_cast<ull*>(&c.scal[kKm1]), (ull)km1);
+    atomicAdd(reinterpret_cast<ull*>(&c.scal[kCut]), (ull)cut);
+  }
+}
+
+cudaError_t launch_metrics(const Launch& L, const RoundCtx& c) {
+  cudaError_t e = cudaMemsetAsync(c.scal + kKm1, 0, sizeof(int64_t) * 2, L.st);
+  if (e != cudaSuccess) return e;
+  if (c.m > 0) k_metrics<<<grid_for(L, c.m, 256), 256, 0, L.st>>>(c);
+  return cudaGetLastError();
+}
+
+// ============================================================ best move
+
+template <int W>
+__device__ __forceinline__ void load_words(const uint32_t* __restrict__ p, uint32_t (&w)[W]) {
+  if constexpr (W % 4 == 0) {
+#pragma unroll
+    for (int i = 0; i < W / 4; ++i) {
+      const uint4 q = __ldg(reinterpret_cast<const uint4*>(p) + i);
+      w[4 * i] = q.x; w[4 * i + 1] = q.y; w[4 * i + 2] = q.z; w[4 * i + 3] = q.w;
+    }
+  } else if constexpr (W == 2) {
+    const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
+    w[0] = q.x; w[1] = q.y;
+  } else {
+#pragma unroll
+    for (int i = 0; i < W; ++i) w[i] = __ldg(p + i);
+  }
+}
+
+struct BestMove {
+  int to;       // target block, == from when none
+  int gain;     // objective delta (< 0 improving, 0 zero-gain move or none)
+  bool border;
+};
+
+// Warp-cooperative Km1Policy::computeMaxGainMoveImpl (gain_policy.h:108-167,
+// disable_randomization) for vertex v, guarded by isBorderNode (h:605-620).
+// Lanes stride over the incident nets: each lane adds its nets' weights into
+// the per-warp shared penalty array `pen` (one int per block, all zero on
+// entry and on exit) for every block of Λ(e) other than `from`, and sums the
+// internal weight of nets with Φ(e, from) > 1. Lanes then stride over blocks
+// and the warp reduces (score, block) to the minimum score with the lowest
+// block id. Feasibility: bw[b] + w(v) <= lmax[b]. With zero_gain, a vertex
+// without an improving move takes the lowest-id feasible block of score 0 if
+// the rebalancing rule of label_propagation_refiner.h:88-95 holds.
+template <int W>
+__device__ __forceinline__ BestMove warp_best_move(const RoundCtx& c, int64_t v, int from,
+                                                   int wv, int* __restrict__ pen,
+                                                   const int64_t* __restrict__ bw,
+                                                   const int64_t* __restrict__ lmax,
+                                                   const int64_t* __restrict__ perfect,
+                                                   int zero_gain, int64_t* deg_out) {
+  const int lane = lane_id();
+  const int k = c.k;
+  const int64_t beg = c.vtx_off[v], end = c.vtx_off[v + 1];
+  *deg_out = end - beg;
+  BestMove r{from, 0, false};
+  if (end - beg > kHighDegree) return r;
+  int internal = 0;
+  bool border = false;
+  const int fw = from >> 5;
+  const uint32_t fbit = 1u << (from & 31);
+  for (int64_t j = beg + lane; j < end; j += 32) {
+    const int e = __ldg(&c.inets[j]);
+    const int we = __ldg(&c.w_e[e]);
+    if (__ldg(&c.phi[(int64_t)e * k + from]) > 1) internal += we;
+    uint32_t words[W];
+    load_words<W>(c.conn + (int64_t)e * W, words);
+    int lam = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      uint32_t bits = words[w];
+      lam += __popc(bits);
+      if (w == fw) bits &= ~fbit;
+      while (bits) {
+        const int t = __ffs(bits) - 1;
+        bits &= bits - 1;
+        atomicAdd(&pen[w * 32 + t], we);
+      }
+    }
+    border |= lam > 1;
+  }
+  border = __any_sync(FULLMASK, border);
+  r.border = border;
+  if (!border) return r;  // no block other than `from` was touched
+  internal = warp_sum(internal);
+  __syncwarp();
+  int best_s = INT_MAX, best_b = INT_MAX, zero_b = INT_MAX;
+  for (int b = lane; b < k; b += 32) {
+    const int pb = pen[b];
+    pen[b] = 0;
+    if (b == from || bw[b] + wv > lmax[b]) continue;
+    const int score = internal - pb;
+    if (score < best_s) { best_s = score; best_b = b; }
+    if (score == 0 && zero_b == INT_MAX) zero_b = b;
+  }
+  __syncwarp();
+  const int ms = __reduce_min_sync(FULLMASK, best_s);
+  if (ms < 0) {
+    r.to = __reduce_min_sync(FULLMASK, best_s == ms ? best_b : INT_MAX);
+    r.gain = ms;
+    return r;
+  }
+  if (zero_gain) {
+    const int zb = __reduce_min_sync(FULLMASK, zero_b);
+    if (zb != INT_MAX && bw[from] - 1 > bw[zb] + 1 && bw[zb] < perfect[zb]) r.to = zb;
+  }
+  return r;
+}
+
+// Best move of every vertex on the current state (parity / debug path).
+template <int W>
+__global__ void __launch_bounds__(256) k_best_moves(RoundCtx c, int32_t* to, int32_t* gain,
+                                                    uint8_t* border) {
+  extern __shared__ unsigned char smem_raw[];
+  int64_t* s_bw = reinterpret_cast<int64_t*>(smem_raw);
+  int64_t* s_lmax = s_bw + c.k;
+  int* pen = reinterpret_cast<int*>(s_lmax + c.k) + (threadIdx.x >> 5) * c.k;
+  for (int b = threadIdx.x; b < c.k; b += blockDim.x) { s_bw[b] = c.bw[b]; s_lmax[b] = c.lmax[b]; }
+  for (int b = lane_id(); b < c.k; b += 32) pen[b] = 0;
+  __syncthreads();
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; v < c.n; v += warps) {
+    const int from = c.part[v];
+    int64_t deg;
+    const BestMove bm = warp_best_move<W>(c, v, from, c.w_v[v], pen, s_bw, s_lmax, nullptr, 0, &deg);
+    if (lane_id() == 0) {
+      if (to) to[v] = bm.to;
+      if (gain) gain[v] = bm.gain;
+      if (border) border[v] = bm.border;
+    }
+  }
+}
+
+#define LPGPU_DISPATCH_W(W, ...)          \
+  switch (W) {                            \
+    case 1: { constexpr int kW = 1; __VA_ARGS__; } break;   \
+    case 2: { constexpr int kW = 2; __VA_ARGS__; } break;   \
+    case 4: { constexpr int kW = 4; __VA_ARGS__; } break;   \
+    case 8: { constexpr int kW = 8; __VA_ARGS__; } break;   \
+    case 16: { constexpr int kW = 16; __VA_ARGS__; } break; \
+    case 32: { constexpr int kW = 32; __VA_ARGS__; } break; \
+    default: return cudaErrorInvalidValue;                  \
+  }
+
+// Words per net rounded up to a template instance.
+static int word_class(int W) {
+  int w = 1;
+  while (w < W) w <<= 1;
+  return w;
+}
+
+cudaError_t launch_best_moves(const Launch& L, const RoundCtx& c, int32_t* to, int32_t* gain,
+                              uint8_t* border) {
+  if (c.n == 0) return cudaSuccess;
+  if (word_class(c.W) != c.W) return cudaErrorInvalidValue;
+  const size_t smem = sizeof(int64_t) * 2 * c.k + sizeof(int) * c.k * 8;
+  LPGPU_DISPATCH_W(c.W, {
+    auto kern = k_best_moves<kW>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grid_for(L, c.n * 32, 256), 256, smem, L.st>>>(c, to, gain, border);
+  });
+  return cudaGetLastError();
+}
+
+// ============================================================ gain cache
+
+// moveFromBenefit / moveToPenalty for every vertex (initializeGainCache,
+// h:707-809): warp per vertex with a per-warp k-bin shared aggregator.
+__global__ void __launch_bounds__(256) k_gain_cache(RoundCtx c, int32_t* benefit, int32_t* penalty) {
+  extern __shared__ int s_agg[];
+  int* agg = s_agg + (threadIdx.x >> 5) * c.k;
+  const int lane = lane_id();
+  for (int b = lane; b < c.k; b += 32) agg[b] = 0;
+  __syncwarp();
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; v < c.n; v += warps) {
+    const int pv = c.part[v];
+    int ben = 0, inc = 0;
+    for (int64_t j = c.vtx_off[v] + lane; j < c.vtx_off[v + 1]; j += 32) {
+      const int e = c.inets[j];
+      const int we = c.w_e[e];
+      if (c.phi[(int64_t)e * c.k + pv] == 1) ben += we;
+      inc += we;
+      for (int w = 0; w < c.W; ++w) {
+        uint32_t bits = c.conn[(int64_t)e * c.W + w];
+        while (bits) {
+          const int t = __ffs(bits) - 1;
+          bits &= bits - 1;
+          atomicAdd(&agg[w * 32 + t], we);
+        }
+      }
+    }
+    ben = warp_sum(ben);
+    inc = warp_sum(inc);
+    __syncwarp();
+    for (int b = lane; b < c.k; b += 32) {
+      penalty[v * c.k + b] = inc - agg[b];
+      agg[b] = 0;
+    }
+    if (lane == 0) benefit[v] = ben;
+    __syncwarp();
+  }
+}
+
+cudaError_t launch_gain_cache(const Launch& L, const RoundCtx& c, int32_t* benefit, int32_t* penalty) {
+  if (c.n == 0) return cudaSuccess;
+  const size_t smem = sizeof(int) * c.k * 8;
+  cudaFuncSetAttribute(k_gain_cache, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_gain_cache<<<grid_for(L, c.n * 32, 256), 256, smem, L.st>>>(c, benefit, penalty);
+  return cudaGetLastError();
+}
+
+// ================================================================ commit
+
+// Moves v from `f` to `t` on Φ and Λ: per incident net one atomic decrement of
+// Φ(e,f) and one atomic increment of Φ(e,t); Λ bits toggle on the 1->0 and
+// 0->1 transitions seen by the atomics (updatePinCountOfHyperedge,
+// h:1133-1167). Returns this lane's share of the attributed delta
+// (km1Delta, hypergraph_common.h:133-140): -w(e) when Φ(e,f) drops to 0,
+// +w(e) when Φ(e,t) rises to 1. The per-move split depends on interleaving;
+// the sum over all concurrent moves is exactly the km1 change.
+__device__ __forceinline__ int64_t warp_commit_vertex(const RoundCtx& c, int64_t v, int f, int t) {
+  int64_t att = 0;
+  const int k = c.k, W = c.W;
+  const uint32_t fbit = 1u << (f & 31), tbit = 1u << (t & 31);
+  for (int64_t j = c.vtx_off[v] + lane_id(); j < c.vtx_off[v + 1]; j += 32) {
+    const int64_t e = c.inets[j];
+    const int we = c.w_e[e];
+    const int of = atomicSub(&c.phi[e * k + f], 1);
+    if (of == 1) {
+      atomicXor(&c.conn[e * W + (f >> 5)], fbit);
+      att -= we;
+    }
+    const int ot = atomicAdd(&c.phi[e * k + t], 1);
+    if (ot == 0) {
+      atomicXor(&c.conn[e * W + (t >> 5)], tbit);
+      att += we;
+    }
+  }
+  return att;
+}
+
+// Concurrent application of an explicit move list (lpgpu_session_apply_moves).
+__global__ void k_apply_moves(RoundCtx c, int64_t count, const int32_t* __restrict__ vs,
+                              const int32_t* __restrict__ fs, const int32_t* __restrict__ ts) {
+  int64_t att = 0;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < count; i += warps) {
+    const int64_t v = vs[i];
+    const int f = fs[i], t = ts[i];
+    att += warp_commit_vertex(c, v, f, t);
+    if (lane_id() == 0) {
+      c.part[v] = t;
+      const int64_t wv = c.w_v[v];
+      atomicAdd(reinterpret_cast<ull*>(&c.bw[t]), (ull)wv);
+      atomicAdd(reinterpret_cast<ull*>(&c.bw[f]), (ull)(-wv));
+    }
+  }
+  att = block_sum_i64(att);
+  if (threadIdx.x == 0) atomicAdd(reinterpret_cast<ull*>(&c.scal[kApplyDelta]), (ull)att);
+}
+
+cudaError_t launch_apply_moves(const Launch& L, const RoundCtx& c, int64_t count, const int32_t* v,
+                               const int32_t* from, const int32_t* to) {
+  cudaError_t e = cudaMemsetAsync(c.scal + kApplyDelta, 0, sizeof(int64_t), L.st);
+  if (e != cudaSuccess) return e;
+  if (count > 0) k_apply_moves<<<grid_for(L, count * 32, 256), 256, 0, L.st>>>(c, count, v, from, to);
+  return cudaGetLastError();
+}
+
+// ========================================================= active lists
+
+constexpr int kTile = 1024;  // vertices per binning tile = 32 chunks of 32
+
+__global__ void k_mark_all(uint8_t* flag, int64_t n) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x)
+    flag[v] = 1;
+}
+
+// initializeActiveNodes without rebalancing: border vertices only.
+__global__ void k_mark_border(RoundCtx c) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < c.n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = c.vtx_off[v], e = c.vtx_off[v + 1];
+    uint8_t f = 0;
+    if (e - b <= kHighDegree) {
+      for (int64_t j = b; j < e && !f; ++j) {
+        int lam = 0;
+        for (int w = 0; w < c.W; ++w) lam += __popc(c.conn[(int64_t)c.inets[j] * c.W + w]);
+        f = lam > 1;
+      }
+    }
+    c.next_flag[v] = f;
+  }
+}
+
+__global__ void k_mark_list(uint8_t* flag, const int32_t* nodes, int64_t count) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x)
+    flag[nodes[i]] = 1;
+}
+
+cudaError_t launch_mark_all(const Launch& L, const RoundCtx& c, int rebalancing) {
+  if (c.n == 0) return cudaSuccess;
+  if (rebalancing)
+    k_mark_all<<<grid_for(L, c.n, 256), 256, 0, L.st>>>(c.next_flag, c.n);
+  else
+    k_mark_border<<<grid_for(L, c.n, 256), 256, 0, L.st>>>(c);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mark_list(const Launch& L, const RoundCtx& c, const int32_t* nodes, int64_t count) {
+  if (c.n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(c.next_flag, 0, c.n, L.st);
+  if (e != cudaSuccess) return e;
+  if (count > 0) k_mark_list<<<grid_for(L, count, 256), 256, 0, L.st>>>(c.next_flag, nodes, count);
+  return cudaGetLastError();
+}
+
+// Per tile, flagged vertices per sub-round (tile_cnt[s * tiles + tile]).
+// All 32 vertices of an aligned chunk share one sub-round.
+__global__ void __launch_bounds__(1024) k_bin_count(const uint8_t* __restrict__ flag, int64_t n,
+                                                    int round, int S, int64_t tiles,
+                                                    int64_t* __restrict__ tile_cnt) {
+  __shared__ int s_cnt[kMaxSubrounds];
+  if (threadIdx.x < S) s_cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t v = blockIdx.x * (int64_t)kTile + threadIdx.x;
+  const bool f = v < n && flag[v];
+  const unsigned bal = __ballot_sync(FULLMASK, f);
+  if (lane_id() == 0 && bal) atomicAdd(&s_cnt[subround_of(v, round, S)], __popc(bal));
+  __syncthreads();
+  if (threadIdx.x < S) tile_cnt[threadIdx.x * tiles + blockIdx.x] = s_cnt[threadIdx.x];
+}
+
+// Writes each sub-round's flagged vertices in increasing id order and clears
+// the flags. Sub-round s occupies list[tile_off[s * tiles] .. tile_off[(s+1) * tiles]).
+__global__ void __launch_bounds__(1024) k_bin_scatter(uint8_t* __restrict__ flag, int64_t n, int round,
+                                                      int S, int64_t tiles,
+                                                      const int64_t* __restrict__ tile_off,
+                                                      int32_t* __restrict__ list) {
+  __shared__ int s_cnt[32];
+  __shared__ int s_sub[32];
+  __shared__ int64_t s_base[32];
+  const int w = threadIdx.x >> 5;
+  const int64_t v = blockIdx.x * (int64_t)kTile + threadIdx.x;
+  const bool f = v < n && flag[v];
+  const unsigned bal = __ballot_sync(FULLMASK, f);
+  const int sub = subround_of(blockIdx.x * (int64_t)kTile + w * 32, round, S);
+  if (lane_id() == 0) { s_cnt[w] = __popc(bal); s_sub[w] = sub; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int64_t run[kMaxSubrounds];
+    for (int s = 0; s < S; ++s) run[s] = tile_off[s * tiles + blockIdx.x];
+    for (int i = 0; i < 32; ++i) { s_base[i] = run[s_sub[i]]; run[s_sub[i]] += s_cnt[i]; }
+  }
+  __syncthreads();
+  if (f) {
+    list[s_base[w] + __popc(bal & lanemask_lt())] = (int32_t)v;
+    flag[v] = 0;
+  }
+}
+
+__global__ void k_sub_offsets(const int64_t* __restrict__ tile_off, const int64_t* __restrict__ tile_cnt,
+                              int S, int64_t tiles, int64_t* __restrict__ sub_off) {
+  const int s = threadIdx.x;
+  if (s < S) sub_off[s] = tile_off[s * tiles];
+  if (s == 0) {
+    const int64_t last = (int64_t)S * tiles - 1;
+    sub_off[S] = tile_off[last] + tile_cnt[last];
+  }
+}
+
+// ================================================================= timer
+
+int PhaseTimer::phase_id(const char* name) {
+  for (size_t i = 0; i < names.size(); ++i)
+    if (names[i] == name) return (int)i;
+  names.emplace_back(name);
+  return (int)names.size() - 1;
+}
+void PhaseTimer::begin(int phase, cudaEvent_t* a) {
+  (void)phase;
+  if (used + 2 > pool.size()) {
+    for (int i = 0; i < 64; ++i) {
+      cudaEvent_t ev;
+      cudaEventCreate(&ev);
+      pool.push_back(ev);
+    }
+  }
+  *a = pool[used++];
+  cudaEventRecord(*a, st);
+}
+void PhaseTimer::end(int phase, cudaEvent_t a) {
+  cudaEvent_t b = pool[used++];
+  cudaEventRecord(b, st);
+  recs.push_back({phase, a, b});
+}
+void PhaseTimer::reset() {
+  recs.clear();
+  used = 0;
+}
+PhaseTimer::~PhaseTimer() {
+  for (auto ev : pool) cudaEventDestroy(ev);
+}
+
+struct Scope {
+  PhaseTimer* t;
+  int id;
+  cudaEvent_t a{};
+  Scope(PhaseTimer* tm, const char* name) : t(tm), id(tm ? tm->phase_id(name) : -1) {
+    if (t) t->begin(id, &a);
+  }
+  ~Scope() {
+    if (t) t->end(id, a);
+  }
+};
+
+cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int S,
+                              int64_t* tile_cnt, int64_t* tile_off, int64_t* scan_tmp,
+                              int64_t scan_tmp_elems, PhaseTimer* timer) {
+  Scope sc(timer, "bin_active");
+  const int64_t tiles = std::max<int64_t>(1, (c.n + kTile - 1) / kTile);
+  k_bin_count<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_cnt);
+  cudaError_t e = scan_exclusive_i64(tile_cnt, tile_off, S * tiles, scan_tmp, scan_tmp_elems, L.st);
+  if (e != cudaSuccess) return e;
+  k_bin_scatter<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_off, c.list);
+  k_sub_offsets<<<1, 64, 0, L.st>>>(tile_off, tile_cnt, S, tiles, c.sub_off);
+  return cudaGetLastError();
+}
+
+// ============================================================= sub-round
+
+constexpr int kSweepThreads = 256;
+
+// Sweep: best move of every active vertex of the sub-round on the current
+// state (moveVertex's isBorderNode + computeMaxGainMove,
+// label_propagation_refiner.h:82-95). Writes rec[pos] = (to, gain) or to = -1,
+// and per-block candidate totals (in_w / in_cnt by target, out_w by source).
+template <int W>
+__global__ void __launch_bounds__(kSweepThreads) k_sweep(RoundCtx c, int round, int sub) {
+  extern __shared__ unsigned char smem_raw[];
+  const int k = c.k;
+  int64_t* s_bw = reinterpret_cast<int64_t*>(smem_raw);
+  int64_t* s_lmax = s_bw + k;
+  int64_t* s_perf = s_lmax + k;
+  ull* s_in_w = reinterpret_cast<ull*>(s_perf + k);
+  ull* s_out_w = s_in_w + k;  // candidate weight by source block
+  unsigned* s_in_cnt = reinterpret_cast<unsigned*>(s_out_w + k);
+  int* pen = reinterpret_cast<int*>(s_in_cnt + k) + (threadIdx.x >> 5) * k;
+  for (int b = threadIdx.x; b < k; b += blockDim.x) {
+    s_bw[b] = c.bw[b];
+    s_lmax[b] = c.lmax[b];
+    s_perf[b] = c.perfect[b];
+    s_in_w[b] = 0;
+    s_out_w[b] = 0;
+    s_in_cnt[b] = 0;
+  }
+  for (int b = lane_id(); b < k; b += 32) pen[b] = 0;
+  __syncthreads();
+  const int64_t beg = c.sub_off[sub], cnt = c.sub_off[sub + 1] - beg;
+  int64_t pins = 0, cands = 0;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < cnt; i += warps) {
+    const int64_t pos = beg + i;
+    const int64_t v = c.list[pos];
+    const int from = c.part[v];
+    const int wv = c.w_v[v];
+    int64_t deg;
+    const BestMove bm = warp_best_move<W>(c, v, from, wv, pen, s_bw, s_lmax, s_perf, c.zero_gain, &deg);
+    if (lane_id() == 0) {
+      pins += deg;
+      int2 r = make_int2(-1, 0);
+      if (bm.to != from) {
+        r = make_int2(bm.to, bm.gain);
+        atomicAdd(&s_in_w[bm.to], (ull)(int64_t)wv);
+        atomicAdd(&s_in_cnt[bm.to], 1u);
+        atomicAdd(&s_out_w[from], (ull)(int64_t)wv);
+        ++cands;
+      }
+      c.rec[pos] = r;
+    }
+  }
+  pins = block_sum_i64(pins);
+  cands = block_sum_i64(cands);
+  if (threadIdx.x == 0) {
+    int64_t* st = c.stats + (int64_t)round * kStats;
+    atomicAdd(reinterpret_cast<ull*>(&st[kStPins]), (ull)pins);
+    atomicAdd(reinterpret_cast<ull*>(&st[kStCands]), (ull)cands);
+    if (blockIdx.x == 0) atomicAdd(reinterpret_cast<ull*>(&st[kStActive]), (ull)cnt);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < k; b += blockDim.x) {
+    if (s_in_cnt[b]) {
+      atomicAdd(reinterpret_cast<ull*>(&c.in_w[b]), s_in_w[b]);
+      atomicAdd(reinterpret_cast<ull*>(&c.in_cnt[b]), (ull)s_in_cnt[b]);
+    }
+    if (s_out_w[b]) atomicAdd(reinterpret_cast<ull*>(&c.cand_out[b]), s_out_w[b]);
+  }
+}
+
+// Plan of the target-side selection (one CTA, blockDim >= k): a block
+// overflows when the candidates into it weigh more than its slack; overflowing
+// blocks get a segment for their candidates. Also decides whether the
+// source-side check can be skipped: if, for every block, all candidates
+// leaving it weigh less than its weight, no block can become empty.
+__global__ void __launch_bounds__(1024) k_plan_to(RoundCtx c) {
+  const int b = threadIdx.x;
+  bool over = false, maybe_from = false;
+  int64_t cnt = 0;
+  if (b < c.k) {
+    over = c.in_w[b] > c.lmax[b] - c.bw[b];
+    maybe_from = c.cand_out[b] >= c.bw[b];
+    cnt = over ? c.in_cnt[b] : 0;
+    c.over_to[b] = over;
+    c.thr_to[b] = ~0ull;
+    c.thr_from[b] = ~0ull;
+    c.over_from[b] = 0;
+    c.acc_w[b] = 0;
+    c.acc_cnt[b] = 0;
+  }
+  int64_t total;
+  const int64_t off = block_scan_excl_i64(cnt, &total);
+  if (b < c.k) {
+    c.seg_off[b] = off;
+    c.cursor[b] = off;
+  }
+  const int any_over = __syncthreads_or(over);
+  const int any_from = __syncthreads_or(maybe_from);
+  if (b == 0) {
+    c.scal[kAnyOverTo] = any_over;
+    c.scal[kAnyOverFrom] = any_from;  // refined by k_plan_from
+    c.scal[kDeltaSub] = 0;
+    c.scal[kDeltaRb] = 0;
+  }
+}
+
+// Places the candidates of overflowing blocks into per-block segments.
+// by_from = 0: candidates grouped by target block;
+// by_from = 1: target-accepted candidates grouped by source block.
+__global__ void k_bin_moves(RoundCtx c, int sub, int by_from) {
+  if (c.scal[by_from ? kAnyOverFrom : kAnyOverTo] == 0) return;
+  const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
+  const uint8_t* over = by_from ? c.over_from : c.over_to;
+  for (int64_t base = beg + (blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane_id());
+       base < end; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pos = base + lane_id();
+    int grp = -1;
+    uint64_t key = 0;
+    int w = 0;
+    if (pos < end) {
+      const int2 r = c.rec[pos];
+      if (r.x >= 0) {
+        const int32_t v = c.list[pos];
+        key = move_key(r.y, v);
+        const int from = c.part[v];
+        if (!by_from) {
+          if (over[r.x]) grp = r.x;
+        } else if (key < c.thr_to[r.x] && over[from]) {
+          grp = from;
+        }
+        w = c.w_v[v];
+      }
+    }
+    // warp-aggregated segment allocation per group
+    const unsigned active = __ballot_sync(FULLMASK, grp >= 0);
+    if (grp >= 0) {
+      const unsigned peers = __match_any_sync(active, grp);
+      const int leader = __ffs(peers) - 1;
+      int64_t slot0 = 0;
+      if (lane_id() == leader)
+        slot0 = (int64_t)atomicAdd(reinterpret_cast<ull*>(&c.cursor[grp]), (ull)__popc(peers));
+      slot0 = __shfl_sync(peers, slot0, leader);
+      const int64_t slot = slot0 + __popc(peers & lanemask_lt());
+      c.seg_key[slot] = key;
+      c.seg_w[slot] = w;
+    }
+  }
+}
+
+// Gain-sorted prefix per block without sorting: radix selection (8 bits per
+// pass, most significant first) of the first key whose inclusive weighted
+// prefix exceeds the budget. Keys below the threshold are accepted. One CTA
+// per block; blocks that do not overflow exit.
+__global__ void __launch_bounds__(1024) k_select(RoundCtx c, int by_from) {
+  const int b = blockIdx.x;
+  const uint8_t* over = by_from ? c.over_from : c.over_to;
+  if (!over[b]) return;
+  __shared__ ull hist[256];
+  __shared__ uint64_t s_prefix, s_mask;
+  __shared__ int64_t s_budget;
+  const int64_t off = c.seg_off[b];
+  const int64_t cnt = (by_from ? c.acc_cnt[b] : c.in_cnt[b]);
+  const uint64_t* keys = c.seg_key + off;
+  const int32_t* ws = c.seg_w + off;
+  if (threadIdx.x == 0) {
+    s_prefix = 0;
+    s_mask = 0;
+    s_budget = by_from ? c.bw[b] - 1 : c.lmax[b] - c.bw[b];
+  }
+  for (int shift = 56; shift >= 0; shift -= 8) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    const uint64_t prefix = s_prefix, mask = s_mask;
+    for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+      const uint64_t key = keys[i];
+      if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255], (ull)(int64_t)ws[i]);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int64_t cum = 0, budget = s_budget;
+      int sel = 255;
+      for (int d = 0; d < 256; ++d) {
+        const int64_t h = (int64_t)hist[d];
+        if (cum + h > budget) { sel = d; break; }
+        cum += h;
+      }
+      s_prefix = prefix | ((uint64_t)sel << shift);
+      s_mask = mask | (255ull << shift);
+      s_budget = budget - cum;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) (by_from ? c.thr_from : c.thr_to)[b] = s_prefix;
+}
+
+// Weight and count of target-accepted moves per source block. Runs only when
+// the plan found a block that might become empty.
+__global__ void k_accept_out(RoundCtx c, int sub) {
+  if (c.scal[kAnyOverFrom] == 0) return;
+  extern __shared__ ull s_acc[];
+  ull* s_w = s_acc;
+  ull* s_n = s_acc + c.k;
+  for (int b = threadIdx.x; b < c.k; b += blockDim.x) { s_w[b] = 0; s_n[b] = 0; }
+  __syncthreads();
+  const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
+  for (int64_t pos = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pos < end;
+       pos += (int64_t)gridDim.x * blockDim.x) {
+    const int2 r = c.rec[pos];
+    if (r.x < 0) continue;
+    const int32_t v = c.list[pos];
+    if (move_key(r.y, v) < c.thr_to[r.x]) {
+      const int f = c.part[v];
+      atomicAdd(&s_w[f], (ull)(int64_t)c.w_v[v]);
+      atomicAdd(&s_n[f], 1ull);
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < c.k; b += blockDim.x) {
+    if (s_n[b]) {
+      atomicAdd(reinterpret_cast<ull*>(&c.acc_w[b]), s_w[b]);
+      atomicAdd(reinterpret_cast<ull*>(&c.acc_cnt[b]), s_n[b]);
+    }
+  }
+}
+
+// Plan of the source-side selection (one CTA): a block overflows when the
+// target-accepted moves leaving it would leave it empty (changeNodePart's
+// from_weight_after > 0, partitioned_hypergraph.h:551).
+__global__ void __launch_bounds__(1024) k_plan_from(RoundCtx c) {
+  if (c.scal[kAnyOverFrom] == 0) return;  // uniform across the CTA
+  const int b = threadIdx.x;
+  bool over = false;
+  int64_t cnt = 0;
+  if (b < c.k) {
+    over = c.bw[b] - c.acc_w[b] < 1;
+    cnt = over ? c.acc_cnt[b] : 0;
+    c.over_from[b] = over;
+  }
+  int64_t total;
+  const int64_t off = block_scan_excl_i64(cnt, &total);
+  if (b < c.k) {
+    c.seg_off[b] = off;
+    c.cursor[b] = off;
+  }
+  const int any = __syncthreads_or(over);
+  if (b == 0) c.scal[kAnyOverFrom] = any;
+}
+
+// Commit of the accepted moves (changeNodePart, h:539-563, without the
+// per-move weight check: the selection already guarantees both bounds).
+// Marks status[pos] = 1 for committed moves and overwrites rec[pos].y with
+// the source block (the gain is no longer needed).
+__global__ void k_commit(RoundCtx c, int round, int sub) {
+  extern __shared__ ull s_dw[];
+  for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_dw[b] = 0;
+  __syncthreads();
+  const int lane = lane_id();
+  const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
+  int64_t att = 0, moved = 0;
+  const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
+  for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
+       base += stride) {
+    const int64_t pos = base + lane;
+    int2 r = make_int2(-1, 0);
+    int32_t v = 0;
+    int f = 0;
+    bool acc = false;
+    if (pos < end) {
+      r = c.rec[pos];
+      if (r.x >= 0) {
+        v = c.list[pos];
+        f = c.part[v];
+        const uint64_t key = move_key(r.y, v);
+        acc = key < c.thr_to[r.x] && key < c.thr_from[f];
+        if (acc) c.rec[pos].y = f;
+      }
+      c.status[pos] = acc ? 1 : 0;
+    }
+    unsigned mask = __ballot_sync(FULLMASK, acc);
+    while (mask) {
+      const int j = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const int32_t vj = __shfl_sync(FULLMASK, v, j);
+      const int fj = __shfl_sync(FULLMASK, f, j);
+      const int tj = __shfl_sync(FULLMASK, r.x, j);
+      att += warp_commit_vertex(c, vj, fj, tj);
+      if (lane == 0) {
+        c.part[vj] = tj;
+        const int64_t wv = c.w_v[vj];
+        atomicAdd(&s_dw[tj], (ull)wv);
+        atomicAdd(&s_dw[fj], (ull)(-wv));
+        ++moved;
+      }
+    }
+  }
+  att = block_sum_i64(att);
+  moved = block_sum_i64(moved);
+  if (threadIdx.x == 0) {
+    atomicAdd(reinterpret_cast<ull*>(&c.scal[kDeltaSub]), (ull)att);
+    atomicAdd(reinterpret_cast<ull*>(&c.stats[(int64_t)round * kStats + kStMoved]), (ull)moved);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < c.k; b += blockDim.x)
+    if (s_dw[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_dw[b]);
+}
+
+// Hindsight check, evaluated for all committed moves on the post-commit state
+// before any is undone: a move from f to t is marked for revert (status 2)
+// when moving the vertex back to f now strictly improves km1. This is the
+// deterministic counterpart of the realised-gain check of moveVertex
+// (label_propagation_refiner.h:100-137).
+__global__ void k_revert_eval(RoundCtx c, int sub) {
+  const int lane = lane_id();
+  const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
+  const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
+  const int k = c.k, W = c.W;
+  for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
+       base += stride) {
+    const int64_t pos = base + lane;
+    const bool moved = pos < end && c.status[pos] == 1;
+    unsigned mask = __ballot_sync(FULLMASK, moved);
+    while (mask) {
+      const int j = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const int64_t pj = base + j;
+      const int64_t v = c.list[pj];
+      const int2 r = c.rec[pj];  // (to, from)
+      const int t = r.x, f = r.y;
+      const uint32_t fbit = 1u << (f & 31);
+      int score = 0;
+      for (int64_t q = c.vtx_off[v] + lane; q < c.vtx_off[v + 1]; q += 32) {
+        const int64_t e = c.inets[q];
+        const int we = c.w_e[e];
+        if (c.phi[e * k + t] > 1) score += we;
+        if (c.conn[e * W + (f >> 5)] & fbit) score -= we;
+      }
+      score = warp_sum(score);
+      if (lane == 0 && score < 0) c.status[pj] = 2;
+    }
+  }
+}
+
+// Undo of the moves marked 2 (revert) or, when the sub-round's delta is
+// positive, of all moves still marked 1 (rollback, status 3).
+__global__ void k_undo(RoundCtx c, int round, int sub, int rollback) {
+  if (rollback && c.scal[kDeltaSub] <= 0) return;
+  extern __shared__ ull s_dw[];
+  for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_dw[b] = 0;
+  __syncthreads();
+  const int lane = lane_id();
+  const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
+  const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
+  const uint8_t want = rollback ? 1 : 2;
+  int64_t att = 0, undone = 0;
+  for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
+       base += stride) {
+    const int64_t pos = base + lane;
+    const bool sel = pos < end && c.status[pos] == want;
+    unsigned mask = __ballot_sync(FULLMASK, sel);
+    while (mask) {
+      const int j = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const int64_t pj = base + j;
+      const int64_t v = c.list[pj];
+      const int2 r = c.rec[pj];  // (to, from)
+      att += warp_commit_vertex(c, v, r.x, r.y);
+      if (lane == 0) {
+        c.part[v] = r.y;
+        const int64_t wv = c.w_v[v];
+        atomicAdd(&s_dw[r.y], (ull)wv);
+        atomicAdd(&s_dw[r.x], (ull)(-wv));
+        if (rollback) c.status[pj] = 3;
+        ++undone;
+      }
+    }
+  }
+  att = block_sum_i64(att);
+  undone = block_sum_i64(undone);
+  if (threadIdx.x == 0) {
+    atomicAdd(reinterpret_cast<ull*>(&c.scal[rollback ? kDeltaRb : kDeltaSub]), (ull)att);
+    int64_t* st = c.stats + (int64_t)round * kStats;
+    atomicAdd(reinterpret_cast<ull*>(&st[kStMoved]), (ull)(-undone));
+    atomicAdd(reinterpret_cast<ull*>(&st[kStReverted]), (ull)undone);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < c.k; b += blockDim.x)
+    if (s_dw[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_dw[b]);
+}
+
+// Neighbour activation of the kept moves (moveVertex, label_propagation_refiner.h:112-128):
+// the vertex and the pins of its nets with |e| <= threshold become active for
+// the next round; each net is expanded once per round (epoch stamp).
+// CTA 0 also books the sub-round delta and clears the sweep accumulators.
+__global__ void k_activate(RoundCtx c, int round, int sub, int epoch) {
+  if (blockIdx.x == 0) {
+    if (threadIdx.x == 0) {
+      c.stats[(int64_t)round * kStats + kStDelta] += c.scal[kDeltaSub] + c.scal[kDeltaRb];
+    }
+    for (int b = threadIdx.x; b < c.k; b += blockDim.x) {
+      c.in_w[b] = 0;
+      c.in_cnt[b] = 0;
+      c.cand_out[b] = 0;
+    }
+  }
+  const int lane = lane_id();
+  const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
+  const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
+  for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
+       base += stride) {
+    const int64_t pos = base + lane;
+    const bool moved = pos < end && c.status[pos] == 1;
+    unsigned mask = __ballot_sync(FULLMASK, moved);
+    while (mask) {
+      const int j = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const int64_t v = c.list[base + j];
+      if (lane == 0) c.next_flag[v] = 1;
+      for (int64_t q = c.vtx_off[v] + lane; q < c.vtx_off[v + 1]; q += 32) {
+        const int64_t e = c.inets[q];
+        const int64_t b0 = c.net_off[e], b1 = c.net_off[e + 1];
+        if (b1 - b0 > c.act_threshold) continue;
+        if (atomicExch(&c.net_epoch[e], epoch) == epoch) continue;
+        for (int64_t p = b0; p < b1; ++p) c.next_flag[c.pins[p]] = 1;
+      }
+    }
+  }
+}
+
+static int occupancy(const void* kern, int threads, size_t smem) {
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, threads, smem) != cudaSuccess ||
+      blocks < 1)
+    blocks = 1;
+  return blocks;
+}
+
+cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int sub, int epoch,
+                            PhaseTimer* timer) {
+  const int k = c.k;
+  const int64_t n = c.n;
+  if (word_class(c.W) != c.W) return cudaErrorInvalidValue;
+  {
+    Scope sc(timer, "sweep");
+    const size_t smem = sizeof(int64_t) * 5 * k + sizeof(unsigned) * k +
+                        sizeof(int) * k * (kSweepThreads / 32);
+    LPGPU_DISPATCH_W(c.W, {
+      auto kern = k_sweep<kW>;
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      const int per_sm = occupancy((const void*)kern, kSweepThreads, smem);
+      kern<<<grid_for(L, n * 32, kSweepThreads, per_sm), kSweepThreads, smem, L.st>>>(c, round, sub);
+    });
+  }
+  const int g = grid_for(L, n, 256, 4);
+  {
+    Scope sc(timer, "select");
+    k_plan_to<<<1, 1024, 0, L.st>>>(c);
+    k_bin_moves<<<g, 256, 0, L.st>>>(c, sub, 0);
+    k_select<<<k, 1024, 0, L.st>>>(c, 0);
+    k_accept_out<<<g, 256, sizeof(ull) * 2 * k, L.st>>>(c, sub);
+    k_plan_from<<<1, 1024, 0, L.st>>>(c);
+    k_bin_moves<<<g, 256, 0, L.st>>>(c, sub, 1);
+    k_select<<<k, 1024, 0, L.st>>>(c, 1);
+  }
+  {
+    Scope sc(timer, "commit");
+    k_commit<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub);
+  }
+  if (c.revert) {
+    Scope sc(timer, "revert");
+    k_revert_eval<<<g, 256, 0, L.st>>>(c, sub);
+    k_undo<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub, 0);
+  }
+  if (c.rollback) {
+    Scope sc(timer, "rollback");
+    k_undo<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub, 1);
+  }
+  {
+    Scope sc(timer, "activate");
+    k_activate<<<g, 256, 0, L.st>>>(c, round, sub, epoch);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace lpgpu

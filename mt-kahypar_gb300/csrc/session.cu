@@ -1,0 +1,777 @@
+// Session management and the C ABI of liblpgpu (declared in include/lpgpu.h).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace lpgpu {
+
+static thread_local std::string g_error;
+void set_error(const std::string& msg) { g_error = msg; }
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t count = 0;
+  cudaError_t alloc(size_t n, int64_t* footprint) {
+    if (n == count && p) return cudaSuccess;
+    release(footprint);
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    count = n;
+    *footprint += (int64_t)(n * sizeof(T));
+    return cudaSuccess;
+  }
+  void release(int64_t* footprint) {
+    if (p) {
+      cudaFree(p);
+      *footprint -= (int64_t)(count * sizeof(T));
+    }
+    p = nullptr;
+    count = 0;
+  }
+};
+
+static int word_count(int k) { return (k + 31) / 32; }
+static int word_class_of(int k) {
+  int w = 1;
+  while (w < word_count(k)) w <<= 1;
+  return w;
+}
+
+static lpgpu_status cuda_fail(cudaError_t e, const char* what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  cudaGetLastError();  // clear sticky-free errors
+  if (e == cudaErrorMemoryAllocation) return LPGPU_ERR_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ||
+      e == cudaErrorNoKernelImageForDevice || e == cudaErrorInvalidDevice)
+    return LPGPU_ERR_NO_DEVICE;
+  return LPGPU_ERR_CUDA;
+}
+
+static lpgpu_status invalid(const std::string& msg) {
+  set_error(msg);
+  return LPGPU_ERR_INVALID_ARG;
+}
+
+}  // namespace lpgpu
+
+using namespace lpgpu;
+
+#define CK(expr)                                   \
+  do {                                             \
+    cudaError_t _e = (expr);                       \
+    if (_e != cudaSuccess) return cuda_fail(_e, #expr); \
+  } while (0)
+
+struct lpgpu_session_s {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  int num_sms = 1;
+  int64_t footprint = 0;
+  // hypergraph
+  bool has_hg = false;
+  int64_t n = 0, m = 0, P = 0;
+  int64_t total_vw = 0;
+  DevBuf<int64_t> net_off, vtx_off;
+  DevBuf<int32_t> pins, inets, w_v, w_e;
+  // partition
+  bool has_part = false;
+  int32_t k = 0, W = 0;
+  DevBuf<int32_t> part, phi;
+  DevBuf<uint32_t> conn;
+  DevBuf<int64_t> bw, lmax, perfect;
+  std::vector<int64_t> h_perfect;
+  // refine scratch
+  DevBuf<int32_t> list, net_epoch, seg_w;
+  DevBuf<int64_t> sub_off, blk64, scal, stats, tile_cnt, tile_off, scan_tmp;
+  DevBuf<uint8_t> next_flag, status, over;
+  DevBuf<int2> rec;
+  DevBuf<uint64_t> seg_key, thr;
+  int64_t scan_tmp_n = 0;
+  int epoch = 0;
+  // results of the last refine
+  std::vector<lpgpu_round_stats> last_stats;
+  // timing
+  bool timing = false;
+  PhaseTimer timer;
+  std::vector<lpgpu_phase_time> phase_times;
+
+  Launch launch() const { return Launch{st, num_sms}; }
+
+  RoundCtx ctx(const lpgpu_config* cfg = nullptr) {
+    RoundCtx c{};
+    c.n = n;
+    c.m = m;
+    c.k = k;
+    c.W = W;
+    c.net_off = net_off.p;
+    c.pins = pins.p;
+    c.vtx_off = vtx_off.p;
+    c.inets = inets.p;
+    c.w_v = w_v.p;
+    c.w_e = w_e.p;
+    c.part = part.p;
+    c.phi = phi.p;
+    c.conn = conn.p;
+    c.bw = bw.p;
+    c.lmax = lmax.p;
+    c.perfect = perfect.p;
+    c.list = list.p;
+    c.sub_off = sub_off.p;
+    c.next_flag = next_flag.p;
+    c.net_epoch = net_epoch.p;
+    c.rec = rec.p;
+    c.status = status.p;
+    int64_t* b = blk64.p;
+    if (b) {
+      c.in_w = b;
+      c.in_cnt = b + k;
+      c.cand_out = b + 2 * k;
+      c.acc_w = b + 3 * k;
+      c.acc_cnt = b + 4 * k;
+      c.seg_off = b + 5 * k;
+      c.cursor = b + 6 * k + 1;
+    }
+    if (thr.p) {
+      c.thr_to = thr.p;
+      c.thr_from = thr.p + k;
+    }
+    if (over.p) {
+      c.over_to = over.p;
+      c.over_from = over.p + k;
+    }
+    c.seg_key = seg_key.p;
+    c.seg_w = seg_w.p;
+    c.scal = scal.p;
+    c.stats = stats.p;
+    if (cfg) {
+      c.zero_gain = cfg->rebalancing ? 1 : 0;
+      c.revert = cfg->revert;
+      c.rollback = cfg->rollback;
+      c.act_threshold = cfg->activation_threshold <= 0 ? INT64_MAX : cfg->activation_threshold;
+    }
+    return c;
+  }
+
+  void release_partition() {
+    part.release(&footprint);
+    phi.release(&footprint);
+    conn.release(&footprint);
+    bw.release(&footprint);
+    lmax.release(&footprint);
+    perfect.release(&footprint);
+    blk64.release(&footprint);
+    thr.release(&footprint);
+    over.release(&footprint);
+    has_part = false;
+  }
+  void release_all() {
+    release_partition();
+    DevBuf<int64_t>* b64[] = {&net_off, &vtx_off, &sub_off, &scal, &stats, &tile_cnt, &tile_off, &scan_tmp};
+    for (auto* b : b64) b->release(&footprint);
+    DevBuf<int32_t>* b32[] = {&pins, &inets, &w_v, &w_e, &list, &net_epoch, &seg_w};
+    for (auto* b : b32) b->release(&footprint);
+    next_flag.release(&footprint);
+    status.release(&footprint);
+    rec.release(&footprint);
+    seg_key.release(&footprint);
+    has_hg = false;
+  }
+};
+
+namespace {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+int64_t tiles_for(int64_t n) { return std::max<int64_t>(1, (n + 1023) / 1024); }
+
+lpgpu_status validate_csr(int64_t n, int64_t m, const int64_t* net_off, const int32_t* pins,
+                          const int32_t* w_v, const int32_t* w_e, int64_t* total_vw) {
+  if (n < 0 || m < 0) return invalid("negative vertex or net count");
+  if (n > INT32_MAX || m > INT32_MAX) return invalid("vertex and net ids must fit int32");
+  if (!net_off || (m > 0 && net_off[m] > 0 && !pins)) return invalid("null CSR pointer");
+  if (net_off[0] != 0) return invalid("net_offsets[0] must be 0");
+  int64_t gain_bound = 0;
+  for (int64_t e = 0; e < m; ++e) {
+    const int64_t sz = net_off[e + 1] - net_off[e];
+    if (sz < 0) return invalid("net_offsets must be non-decreasing");
+    if (w_e && w_e[e] < 0) return invalid("net weights must be >= 0");
+    gain_bound += sz * (w_e ? (int64_t)w_e[e] : 1);
+  }
+  if (gain_bound > INT32_MAX)
+    return invalid("sum of |e| * w(e) exceeds int32: gains would overflow the reference's Gain type");
+  const int64_t P = net_off[m];
+  for (int64_t i = 0; i < P; ++i)
+    if (pins[i] < 0 || pins[i] >= n) return invalid("pin id out of range");
+  // duplicate pins inside a net are not allowed (the reference's construct
+  // assumes a set); checked with a stamp array
+  {
+    std::vector<int32_t> stamp(n, -1);
+    for (int64_t e = 0; e < m; ++e)
+      for (int64_t i = net_off[e]; i < net_off[e + 1]; ++i) {
+        if (stamp[pins[i]] == (int32_t)e) return invalid("duplicate pin inside a net");
+        stamp[pins[i]] = (int32_t)e;
+      }
+  }
+  int64_t tw = 0;
+  for (int64_t v = 0; v < n; ++v) {
+    const int64_t w = w_v ? w_v[v] : 1;
+    if (w < 0) return invalid("vertex weights must be >= 0");
+    tw += w;
+  }
+  *total_vw = tw;
+  return LPGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void lpgpu_config_default(lpgpu_config* cfg) {
+  if (!cfg) return;
+  cfg->rounds = 5;
+  cfg->activation_threshold = 100;
+  cfg->rebalancing = 1;
+  cfg->subrounds = 16;
+  cfg->revert = 1;
+  cfg->rollback = 1;
+  cfg->reserved0 = 0;
+  cfg->reserved1 = 0;
+}
+
+const char* lpgpu_status_string(lpgpu_status s) {
+  switch (s) {
+    case LPGPU_OK: return "ok";
+    case LPGPU_ERR_INVALID_ARG: return "invalid argument";
+    case LPGPU_ERR_OOM: return "out of device memory";
+    case LPGPU_ERR_ADMISSION: return "admission rejected";
+    case LPGPU_ERR_TIMEOUT: return "device wait timed out";
+    case LPGPU_ERR_CUDA: return "CUDA error";
+    case LPGPU_ERR_NO_DEVICE: return "no usable CUDA device";
+    case LPGPU_ERR_STATE: return "invalid call order";
+  }
+  return "unknown status";
+}
+
+const char* lpgpu_last_error(void) { return g_error.c_str(); }
+
+lpgpu_status lpgpu_session_create(int32_t device, lpgpu_session** out) {
+  if (!out) return invalid("null output pointer");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    set_error(std::string("no CUDA device: ") + cudaGetErrorString(e));
+    cudaGetLastError();
+    return LPGPU_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= count) return invalid("device index out of range");
+  DeviceGuard g(device);
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, device));
+  auto* s = new lpgpu_session_s();
+  s->device = device;
+  s->num_sms = prop.multiProcessorCount;
+  e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete s;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  s->timer.st = s->st;
+  if ((e = s->scal.alloc(kScalars, &s->footprint)) != cudaSuccess) {
+    cudaStreamDestroy(s->st);
+    delete s;
+    return cuda_fail(e, "alloc scalars");
+  }
+  *out = s;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_destroy(lpgpu_session* s) {
+  if (!s) return LPGPU_OK;
+  {
+    DeviceGuard g(s->device);
+    cudaStreamSynchronize(s->st);
+    s->release_all();
+    s->scal.release(&s->footprint);
+    cudaStreamDestroy(s->st);
+  }
+  delete s;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_upload(lpgpu_session* s, int64_t n, int64_t m, const int64_t* net_off,
+                                  const int32_t* pins, const int32_t* w_v, const int32_t* w_e) {
+  if (!s) return invalid("null session");
+  int64_t total = 0;
+  lpgpu_status vs = validate_csr(n, m, net_off, pins, w_v, w_e, &total);
+  if (vs != LPGPU_OK) return vs;
+  DeviceGuard g(s->device);
+  CK(cudaStreamSynchronize(s->st));
+  s->release_all();
+  s->n = n;
+  s->m = m;
+  s->P = net_off[m];
+  s->total_vw = total;
+  int64_t* fp = &s->footprint;
+  const int64_t P = s->P;
+  CK(s->net_off.alloc(m + 1, fp));
+  CK(s->vtx_off.alloc(n + 1, fp));
+  CK(s->pins.alloc(P, fp));
+  CK(s->inets.alloc(P, fp));
+  CK(s->w_v.alloc(n, fp));
+  CK(s->w_e.alloc(m, fp));
+  CK(s->net_epoch.alloc(m, fp));
+  CK(s->list.alloc(n, fp));
+  CK(s->next_flag.alloc(n, fp));
+  CK(s->status.alloc(n, fp));
+  CK(s->rec.alloc(n, fp));
+  CK(s->seg_key.alloc(n, fp));
+  CK(s->seg_w.alloc(n, fp));
+  CK(s->sub_off.alloc(kMaxSubrounds + 1, fp));
+  const int64_t tiles = tiles_for(n);
+  CK(s->tile_cnt.alloc(kMaxSubrounds * tiles, fp));
+  CK(s->tile_off.alloc(kMaxSubrounds * tiles, fp));
+  s->scan_tmp_n = std::max<int64_t>(1, std::max(scan_tmp_elems(n + 1), scan_tmp_elems(kMaxSubrounds * tiles)));
+  CK(s->scan_tmp.alloc(s->scan_tmp_n, fp));
+  cudaStream_t st = s->st;
+  CK(cudaMemcpyAsync(s->net_off.p, net_off, sizeof(int64_t) * (m + 1), cudaMemcpyHostToDevice, st));
+  if (P > 0) CK(cudaMemcpyAsync(s->pins.p, pins, sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
+  if (n > 0) {
+    if (w_v) {
+      CK(cudaMemcpyAsync(s->w_v.p, w_v, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+    } else {
+      std::vector<int32_t> ones(n, 1);
+      CK(cudaMemcpyAsync(s->w_v.p, ones.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+    }
+    CK(cudaMemsetAsync(s->next_flag.p, 0, n, st));
+  }
+  if (m > 0) {
+    if (w_e) {
+      CK(cudaMemcpyAsync(s->w_e.p, w_e, sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
+    } else {
+      std::vector<int32_t> ones(m, 1);
+      CK(cudaMemcpyAsync(s->w_e.p, ones.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+    }
+    CK(cudaMemsetAsync(s->net_epoch.p, 0, sizeof(int32_t) * m, st));
+  }
+  s->epoch = 0;
+  CK(launch_build_incidence(s->launch(), n, m, s->net_off.p, s->pins.p, s->vtx_off.p, s->inets.p,
+                            reinterpret_cast<int64_t*>(s->seg_key.p), s->scan_tmp.p, s->scan_tmp_n));
+  CK(cudaStreamSynchronize(st));
+  s->has_hg = true;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_set_partition(lpgpu_session* s, int32_t k, double eps,
+                                         const int32_t* partition, const int64_t* max_w,
+                                         const int64_t* perfect_w) {
+  if (!s) return invalid("null session");
+  if (!s->has_hg) {
+    set_error("set_partition before upload");
+    return LPGPU_ERR_STATE;
+  }
+  if (k < 1 || k > LPGPU_MAX_K) return invalid("k must be in [1, 1024]");
+  if (s->n > 0 && !partition) return invalid("null partition");
+  for (int64_t v = 0; v < s->n; ++v)
+    if (partition[v] < 0 || partition[v] >= k) return invalid("block id out of range");
+  std::vector<int64_t> hp(k), hl(k);
+  // Context::setupPartWeights (context.cpp:237-250)
+  const int64_t perfect = (int64_t)std::ceil((double)s->total_vw / (double)k);
+  const int64_t lmax = (int64_t)((1.0 + eps) * (double)perfect);
+  for (int b = 0; b < k; ++b) {
+    hp[b] = perfect_w ? perfect_w[b] : perfect;
+    hl[b] = max_w ? max_w[b] : lmax;
+    if (hp[b] < 1) hp[b] = 1;
+  }
+  DeviceGuard g(s->device);
+  CK(cudaStreamSynchronize(s->st));
+  s->release_partition();
+  s->k = k;
+  s->W = word_class_of(k);
+  int64_t* fp = &s->footprint;
+  CK(s->part.alloc(s->n, fp));
+  CK(s->phi.alloc((size_t)s->m * k, fp));
+  CK(s->conn.alloc((size_t)s->m * s->W, fp));
+  CK(s->bw.alloc(k, fp));
+  CK(s->lmax.alloc(k, fp));
+  CK(s->perfect.alloc(k, fp));
+  CK(s->blk64.alloc(7 * k + 1, fp));
+  CK(s->thr.alloc(2 * k, fp));
+  CK(s->over.alloc(2 * k, fp));
+  cudaStream_t st = s->st;
+  if (s->n > 0) CK(cudaMemcpyAsync(s->part.p, partition, sizeof(int32_t) * s->n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(s->lmax.p, hl.data(), sizeof(int64_t) * k, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(s->perfect.p, hp.data(), sizeof(int64_t) * k, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(s->blk64.p, 0, sizeof(int64_t) * (7 * k + 1), st));
+  RoundCtx c = s->ctx();
+  CK(launch_init_partition(s->launch(), c));
+  CK(cudaStreamSynchronize(st));
+  s->h_perfect = hp;
+  s->has_part = true;
+  return LPGPU_OK;
+}
+
+static lpgpu_status read_metrics(lpgpu_session* s, int64_t* km1, int64_t* cut) {
+  RoundCtx c = s->ctx();
+  CK(launch_metrics(s->launch(), c));
+  int64_t h[2];
+  CK(cudaMemcpyAsync(h, s->scal.p + kKm1, sizeof(h), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  if (km1) *km1 = h[0];
+  if (cut) *cut = h[1];
+  return LPGPU_OK;
+}
+
+static lpgpu_status read_imbalance(lpgpu_session* s, double* imb) {
+  std::vector<int64_t> w(s->k);
+  CK(cudaMemcpyAsync(w.data(), s->bw.p, sizeof(int64_t) * s->k, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  // metrics::imbalance (metrics.cpp:114-128)
+  double mx = (double)w[0] / (double)s->h_perfect[0];
+  for (int b = 1; b < s->k; ++b) mx = std::max(mx, (double)w[b] / (double)s->h_perfect[b]);
+  *imb = mx - 1.0;
+  return LPGPU_OK;
+}
+
+static lpgpu_status need_part(lpgpu_session* s) {
+  if (!s) return invalid("null session");
+  if (!s->has_part) {
+    set_error("no partition set");
+    return LPGPU_ERR_STATE;
+  }
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
+                                  const int32_t* nodes, int64_t num_nodes, lpgpu_result* result) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  lpgpu_config cfg;
+  if (cfg_in) cfg = *cfg_in; else lpgpu_config_default(&cfg);
+  if (cfg.rounds < 0) return invalid("rounds must be >= 0");
+  if (cfg.subrounds < 1 || cfg.subrounds > kMaxSubrounds) return invalid("subrounds must be in [1, 64]");
+  if (num_nodes < 0 || (num_nodes > 0 && !nodes)) return invalid("bad refinement node list");
+  for (int64_t i = 0; i < num_nodes; ++i)
+    if (nodes[i] < 0 || nodes[i] >= s->n) return invalid("refinement node out of range");
+  DeviceGuard g(s->device);
+  const int R = cfg.rounds, S = cfg.subrounds;
+  int64_t* fp = &s->footprint;
+  CK(s->stats.alloc(std::max(1, R) * kStats, fp));
+  cudaStream_t st = s->st;
+  CK(cudaMemsetAsync(s->stats.p, 0, sizeof(int64_t) * std::max(1, R) * kStats, st));
+  CK(cudaMemsetAsync(s->blk64.p, 0, sizeof(int64_t) * (7 * s->k + 1), st));
+  int64_t km1_before = 0;
+  lpgpu_status ms = read_metrics(s, &km1_before, nullptr);
+  if (ms != LPGPU_OK) return ms;
+  RoundCtx c = s->ctx(&cfg);
+  const Launch L = s->launch();
+  DevBuf<int32_t> dnodes;
+  int64_t tmpfp = 0;
+  if (num_nodes > 0) {
+    CK(dnodes.alloc(num_nodes, &tmpfp));
+    CK(cudaMemcpyAsync(dnodes.p, nodes, sizeof(int32_t) * num_nodes, cudaMemcpyHostToDevice, st));
+    CK(launch_mark_list(L, c, dnodes.p, num_nodes));
+  } else {
+    if (s->n > 0) CK(cudaMemsetAsync(s->next_flag.p, 0, s->n, st));
+    CK(launch_mark_all(L, c, cfg.rebalancing));
+  }
+  PhaseTimer* tm = s->timing ? &s->timer : nullptr;
+  if (tm) tm->reset();
+  for (int r = 0; r < R; ++r) {
+    CK(launch_bin_active(L, c, r, S, s->tile_cnt.p, s->tile_off.p, s->scan_tmp.p, s->scan_tmp_n, tm));
+    ++s->epoch;
+    for (int sub = 0; sub < S; ++sub) CK(launch_subround(L, c, r, sub, s->epoch, tm));
+  }
+  // drop flags left by the last round
+  if (s->n > 0) CK(cudaMemsetAsync(s->next_flag.p, 0, s->n, st));
+  std::vector<int64_t> hs(std::max(1, R) * kStats);
+  CK(cudaMemcpyAsync(hs.data(), s->stats.p, sizeof(int64_t) * hs.size(), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  dnodes.release(&tmpfp);
+  if (tm) {
+    std::map<int, lpgpu_phase_time> acc;
+    for (auto& rec : tm->recs) {
+      float ms_ = 0.f;
+      cudaEventElapsedTime(&ms_, rec.a, rec.b);
+      auto& a = acc[rec.phase];
+      a.launches += 1;
+      a.ms += ms_;
+    }
+    s->phase_times.clear();
+    for (auto& kv : acc) {
+      lpgpu_phase_time t = kv.second;
+      std::memset(t.name, 0, sizeof(t.name));
+      std::strncpy(t.name, tm->names[kv.first].c_str(), sizeof(t.name) - 1);
+      s->phase_times.push_back(t);
+    }
+  }
+  s->last_stats.clear();
+  int executed = 0;
+  bool stopped = false;
+  int64_t delta = 0, moves = 0, pins = 0;
+  for (int r = 0; r < R; ++r) {
+    const int64_t* x = &hs[r * kStats];
+    if (x[kStActive] == 0) stopped = true;
+    if (stopped) continue;
+    lpgpu_round_stats rs{x[kStActive], x[kStPins], x[kStCands], x[kStMoved], x[kStReverted], x[kStDelta]};
+    s->last_stats.push_back(rs);
+    ++executed;
+    delta += rs.delta;
+    moves += rs.moved;
+    pins += rs.pins;
+  }
+  if (result) {
+    int64_t km1_after = 0;
+    ms = read_metrics(s, &km1_after, nullptr);
+    if (ms != LPGPU_OK) return ms;
+    double imb = 0;
+    ms = read_imbalance(s, &imb);
+    if (ms != LPGPU_OK) return ms;
+    result->km1_before = km1_before;
+    result->km1_after = km1_after;
+    result->delta = delta;
+    result->moves = moves;
+    result->pins_processed = pins;
+    result->rounds = executed;
+    result->improved = delta < 0;
+    result->imbalance = imb;
+  }
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_round_stats(lpgpu_session* s, lpgpu_round_stats* out, int32_t max_rounds,
+                                       int32_t* rounds) {
+  if (!s) return invalid("null session");
+  const int cnt = (int)std::min<size_t>(s->last_stats.size(), (size_t)std::max(0, max_rounds));
+  for (int i = 0; i < cnt; ++i) out[i] = s->last_stats[i];
+  if (rounds) *rounds = (int32_t)s->last_stats.size();
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_get_partition(lpgpu_session* s, int32_t* partition) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  DeviceGuard g(s->device);
+  if (s->n > 0) CK(cudaMemcpyAsync(partition, s->part.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_metrics(lpgpu_session* s, int64_t* km1, int64_t* cut, double* imbalance) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  DeviceGuard g(s->device);
+  ps = read_metrics(s, km1, cut);
+  if (ps != LPGPU_OK) return ps;
+  if (imbalance) return read_imbalance(s, imbalance);
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_get_block_weights(lpgpu_session* s, int64_t* weights) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  DeviceGuard g(s->device);
+  CK(cudaMemcpyAsync(weights, s->bw.p, sizeof(int64_t) * s->k, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_get_pin_counts(lpgpu_session* s, int32_t* pc) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  DeviceGuard g(s->device);
+  if (s->m > 0)
+    CK(cudaMemcpyAsync(pc, s->phi.p, sizeof(int32_t) * s->m * s->k, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_get_connectivity(lpgpu_session* s, uint32_t* words) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  DeviceGuard g(s->device);
+  const int wc = word_count(s->k);
+  if (s->m > 0) {
+    // device rows have W >= wc words; copy the first wc of every row
+    CK(cudaMemcpy2DAsync(words, sizeof(uint32_t) * wc, s->conn.p, sizeof(uint32_t) * s->W,
+                         sizeof(uint32_t) * wc, s->m, cudaMemcpyDeviceToHost, s->st));
+  }
+  CK(cudaStreamSynchronize(s->st));
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_get_incidence(lpgpu_session* s, int64_t* vtx_off, int32_t* inets) {
+  if (!s) return invalid("null session");
+  if (!s->has_hg) {
+    set_error("no hypergraph uploaded");
+    return LPGPU_ERR_STATE;
+  }
+  DeviceGuard g(s->device);
+  if (vtx_off) CK(cudaMemcpyAsync(vtx_off, s->vtx_off.p, sizeof(int64_t) * (s->n + 1), cudaMemcpyDeviceToHost, s->st));
+  if (inets && s->P > 0) CK(cudaMemcpyAsync(inets, s->inets.p, sizeof(int32_t) * s->P, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_best_moves(lpgpu_session* s, int32_t* to, int32_t* gain, uint8_t* border) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  DeviceGuard g(s->device);
+  int64_t fp = 0;
+  DevBuf<int32_t> dto, dgain;
+  DevBuf<uint8_t> dborder;
+  CK(dto.alloc(s->n, &fp));
+  CK(dgain.alloc(s->n, &fp));
+  CK(dborder.alloc(s->n, &fp));
+  RoundCtx c = s->ctx();
+  CK(launch_best_moves(s->launch(), c, dto.p, dgain.p, dborder.p));
+  if (s->n > 0) {
+    if (to) CK(cudaMemcpyAsync(to, dto.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
+    if (gain) CK(cudaMemcpyAsync(gain, dgain.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
+    if (border) CK(cudaMemcpyAsync(border, dborder.p, s->n, cudaMemcpyDeviceToHost, s->st));
+  }
+  CK(cudaStreamSynchronize(s->st));
+  dto.release(&fp);
+  dgain.release(&fp);
+  dborder.release(&fp);
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_gain_cache(lpgpu_session* s, int32_t* benefit, int32_t* penalty) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  DeviceGuard g(s->device);
+  int64_t fp = 0;
+  DevBuf<int32_t> db, dp;
+  CK(db.alloc(s->n, &fp));
+  CK(dp.alloc((size_t)s->n * s->k, &fp));
+  RoundCtx c = s->ctx();
+  CK(launch_gain_cache(s->launch(), c, db.p, dp.p));
+  if (s->n > 0) {
+    if (benefit) CK(cudaMemcpyAsync(benefit, db.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
+    if (penalty) CK(cudaMemcpyAsync(penalty, dp.p, sizeof(int32_t) * s->n * s->k, cudaMemcpyDeviceToHost, s->st));
+  }
+  CK(cudaStreamSynchronize(s->st));
+  db.release(&fp);
+  dp.release(&fp);
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_apply_moves(lpgpu_session* s, int64_t count, const int32_t* vs,
+                                       const int32_t* fs, const int32_t* ts, int64_t* delta) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  if (count < 0 || (count > 0 && (!vs || !fs || !ts))) return invalid("bad move list");
+  DeviceGuard g(s->device);
+  std::vector<int32_t> part(s->n);
+  if (s->n > 0) {
+    CK(cudaMemcpyAsync(part.data(), s->part.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+  }
+  std::vector<uint8_t> seen(s->n, 0);
+  for (int64_t i = 0; i < count; ++i) {
+    if (vs[i] < 0 || vs[i] >= s->n) return invalid("move vertex out of range");
+    if (ts[i] < 0 || ts[i] >= s->k || fs[i] < 0 || fs[i] >= s->k) return invalid("move block out of range");
+    if (fs[i] == ts[i]) return invalid("move with from == to");
+    if (part[vs[i]] != fs[i]) return invalid("move source is not the vertex's current block");
+    if (seen[vs[i]]) return invalid("vertex moved twice in one batch");
+    seen[vs[i]] = 1;
+  }
+  int64_t fp = 0;
+  DevBuf<int32_t> dv, df, dt;
+  CK(dv.alloc(count, &fp));
+  CK(df.alloc(count, &fp));
+  CK(dt.alloc(count, &fp));
+  if (count > 0) {
+    CK(cudaMemcpyAsync(dv.p, vs, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(df.p, fs, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(dt.p, ts, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s->st));
+  }
+  RoundCtx c = s->ctx();
+  CK(launch_apply_moves(s->launch(), c, count, dv.p, df.p, dt.p));
+  int64_t d = 0;
+  CK(cudaMemcpyAsync(&d, s->scal.p + kApplyDelta, sizeof(int64_t), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  dv.release(&fp);
+  df.release(&fp);
+  dt.release(&fp);
+  if (delta) *delta = d;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_footprint(lpgpu_session* s, int64_t* bytes) {
+  if (!s || !bytes) return invalid("null pointer");
+  *bytes = s->footprint;
+  return LPGPU_OK;
+}
+
+int64_t lpgpu_estimate_footprint(int64_t n, int64_t m, int64_t P, int32_t k, int32_t subrounds) {
+  (void)subrounds;
+  const int64_t W = word_class_of(std::max(1, k));
+  const int64_t tiles = tiles_for(n);
+  int64_t b = 0;
+  b += 8 * (m + 1) + 8 * (n + 1) + 4 * P * 2 + 4 * n + 4 * m;          // CSR + weights
+  b += 4 * m + 4 * n + n + n + 8 * n + 8 * n + 4 * n;                  // epoch, list, flags, status, rec, seg
+  b += 8 * (kMaxSubrounds + 1) + 2 * 8 * kMaxSubrounds * tiles;        // sub-round bins
+  b += 8 * (scan_tmp_elems(std::max(n + 1, kMaxSubrounds * tiles)) + 1);
+  b += 4 * n + 4 * m * (int64_t)k + 4 * m * W;                         // part, Φ, Λ
+  b += 8 * (3 * k + 7 * k + 1 + 2 * k) + 2 * k + 8 * 64 + 8 * 8;       // per-block, stats, scalars
+  return b;
+}
+
+lpgpu_status lpgpu_session_enable_timing(lpgpu_session* s, int32_t enable) {
+  if (!s) return invalid("null session");
+  s->timing = enable != 0;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_phase_times(lpgpu_session* s, lpgpu_phase_time* out, int32_t max,
+                                       int32_t* count) {
+  if (!s) return invalid("null session");
+  const int cnt = (int)std::min<size_t>(s->phase_times.size(), (size_t)std::max(0, max));
+  for (int i = 0; i < cnt; ++i) out[i] = s->phase_times[i];
+  if (count) *count = (int32_t)s->phase_times.size();
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_refine_km1(int64_t n, int64_t m, const int64_t* net_off, const int32_t* pins,
+                              const int32_t* w_v, const int32_t* w_e, int32_t k, double eps,
+                              int32_t* part, const lpgpu_config* cfg, lpgpu_result* result) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    dev = 0;
+  }
+  lpgpu_session* s = nullptr;
+  lpgpu_status st = lpgpu_session_create(dev, &s);
+  if (st != LPGPU_OK) return st;
+  if ((st = lpgpu_session_upload(s, n, m, net_off, pins, w_v, w_e)) == LPGPU_OK &&
+      (st = lpgpu_session_set_partition(s, k, eps, part, nullptr, nullptr)) == LPGPU_OK &&
+      (st = lpgpu_session_refine(s, cfg, nullptr, 0, result)) == LPGPU_OK)
+    st = lpgpu_session_get_partition(s, part);
+  lpgpu_session_destroy(s);
+  return st;
+}
+
+}  // extern "C"

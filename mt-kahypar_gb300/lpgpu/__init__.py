@@ -1,0 +1,258 @@
+"""lpgpu: GB300-native label-propagation (km1) refinement behind a C ABI.
+
+This module is a thin ctypes binding of ``liblpgpu.so`` (declared in
+``include/lpgpu.h``). It loads the in-tree library and raises if it is
+missing: there is no CPU fallback anywhere in the product path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblpgpu.so")
+
+I64P = ctypes.POINTER(ctypes.c_int64)
+I32P = ctypes.POINTER(ctypes.c_int32)
+U32P = ctypes.POINTER(ctypes.c_uint32)
+U8P = ctypes.POINTER(ctypes.c_uint8)
+
+OK, ERR_INVALID_ARG, ERR_OOM, ERR_ADMISSION, ERR_TIMEOUT, ERR_CUDA, ERR_NO_DEVICE, ERR_STATE = range(8)
+MAX_K = 1024
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("rounds", ctypes.c_int32), ("activation_threshold", ctypes.c_int32),
+                ("rebalancing", ctypes.c_int32), ("subrounds", ctypes.c_int32),
+                ("revert", ctypes.c_int32), ("rollback", ctypes.c_int32),
+                ("reserved0", ctypes.c_int32), ("reserved1", ctypes.c_int32)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("km1_before", ctypes.c_int64), ("km1_after", ctypes.c_int64),
+                ("delta", ctypes.c_int64), ("moves", ctypes.c_int64),
+                ("pins_processed", ctypes.c_int64), ("rounds", ctypes.c_int32),
+                ("improved", ctypes.c_int32), ("imbalance", ctypes.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class RoundStats(ctypes.Structure):
+    _fields_ = [("active", ctypes.c_int64), ("pins", ctypes.c_int64),
+                ("candidates", ctypes.c_int64), ("moved", ctypes.c_int64),
+                ("reverted", ctypes.c_int64), ("delta", ctypes.c_int64)]
+
+
+class PhaseTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 24), ("launches", ctypes.c_int64), ("ms", ctypes.c_double)]
+
+
+class LpgpuError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"lpgpu status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+# exported C symbols (every declaration of include/lpgpu.h)
+SYMBOLS = [
+    "lpgpu_config_default", "lpgpu_status_string", "lpgpu_last_error", "lpgpu_refine_km1",
+    "lpgpu_session_create", "lpgpu_session_destroy", "lpgpu_session_upload",
+    "lpgpu_session_set_partition", "lpgpu_session_refine", "lpgpu_session_round_stats",
+    "lpgpu_session_get_partition", "lpgpu_session_metrics", "lpgpu_session_get_block_weights",
+    "lpgpu_session_get_pin_counts", "lpgpu_session_get_connectivity",
+    "lpgpu_session_get_incidence", "lpgpu_session_best_moves", "lpgpu_session_gain_cache",
+    "lpgpu_session_apply_moves", "lpgpu_session_footprint", "lpgpu_estimate_footprint",
+    "lpgpu_session_enable_timing", "lpgpu_session_phase_times",
+]
+
+
+def lib():
+    """Loads liblpgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run build() first (no CPU fallback exists)")
+        L = ctypes.CDLL(LIB_PATH)
+        L.lpgpu_last_error.restype = ctypes.c_char_p
+        L.lpgpu_status_string.restype = ctypes.c_char_p
+        L.lpgpu_estimate_footprint.restype = ctypes.c_int64
+        L.lpgpu_estimate_footprint.argtypes = [ctypes.c_int64] * 3 + [ctypes.c_int32] * 2
+        _lib = L
+    return _lib
+
+
+def _check(status):
+    if status != OK:
+        msg = lib().lpgpu_last_error().decode(errors="replace")
+        raise LpgpuError(status, msg)
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def default_config(**over) -> Config:
+    c = Config()
+    lib().lpgpu_config_default(ctypes.byref(c))
+    for k, v in over.items():
+        setattr(c, k, int(v))
+    return c
+
+
+class Session:
+    """Device-resident hypergraph + partition state (one CUDA stream)."""
+
+    def __init__(self, device: int = 0):
+        self._h = ctypes.c_void_p()
+        _check(lib().lpgpu_session_create(ctypes.c_int32(device), ctypes.byref(self._h)))
+        self.n = self.m = self.k = 0
+
+    def close(self):
+        if self._h:
+            lib().lpgpu_session_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, hg):
+        self.n, self.m = int(hg.n), int(hg.m)
+        self._keep = (np.ascontiguousarray(hg.net_off, np.int64), np.ascontiguousarray(hg.pins, np.int32),
+                      np.ascontiguousarray(hg.w_v, np.int32), np.ascontiguousarray(hg.w_e, np.int32))
+        no, pi, wv, we = self._keep
+        _check(lib().lpgpu_session_upload(self._h, ctypes.c_int64(self.n), ctypes.c_int64(self.m),
+                                          _p(no, I64P), _p(pi, I32P), _p(wv, I32P), _p(we, I32P)))
+        self._keep = None
+        return self
+
+    def set_partition(self, k, part, eps=0.03, lmax=None, perfect=None):
+        self.k = int(k)
+        p = np.ascontiguousarray(part, np.int32)
+        lm = None if lmax is None else np.ascontiguousarray(lmax, np.int64)
+        pf = None if perfect is None else np.ascontiguousarray(perfect, np.int64)
+        _check(lib().lpgpu_session_set_partition(self._h, ctypes.c_int32(k), ctypes.c_double(eps),
+                                                 _p(p, I32P), _p(lm, I64P), _p(pf, I64P)))
+        return self
+
+    def refine(self, cfg: Config = None, nodes=None) -> Result:
+        r = Result()
+        nd = None if nodes is None else np.ascontiguousarray(nodes, np.int32)
+        _check(lib().lpgpu_session_refine(self._h, None if cfg is None else ctypes.byref(cfg),
+                                          _p(nd, I32P), ctypes.c_int64(0 if nd is None else len(nd)),
+                                          ctypes.byref(r)))
+        return r
+
+    def round_stats(self):
+        buf = (RoundStats * 256)()
+        cnt = ctypes.c_int32()
+        _check(lib().lpgpu_session_round_stats(self._h, buf, 256, ctypes.byref(cnt)))
+        return [{f: getattr(buf[i], f) for f, _ in RoundStats._fields_} for i in range(min(256, cnt.value))]
+
+    def partition(self):
+        out = np.empty(self.n, np.int32)
+        _check(lib().lpgpu_session_get_partition(self._h, _p(out, I32P)))
+        return out
+
+    def metrics(self):
+        km1, cut, imb = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
+        _check(lib().lpgpu_session_metrics(self._h, ctypes.byref(km1), ctypes.byref(cut), ctypes.byref(imb)))
+        return km1.value, cut.value, imb.value
+
+    def block_weights(self):
+        out = np.empty(self.k, np.int64)
+        _check(lib().lpgpu_session_get_block_weights(self._h, _p(out, I64P)))
+        return out
+
+    def pin_counts(self):
+        out = np.empty(self.m * self.k, np.int32)
+        _check(lib().lpgpu_session_get_pin_counts(self._h, _p(out, I32P)))
+        return out.reshape(self.m, self.k)
+
+    def connectivity(self):
+        W = (self.k + 31) // 32
+        out = np.empty(self.m * W, np.uint32)
+        _check(lib().lpgpu_session_get_connectivity(self._h, _p(out, U32P)))
+        return out.reshape(self.m, W)
+
+    def incidence(self, num_pins):
+        vo = np.empty(self.n + 1, np.int64)
+        ie = np.empty(num_pins, np.int32)
+        _check(lib().lpgpu_session_get_incidence(self._h, _p(vo, I64P), _p(ie, I32P)))
+        return vo, ie
+
+    def best_moves(self):
+        to = np.empty(self.n, np.int32)
+        gain = np.empty(self.n, np.int32)
+        border = np.empty(self.n, np.uint8)
+        _check(lib().lpgpu_session_best_moves(self._h, _p(to, I32P), _p(gain, I32P), _p(border, U8P)))
+        return to, gain, border.astype(bool)
+
+    def gain_cache(self):
+        b = np.empty(self.n, np.int32)
+        p = np.empty(self.n * self.k, np.int32)
+        _check(lib().lpgpu_session_gain_cache(self._h, _p(b, I32P), _p(p, I32P)))
+        return b, p.reshape(self.n, self.k)
+
+    def apply_moves(self, vertices, from_, to):
+        v = np.ascontiguousarray(vertices, np.int32)
+        f = np.ascontiguousarray(from_, np.int32)
+        t = np.ascontiguousarray(to, np.int32)
+        d = ctypes.c_int64()
+        _check(lib().lpgpu_session_apply_moves(self._h, ctypes.c_int64(len(v)), _p(v, I32P), _p(f, I32P),
+                                               _p(t, I32P), ctypes.byref(d)))
+        return d.value
+
+    def footprint(self):
+        b = ctypes.c_int64()
+        _check(lib().lpgpu_session_footprint(self._h, ctypes.byref(b)))
+        return b.value
+
+    def enable_timing(self, on=True):
+        _check(lib().lpgpu_session_enable_timing(self._h, ctypes.c_int32(1 if on else 0)))
+
+    def phase_times(self):
+        buf = (PhaseTime * 64)()
+        cnt = ctypes.c_int32()
+        _check(lib().lpgpu_session_phase_times(self._h, buf, 64, ctypes.byref(cnt)))
+        return {buf[i].name.decode(): (buf[i].launches, buf[i].ms) for i in range(min(64, cnt.value))}
+
+
+def refine_km1(hg, k, part, eps=0.03, cfg: Config = None):
+    """One-shot lpgpu_refine_km1 on host buffers; returns (new partition, Result)."""
+    p = np.array(part, np.int32, copy=True)
+    r = Result()
+    no = np.ascontiguousarray(hg.net_off, np.int64)
+    pi = np.ascontiguousarray(hg.pins, np.int32)
+    wv = np.ascontiguousarray(hg.w_v, np.int32)
+    we = np.ascontiguousarray(hg.w_e, np.int32)
+    _check(lib().lpgpu_refine_km1(ctypes.c_int64(hg.n), ctypes.c_int64(hg.m), _p(no, I64P), _p(pi, I32P),
+                                  _p(wv, I32P), _p(we, I32P), ctypes.c_int32(k), ctypes.c_double(eps),
+                                  _p(p, I32P), None if cfg is None else ctypes.byref(cfg), ctypes.byref(r)))
+    return p, r
+
+
+def estimate_footprint(n, m, pins, k, subrounds=16):
+    return int(lib().lpgpu_estimate_footprint(n, m, pins, k, subrounds))
+
+
+def build(force=False):
+    """Compiles liblpgpu.so in-tree (see mt-kahypar_gb300/build.py)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_lpgpu_build", os.path.join(os.path.dirname(HERE), "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)

@@ -1,0 +1,273 @@
+"""Device path vs the CPU oracle, bit-exact (integer work: no tolerance).
+
+Every test goes through the C ABI (liblpgpu.so via ctypes)."""
+import numpy as np
+import pytest
+
+from conftest import load_golden, seven_vertex_fixture
+
+pytestmark = pytest.mark.gpu
+
+INF = np.iinfo(np.int32).max
+GOLDEN = ["twocenters", "contracted_unweighted_ibm01", "contracted_ibm01",
+          "hypergraph_with_node_and_edge_weights", "karate_club.graph", "test_instance",
+          "powersim.mtx"]
+
+
+def session(lp, hg, k, part, lmax=None, perfect=None, eps=0.03):
+    s = lp.Session(0)
+    s.upload(hg)
+    s.set_partition(k, part, eps=eps, lmax=lmax, perfect=perfect)
+    return s
+
+
+def check_state(orc, s, hg, k, part):
+    phi, conn, bw = orc.init_partition(hg, k, part)
+    assert np.array_equal(s.pin_counts(), phi)
+    assert np.array_equal(s.connectivity(), conn)
+    assert np.array_equal(s.block_weights(), bw)
+    km1, cut = orc.metrics(hg, k, conn)
+    dk, dc, _ = s.metrics()
+    assert (dk, dc) == (km1, cut)
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_golden_state_and_moves(lp, orc, name):
+    hg, d = load_golden(name)
+    for k in (2, 3, 8):
+        part = d[f"k{k}_part"]
+        s = session(lp, hg, k, part, lmax=d[f"k{k}_lmax"], perfect=d[f"k{k}_perfect"])
+        assert np.array_equal(s.pin_counts(), d[f"k{k}_phi"])
+        assert np.array_equal(s.connectivity(), d[f"k{k}_conn"])
+        assert np.array_equal(s.block_weights(), d[f"k{k}_bw"])
+        km1, cut, _ = s.metrics()
+        assert (km1, cut) == (int(d[f"k{k}_km1"]), int(d[f"k{k}_cut"]))
+        to, gain, border = s.best_moves()
+        assert np.array_equal(to, d[f"k{k}_to"])
+        assert np.array_equal(gain, d[f"k{k}_gain"])
+        assert np.array_equal(border, d[f"k{k}_border"])
+        ben, pen = s.gain_cache()
+        assert np.array_equal(ben, d[f"k{k}_benefit"])
+        assert np.array_equal(pen, d[f"k{k}_penalty"])
+        cfg = lp.default_config(rounds=5, subrounds=4, revert=1, rollback=1, rebalancing=1)
+        r = s.refine(cfg)
+        assert np.array_equal(s.partition(), d[f"k{k}_lp_part"])
+        stats = s.round_stats()
+        assert [st["delta"] for st in stats] == d[f"k{k}_lp_delta"].tolist()
+        assert r.km1_after == r.km1_before + r.delta
+        s.close()
+
+
+def test_incidence_matches_stable_transpose(lp, orc):
+    from lpgpu import gen
+    inst = gen.plain_small(seed=1)
+    hg = inst.hg
+    s = session(lp, hg, inst.k, inst.part)
+    vo, ie = s.incidence(hg.num_pins)
+    assert np.array_equal(vo, hg.vtx_off)
+    for v in range(hg.n):
+        a, b = vo[v], vo[v + 1]
+        assert np.array_equal(np.sort(ie[a:b]), hg.inets[a:b])
+    s.close()
+
+
+KM1_CASES = [
+    (2, [1, 0, 0, 0, 0, 1, 1], 0, (0, -2)),
+    (2, [0, 0, 0, 1, 0, 1, 1], 3, (0, -1)),
+    (2, [0, 0, 0, 0, 0, 1, 1], 4, (0, 0)),
+    (4, [0, 1, 2, 3, 3, 1, 2], 0, (1, -1)),
+    (4, [0, 3, 1, 2, 2, 0, 3], 6, (0, -1)),
+    (4, [0, 3, 1, 2, 2, 0, 3], 3, (2, 0)),
+]
+
+
+@pytest.mark.parametrize("k,part,v,expected", KM1_CASES)
+def test_km1_policy_known_answers_on_device(lp, k, part, v, expected):
+    """gain_policy_test.cc:63-276 through the C ABI."""
+    hg = seven_vertex_fixture()
+    s = session(lp, hg, k, np.array(part, np.int32), lmax=np.full(k, INF, np.int64))
+    to, gain, _ = s.best_moves()
+    assert (to[v], gain[v]) == expected
+    s.close()
+
+
+@pytest.mark.parametrize("moves,delta", [
+    ([(0, 1, 0)], -2),
+    ([(3, 1, 0)], -1),
+])
+def test_km1_delta_known_answers_on_device(lp, moves, delta):
+    hg = seven_vertex_fixture()
+    part = [1, 0, 0, 0, 0, 1, 1] if moves[0][0] == 0 else [0, 0, 0, 1, 0, 1, 1]
+    s = session(lp, hg, 2, np.array(part, np.int32))
+    v, f, t = zip(*moves)
+    assert s.apply_moves(v, f, t) == delta
+    s.close()
+
+
+CONCURRENT = [
+    [(0, 0, 1), (3, 1, 2), (2, 0, 2), (5, 2, 1), (6, 2, 0), (4, 1, 2)],
+    [(0, 0, 1), (1, 0, 2)],
+    [(3, 1, 2), (6, 2, 0)],
+    [(0, 0, 1), (2, 0, 2), (4, 1, 0), (6, 2, 1), (1, 0, 2), (3, 1, 0), (5, 2, 1)],
+    [(0, 0, 1), (3, 1, 0), (6, 2, 0), (1, 0, 2), (2, 0, 1), (4, 1, 0), (5, 2, 1)],
+]
+
+
+@pytest.mark.parametrize("moves", CONCURRENT)
+def test_concurrent_moves_on_device(lp, orc, moves):
+    """partitioned_hypergraph_test.cc:181-378: moves applied concurrently on the
+    device give the pin counts, connectivity sets and part weights of the
+    sequential oracle, and the attributed delta equals the km1 change."""
+    hg = seven_vertex_fixture()
+    base = np.array([0, 0, 0, 1, 1, 2, 2], np.int32)
+    s = session(lp, hg, 3, base)
+    km0 = s.metrics()[0]
+    v, f, t = zip(*moves)
+    d = s.apply_moves(v, f, t)
+    p = base.copy()
+    p[list(v)] = list(t)
+    check_state(orc, s, hg, 3, p)
+    assert np.array_equal(s.partition(), p)
+    assert s.metrics()[0] == km0 + d
+    s.close()
+
+
+@pytest.mark.parametrize("seed", range(8))
+@pytest.mark.parametrize("k", [1, 2, 3, 31, 32, 33, 64, 100, 128, 200, 1024])
+def test_random_state_and_best_moves(lp, orc, seed, k):
+    from lpgpu import gen
+    inst = gen.random_small(seed, n=300, m=360, k=k, max_size=12)
+    hg, part = inst.hg, inst.part
+    s = session(lp, hg, k, part, lmax=inst.lmax, perfect=inst.perfect)
+    check_state(orc, s, hg, k, part)
+    to, gain, border = s.best_moves()
+    eto, egain, eborder = orc.best_moves(hg, k, part, inst.lmax)
+    assert np.array_equal(to, eto) and np.array_equal(gain, egain) and np.array_equal(border, eborder)
+    if k <= 200:
+        ben, pen = s.gain_cache()
+        eben, epen = orc.gain_cache(hg, k, part)
+        assert np.array_equal(ben, eben) and np.array_equal(pen, epen)
+    s.close()
+
+
+LP_MODES = [
+    dict(subrounds=1, revert=0, rollback=0, rebalancing=1),
+    dict(subrounds=1, revert=1, rollback=1, rebalancing=1),
+    dict(subrounds=4, revert=1, rollback=0, rebalancing=0),
+    dict(subrounds=16, revert=1, rollback=1, rebalancing=1),
+    dict(subrounds=64, revert=0, rollback=1, rebalancing=1),
+]
+
+
+def run_both(lp, orc, inst, rounds, mode, threshold=100):
+    hg, k = inst.hg, inst.k
+    s = session(lp, hg, k, inst.part, lmax=inst.lmax, perfect=inst.perfect)
+    cfg = lp.default_config(rounds=rounds, activation_threshold=threshold, **mode)
+    r = s.refine(cfg)
+    dpart = s.partition()
+    dstats = s.round_stats()
+    epart, estats = orc.lp_sync(hg, k, inst.lmax, inst.part, perfect=inst.perfect, rounds=rounds,
+                                activation_threshold=threshold, subrounds=mode["subrounds"],
+                                revert=mode["revert"], rollback=mode["rollback"],
+                                zero_gain=mode["rebalancing"])
+    return s, r, dpart, dstats, epart, estats
+
+
+def assert_same_run(s, r, dpart, dstats, epart, estats, orc, inst):
+    assert np.array_equal(dpart, epart)
+    keys = ["active", "pins", "candidates", "moved", "reverted", "delta"]
+    assert [[st[k] for k in keys] for st in dstats] == [[st[k] for k in keys] for st in estats]
+    check_state(orc, s, inst.hg, inst.k, epart)
+    assert r.km1_after == r.km1_before + r.delta
+    assert (s.block_weights() <= inst.lmax).all()
+
+
+@pytest.mark.parametrize("mode", LP_MODES)
+@pytest.mark.parametrize("seed", range(4))
+def test_lp_rounds_bit_exact_small(lp, orc, mode, seed):
+    from lpgpu import gen
+    inst = gen.random_small(seed, n=400, m=480, k=[2, 4, 7, 33][seed], max_size=10)
+    out = run_both(lp, orc, inst, 6, mode)
+    assert_same_run(*out, orc, inst)
+    out[0].close()
+
+
+@pytest.mark.parametrize("mode", LP_MODES[1:4])
+def test_lp_rounds_bit_exact_plain_small(lp, orc, mode):
+    """The 16,384-vertex k=2 workload: 5 rounds plus full recompute, bit-exact."""
+    from lpgpu import gen
+    inst = gen.plain_small(seed=0)
+    out = run_both(lp, orc, inst, 5, mode)
+    assert_same_run(*out, orc, inst)
+    out[0].close()
+
+
+def test_refinement_nodes_and_threshold(lp, orc):
+    from lpgpu import gen
+    inst = gen.random_small(5, n=500, m=600, k=4)
+    s = session(lp, inst.hg, inst.k, inst.part, lmax=inst.lmax, perfect=inst.perfect)
+    nodes = np.arange(0, 500, 3, dtype=np.int32)
+    r = s.refine(lp.default_config(rounds=3, subrounds=2), nodes=nodes)
+    st = s.round_stats()
+    assert st[0]["active"] == len(nodes)
+    assert r.km1_after == r.km1_before + r.delta
+    s.close()
+
+
+def test_edge_cases(lp, orc):
+    from lpgpu import gen
+    # no nets at all
+    hg = gen.Hypergraph(10, 0, np.zeros(1, np.int64), np.zeros(0, np.int32), np.ones(10, np.int32),
+                        np.zeros(0, np.int32)).with_incidence()
+    s = session(lp, hg, 2, np.arange(10, dtype=np.int32) % 2)
+    assert s.metrics()[:2] == (0, 0)
+    r = s.refine(lp.default_config())
+    assert r.moves == 0 and r.km1_after == 0
+    s.close()
+    # single-pin nets and isolated vertices are kept and never counted
+    off = np.array([0, 1, 3, 4, 6], np.int64)
+    pins = np.array([0, 1, 2, 3, 4, 5], np.int32)
+    hg = gen.Hypergraph(8, 4, off, pins, np.ones(8, np.int32), np.array([5, 1, 2, 3], np.int32)).with_incidence()
+    part = np.array([0, 1, 0, 1, 0, 1, 0, 1], np.int32)
+    s = session(lp, hg, 2, part, eps=0.5)
+    check_state(orc, s, hg, 2, part)
+    s.close()
+
+
+def test_invalid_arguments_are_rejected(lp):
+    from lpgpu import gen
+    s = lp.Session(0)
+    bad = gen.Hypergraph(4, 1, np.array([0, 2], np.int64), np.array([0, 9], np.int32),
+                         np.ones(4, np.int32), np.ones(1, np.int32))
+    with pytest.raises(lp.LpgpuError) as e:
+        s.upload(bad)
+    assert e.value.status == lp.ERR_INVALID_ARG
+    dup = gen.Hypergraph(4, 1, np.array([0, 2], np.int64), np.array([1, 1], np.int32),
+                         np.ones(4, np.int32), np.ones(1, np.int32))
+    with pytest.raises(lp.LpgpuError):
+        s.upload(dup)
+    with pytest.raises(lp.LpgpuError) as e:
+        s.set_partition(2, np.zeros(4, np.int32))
+    assert e.value.status == lp.ERR_STATE
+    ok = gen.Hypergraph(4, 1, np.array([0, 2], np.int64), np.array([0, 1], np.int32),
+                        np.ones(4, np.int32), np.ones(1, np.int32))
+    s.upload(ok)
+    with pytest.raises(lp.LpgpuError):
+        s.set_partition(2, np.array([0, 1, 2, 0], np.int32))
+    with pytest.raises(lp.LpgpuError):
+        s.set_partition(2000, np.zeros(4, np.int32))
+    s.set_partition(2, np.array([0, 1, 0, 1], np.int32))
+    with pytest.raises(lp.LpgpuError):
+        s.apply_moves([0], [1], [0])   # wrong source block
+    s.close()
+
+
+def test_one_shot_entry_point(lp, orc):
+    from lpgpu import gen
+    inst = gen.plain_small(seed=2)
+    cfg = lp.default_config(rounds=5, subrounds=8)
+    p, r = lp.refine_km1(inst.hg, inst.k, inst.part, eps=0.03, cfg=cfg)
+    ep, est = orc.lp_sync(inst.hg, inst.k, inst.lmax, inst.part, perfect=inst.perfect, rounds=5,
+                          subrounds=8, revert=1, rollback=1, zero_gain=1)
+    assert np.array_equal(p, ep)
+    assert r.km1_after == r.km1_before + r.delta and r.km1_after < r.km1_before
