@@ -1,0 +1,358 @@
+#!/usr/bin/env python
+"""Benchmark of the synchronous LP (km1) refinement path on one GB300.
+
+A step is one full refinement of the row-net workload from its initial
+partition: initializePartition (block weights, pin counts, connectivity sets)
+followed by 10 synchronous LP rounds and the km1 recompute. The metric is
+pins processed per second (sum over rounds of the degrees of the swept
+vertices, divided by the step time).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+GPU arm (`value`): inputs resident in HBM, device time with CUDA events on
+the session stream. `e2e`: the same work through the public session API from
+pinned host buffers (upload + set_partition + refine + download per step),
+wall-clock. `roofline`: the sweep kernel (dominant) against the measured HBM
+copy bandwidth. `cpu_baseline`: the reference-style asynchronous LP (CPU
+restatement, all host cores) on one full refinement of the same instance.
+
+Reference arm (`--impl reference`): the reference's LP algorithm cannot be
+built here (TBB legacy task API, hwloc, Boost, un-vendored submodule), so its
+CPU restatement runs with all host threads on the same workload, one full
+refinement per step.
+
+Multi-GPU: the path runs as independent replicas (one instance per rank, no
+collective); `value` is the sum over ranks of pins / the max step time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "mt-kahypar_gb300"))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "LP refinement throughput (pins processed per second)"
+UNIT = "pins/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--workload", choices=["rownet", "plain_large", "plain_small"], default="rownet")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--subrounds", type=int, default=16)
+    ap.add_argument("--no-baseline", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    return ap.parse_args()
+
+
+def dist_info():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+class Dist:
+    """Host-side barrier / max / sum across replicas (gloo); no data-path collective."""
+
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def reduce(self, x, op):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX if op == "max" else self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic_ratio():
+    """DRAM bytes / algorithmic bytes of the sweep kernel from the committed ncu
+    summary (profiles/k_sweep_rownet.txt), or None."""
+    path = os.path.join(ROOT, "profiles", "k_sweep_rownet.txt")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_over_algorithmic:"):
+                return float(line.split(":", 1)[1])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def make_instance(name, seed):
+    from lpgpu import gen
+    return getattr(gen, name)(seed=seed)
+
+
+def sweep_bytes(stats, k):
+    """Algorithmic bytes of the sweep: per swept vertex offsets (8), part (4),
+    vertex weight (4), move record out (8) and the (to, gain) read back (4):
+    28 B; per incidence net id (4), net weight (4), Φ(e, from) (4) and Λ(e)
+    (8 * ceil(k / 64))."""
+    L = 8 * ((k + 63) // 64)
+    return sum(s["active"] * 28 + s["pins"] * (12 + L) for s in stats)
+
+
+def run_cpu_async(inst, threads, rounds):
+    import oracle
+    oracle.build_oracle()
+    t0 = time.perf_counter()
+    part, stats = oracle.lp_async(inst.hg, inst.k, inst.lmax, inst.perfect, inst.part, rounds=rounds,
+                                  threads=threads, seed=1)
+    wall = time.perf_counter() - t0
+    secs = sum(s["seconds"] for s in stats)
+    pins = sum(s["pins"] for s in stats)
+    return pins / secs, pins, secs, wall, stats
+
+
+def config_dict(args, inst, cfg=None):
+    hg = inst.hg
+    d = {"workload": f"{inst.name}: {hg.n} vertices, {hg.m} nets, {hg.num_pins} pins, k={inst.k}, "
+                     f"eps={inst.eps}, {inst.rounds} synchronous LP rounds per step",
+         "n": hg.n, "m": hg.m, "pins": hg.num_pins, "k": inst.k, "eps": inst.eps,
+         "rounds": inst.rounds, "seed": args.seed,
+         "l2": "inputs larger than L2 (CSR + pin counts exceed 129 MB)"}
+    if cfg is not None:
+        d["subrounds"] = cfg.subrounds
+    return d
+
+
+def reference_arm(args):
+    rank, _, world = dist_info()
+    if rank != 0:
+        return 0
+    inst = make_instance(args.workload, args.seed)
+    threads = os.cpu_count() or 1
+    values, times = [], []
+    for i in range(args.warmup + args.steps):
+        v, pins, secs, wall, _ = run_cpu_async(inst, threads, inst.rounds)
+        if i >= args.warmup:
+            values.append(v)
+            times.append(secs)
+    value = statistics.mean(values) if values else 0.0
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded generator, same instance as the GPU arm)",
+            "config": config_dict(args, inst),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"one full {inst.rounds}-round asynchronous LP refinement per step "
+                                       "(CPU restatement of the reference's TBB LP refiner; the "
+                                       "reference itself cannot be built)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def gpu_arm(args):
+    import lpgpu
+    rank, local_rank, world = dist_info()
+    dist = Dist(world)
+    lpgpu.build()
+    inst = make_instance(args.workload, args.seed)
+    hg = inst.hg
+    cfg = lpgpu.default_config(rounds=inst.rounds, subrounds=args.subrounds)
+    s = lpgpu.Session(local_rank)
+    s.upload(hg)
+    s.set_partition(inst.k, inst.part, lmax=inst.lmax, perfect=inst.perfect)
+    s.save_partition()
+    s.enable_timing(True)
+
+    def step():
+        s.restore_partition()
+        return s.refine(cfg), s.round_stats(), s.phase_times()
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    clocks = ClockSampler(local_rank)
+    dist.barrier()
+    s.synchronize()
+    clocks.start()
+    launches0 = lpgpu.kernel_launches()
+    s.record(0)
+    pins = 0
+    sweep_ms = 0.0
+    sweep_launches = 0
+    sweep_alg = 0
+    results = []
+    for _ in range(args.steps):
+        r, stats, phases = step()
+        pins += r.pins_processed
+        sweep_ms += phases["sweep"][1]
+        sweep_launches += phases["sweep"][0]
+        sweep_alg += sweep_bytes(stats, inst.k)
+        results.append(r)
+    s.record(1)
+    elapsed_ms = s.elapsed_ms(0, 1)
+    launches = lpgpu.kernel_launches() - launches0
+    clk = clocks.stop()
+    dist.barrier()
+    max_ms = dist.reduce(elapsed_ms, "max")
+    total_pins = dist.reduce(pins, "sum")
+    value = total_pins / (max_ms / 1e3)
+
+    peak, peak_kind = hbm_peak()
+    achieved = (sweep_alg / sweep_launches) / ((sweep_ms / sweep_launches) / 1e3) / 1e9
+    ratio = ncu_traffic_ratio()
+    roofline = {"bound": "hbm", "kernel": "k_sweep", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
+                if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "traffic": None if ratio is None else ratio * sweep_alg / sweep_launches,
+                "algorithmic_bytes_per_launch": sweep_alg / sweep_launches,
+                "avg_launch_ms": sweep_ms / sweep_launches, "launches": sweep_launches}
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_leg(args, inst, cfg, local_rank, dist)
+    cpu = None
+    if not args.no_baseline and rank == 0 and world == 1:
+        threads = os.cpu_count() or 1
+        v, cpins, secs, wall, _ = run_cpu_async(inst, threads, inst.rounds)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"one full {inst.rounds}-round asynchronous LP refinement of the same instance "
+                         f"({cpins} pins in {secs:.2f} s; CPU restatement of the reference's TBB LP refiner)"}
+    r0 = results[-1]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": max_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded generator; no public dataset)",
+            "config": dict(config_dict(args, inst, cfg), parallelism=f"replicas{world}"),
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk,
+            "quality": {"km1_before": r0.km1_before, "km1_after": r0.km1_after, "delta": r0.delta,
+                        "moves": r0.moves, "imbalance": r0.imbalance, "rounds": r0.rounds}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    s.close()
+    dist.close()
+    return 0
+
+
+def e2e_leg(args, inst, cfg, device, dist):
+    """Per step: pinned host CSR + partition -> upload, set_partition, refine,
+    partition download, all through the public session API (wall clock)."""
+    import lpgpu
+    hg = inst.hg
+    pn = {k: lpgpu.pinned_copy(np.ascontiguousarray(v)) for k, v in
+          (("net_off", hg.net_off), ("pins", hg.pins), ("w_v", hg.w_v), ("w_e", hg.w_e),
+           ("part", inst.part))}
+    out = lpgpu.PinnedArray((hg.n,), np.int32)
+    host_hg = type(hg)(hg.n, hg.m, pn["net_off"].array, pn["pins"].array, pn["w_v"].array, pn["w_e"].array)
+    s = lpgpu.Session(device)
+    import ctypes
+    from lpgpu import I32P, _check, lib
+
+    def one():
+        s.upload(host_hg)
+        s.set_partition(inst.k, pn["part"].array, lmax=inst.lmax, perfect=inst.perfect)
+        r = s.refine(cfg)
+        _check(lib().lpgpu_session_get_partition(s._h, out.array.ctypes.data_as(I32P)))
+        return r
+
+    for _ in range(2):
+        one()
+    dist.barrier()
+    t0 = time.perf_counter()
+    pins = 0
+    for _ in range(args.steps):
+        pins += one().pins_processed
+    wall = time.perf_counter() - t0
+    wall = dist.reduce(wall, "max")
+    pins = dist.reduce(pins, "sum")
+    s.close()
+    h2d = 8 * (hg.m + 1) + 4 * hg.num_pins + 4 * hg.n + 4 * hg.m + 4 * hg.n
+    return {"value": pins / wall, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4 * hg.n,
+            "ms_per_step": 1e3 * wall / args.steps,
+            "path": "lpgpu_session_upload + set_partition + refine + get_partition from pinned host buffers"}
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

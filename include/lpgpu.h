@@ -15,6 +15,8 @@
  *
  * Conventions
  *   - All ids are int32 (vertices, nets, blocks); CSR offsets are int64.
+ *   - A pin listed twice in one net counts twice (the reference's
+ *     construction does not deduplicate either).
  *   - Host pointers are caller-owned and only read/written during the call.
  *   - Device state lives in an opaque session; every call returns a status.
  *   - There is no CPU fallback: without a usable CUDA device every call that
@@ -209,6 +211,17 @@ LPGPU_API lpgpu_status lpgpu_session_apply_moves(lpgpu_session* s, int64_t count
                                                  const int32_t* vertices, const int32_t* from,
                                                  const int32_t* to, int64_t* delta);
 
+/* Saves the current partition on the device / restores it and rebuilds
+ * block weights, pin counts and connectivity sets from it
+ * (PartitionedHypergraph::initializePartition, h:693-698). Lets a caller
+ * repeat a refinement from the same start without host traffic. Restore is
+ * asynchronous on the session stream. */
+LPGPU_API lpgpu_status lpgpu_session_save_partition(lpgpu_session* s);
+LPGPU_API lpgpu_status lpgpu_session_restore_partition(lpgpu_session* s);
+
+/* Number of kernels this thread has launched through the library. */
+LPGPU_API int64_t lpgpu_kernel_launches(void);
+
 /* Device memory held by the session, in bytes. */
 LPGPU_API lpgpu_status lpgpu_session_footprint(lpgpu_session* s, int64_t* bytes);
 
@@ -217,7 +230,19 @@ LPGPU_API lpgpu_status lpgpu_session_footprint(lpgpu_session* s, int64_t* bytes)
 LPGPU_API int64_t lpgpu_estimate_footprint(int64_t num_vertices, int64_t num_nets,
                                            int64_t num_pins, int32_t k, int32_t subrounds);
 
+/* Page-locked host buffers (cudaHostAlloc) so that uploads and downloads
+ * run as DMA copies. Returns NULL on failure. */
+LPGPU_API void* lpgpu_host_alloc(size_t bytes);
+LPGPU_API void lpgpu_host_free(void* p);
+
 /* ------------------------------------------------------------- timing */
+
+/* CUDA events on the session stream: record into one of 16 slots, read the
+ * elapsed device time between two recorded slots (waits for the later one). */
+LPGPU_API lpgpu_status lpgpu_session_event_record(lpgpu_session* s, int32_t slot);
+LPGPU_API lpgpu_status lpgpu_session_event_elapsed(lpgpu_session* s, int32_t a, int32_t b,
+                                                   double* ms);
+LPGPU_API lpgpu_status lpgpu_session_synchronize(lpgpu_session* s);
 
 /* Kernel-phase timing with CUDA events on the session stream. When enabled,
  * every refine records, per named phase, the summed device time and launch

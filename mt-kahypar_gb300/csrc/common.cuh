@@ -103,6 +103,9 @@ struct RoundCtx {
   int64_t act_threshold;
 };
 
+// Kernels launched by this thread through the library so far.
+int64_t kernel_launches();
+
 // Launch helpers (lp_kernels.cu). All launch on `st`; none synchronizes.
 struct Launch {
   cudaStream_t st;

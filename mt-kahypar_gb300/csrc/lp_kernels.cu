@@ -73,6 +73,23 @@ static int grid_for(const Launch& L, int64_t work_items, int threads, int per_sm
   return (int)std::max<int64_t>(1, std::min<int64_t>(cap, need));
 }
 
+// Reports the kernel that failed to launch (and a sticky error left by an
+// earlier call) through the library's error text.
+static thread_local int64_t t_launches = 0;
+int64_t kernel_launches() { return t_launches; }
+
+static cudaError_t launched(const char* name) {
+  ++t_launches;
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) set_error(std::string(name) + ": " + cudaGetErrorString(e));
+  return e;
+}
+#define LAUNCHED(name)                          \
+  do {                                          \
+    const cudaError_t _e = launched(name);      \
+    if (_e != cudaSuccess) return _e;           \
+  } while (0)
+
 // =================================================================== scan
 
 constexpr int kScanThreads = 256;
@@ -121,14 +138,17 @@ cudaError_t scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t count, i
   const int64_t tiles = (count + kScanTile - 1) / kScanTile;
   if (tiles == 1) {
     k_scan_tiles<<<1, kScanThreads, 0, st>>>(in, out, count, nullptr);
+    LAUNCHED("k_scan_tiles");
     return cudaGetLastError();
   }
   if (tmp_elems < scan_tmp_elems(count)) return cudaErrorInvalidValue;
   int64_t* sums = tmp;
   k_tile_sums<<<(unsigned)tiles, kScanThreads, 0, st>>>(in, count, sums);
+  LAUNCHED("k_tile_sums");
   cudaError_t e = scan_exclusive_i64(sums, sums, tiles, tmp + tiles, tmp_elems - tiles, st);
   if (e != cudaSuccess) return e;
   k_scan_tiles<<<(unsigned)tiles, kScanThreads, 0, st>>>(in, out, count, sums);
+  LAUNCHED("k_scan_tiles");
   return cudaGetLastError();
 }
 
@@ -162,13 +182,19 @@ cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const 
   if (e != cudaSuccess) return e;
   if ((e = cudaStreamSynchronize(L.st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(vtx_off, 0, sizeof(int64_t) * (n + 1), L.st)) != cudaSuccess) return e;
-  if (P > 0) k_count_pins<<<grid_for(L, P, 256, 8), 256, 0, L.st>>>(pins, P, vtx_off);
+  if (P > 0) {
+    k_count_pins<<<grid_for(L, P, 256, 8), 256, 0, L.st>>>(pins, P, vtx_off);
+    LAUNCHED("k_count_pins");
+  }
   if ((e = scan_exclusive_i64(vtx_off, vtx_off, n + 1, scan_tmp, scan_tmp_elems, L.st)) != cudaSuccess)
     return e;
   if ((e = cudaMemcpyAsync(cursor, vtx_off, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, L.st)) !=
       cudaSuccess)
     return e;
-  if (m > 0) k_scatter_incidence<<<grid_for(L, m * 32, 256, 8), 256, 0, L.st>>>(m, net_off, pins, cursor, inets);
+  if (m > 0) {
+    k_scatter_incidence<<<grid_for(L, m * 32, 256, 8), 256, 0, L.st>>>(m, net_off, pins, cursor, inets);
+    LAUNCHED("k_scatter_incidence");
+  }
   return cudaGetLastError();
 }
 
@@ -234,13 +260,16 @@ cudaError_t launch_init_partition(const Launch& L, const RoundCtx& c) {
   cudaError_t e;
   if ((e = cudaMemsetAsync(c.bw, 0, sizeof(int64_t) * c.k, L.st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(c.scal, 0, sizeof(int64_t) * kScalars, L.st)) != cudaSuccess) return e;
-  if (c.n > 0)
+  if (c.n > 0) {
     k_block_weights<<<grid_for(L, c.n, 256), 256, sizeof(ull) * c.k, L.st>>>(c);
+    LAUNCHED("k_block_weights");
+  }
   if (c.m > 0) {
     const size_t smem = sizeof(int) * c.k * 8;
     k_pin_counts<<<grid_for(L, c.m * 32, 256), 256, smem, L.st>>>(c);
+    LAUNCHED("k_pin_counts");
   }
-  return cudaGetLastError();
+  return cudaSuccess;
 }
 
 // metrics::km1 / hyperedgeCut (metrics.cpp:29-65): thread per net.
@@ -265,7 +294,10 @@ __global__ void k_metrics(RoundCtx c) {
 cudaError_t launch_metrics(const Launch& L, const RoundCtx& c) {
   cudaError_t e = cudaMemsetAsync(c.scal + kKm1, 0, sizeof(int64_t) * 2, L.st);
   if (e != cudaSuccess) return e;
-  if (c.m > 0) k_metrics<<<grid_for(L, c.m, 256), 256, 0, L.st>>>(c);
+  if (c.m > 0) {
+    k_metrics<<<grid_for(L, c.m, 256), 256, 0, L.st>>>(c);
+    LAUNCHED("k_metrics");
+  }
   return cudaGetLastError();
 }
 
@@ -420,6 +452,7 @@ cudaError_t launch_best_moves(const Launch& L, const RoundCtx& c, int32_t* to, i
     auto kern = k_best_moves<kW>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<grid_for(L, c.n * 32, 256), 256, smem, L.st>>>(c, to, gain, border);
+    LAUNCHED("k_best_moves");
   });
   return cudaGetLastError();
 }
@@ -469,6 +502,7 @@ cudaError_t launch_gain_cache(const Launch& L, const RoundCtx& c, int32_t* benef
   const size_t smem = sizeof(int) * c.k * 8;
   cudaFuncSetAttribute(k_gain_cache, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k_gain_cache<<<grid_for(L, c.n * 32, 256), 256, smem, L.st>>>(c, benefit, penalty);
+  LAUNCHED("k_gain_cache");
   return cudaGetLastError();
 }
 
@@ -526,7 +560,10 @@ cudaError_t launch_apply_moves(const Launch& L, const RoundCtx& c, int64_t count
                                const int32_t* from, const int32_t* to) {
   cudaError_t e = cudaMemsetAsync(c.scal + kApplyDelta, 0, sizeof(int64_t), L.st);
   if (e != cudaSuccess) return e;
-  if (count > 0) k_apply_moves<<<grid_for(L, count * 32, 256), 256, 0, L.st>>>(c, count, v, from, to);
+  if (count > 0) {
+    k_apply_moves<<<grid_for(L, count * 32, 256), 256, 0, L.st>>>(c, count, v, from, to);
+    LAUNCHED("k_apply_moves");
+  }
   return cudaGetLastError();
 }
 
@@ -565,10 +602,13 @@ __global__ void k_mark_list(uint8_t* flag, const int32_t* nodes, int64_t count) 
 
 cudaError_t launch_mark_all(const Launch& L, const RoundCtx& c, int rebalancing) {
   if (c.n == 0) return cudaSuccess;
-  if (rebalancing)
+  if (rebalancing) {
     k_mark_all<<<grid_for(L, c.n, 256), 256, 0, L.st>>>(c.next_flag, c.n);
-  else
+    LAUNCHED("k_mark_all");
+  } else {
     k_mark_border<<<grid_for(L, c.n, 256), 256, 0, L.st>>>(c);
+    LAUNCHED("k_mark_border");
+  }
   return cudaGetLastError();
 }
 
@@ -576,7 +616,10 @@ cudaError_t launch_mark_list(const Launch& L, const RoundCtx& c, const int32_t* 
   if (c.n == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(c.next_flag, 0, c.n, L.st);
   if (e != cudaSuccess) return e;
-  if (count > 0) k_mark_list<<<grid_for(L, count, 256), 256, 0, L.st>>>(c.next_flag, nodes, count);
+  if (count > 0) {
+    k_mark_list<<<grid_for(L, count, 256), 256, 0, L.st>>>(c.next_flag, nodes, count);
+    LAUNCHED("k_mark_list");
+  }
   return cudaGetLastError();
 }
 
@@ -685,10 +728,13 @@ cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int
   Scope sc(timer, "bin_active");
   const int64_t tiles = std::max<int64_t>(1, (c.n + kTile - 1) / kTile);
   k_bin_count<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_cnt);
+  LAUNCHED("k_bin_count");
   cudaError_t e = scan_exclusive_i64(tile_cnt, tile_off, S * tiles, scan_tmp, scan_tmp_elems, L.st);
   if (e != cudaSuccess) return e;
   k_bin_scatter<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_off, c.list);
+  LAUNCHED("k_bin_scatter");
   k_sub_offsets<<<1, 64, 0, L.st>>>(tile_off, tile_cnt, S, tiles, c.sub_off);
+  LAUNCHED("k_sub_offsets");
   return cudaGetLastError();
 }
 
@@ -1142,35 +1188,48 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       const int per_sm = occupancy((const void*)kern, kSweepThreads, smem);
       kern<<<grid_for(L, n * 32, kSweepThreads, per_sm), kSweepThreads, smem, L.st>>>(c, round, sub);
+      LAUNCHED("k_sweep");
     });
   }
   const int g = grid_for(L, n, 256, 4);
   {
     Scope sc(timer, "select");
     k_plan_to<<<1, 1024, 0, L.st>>>(c);
+    LAUNCHED("k_plan_to");
     k_bin_moves<<<g, 256, 0, L.st>>>(c, sub, 0);
+    LAUNCHED("k_bin_moves");
     k_select<<<k, 1024, 0, L.st>>>(c, 0);
+    LAUNCHED("k_select");
     k_accept_out<<<g, 256, sizeof(ull) * 2 * k, L.st>>>(c, sub);
+    LAUNCHED("k_accept_out");
     k_plan_from<<<1, 1024, 0, L.st>>>(c);
+    LAUNCHED("k_plan_from");
     k_bin_moves<<<g, 256, 0, L.st>>>(c, sub, 1);
+    LAUNCHED("k_bin_moves");
     k_select<<<k, 1024, 0, L.st>>>(c, 1);
+    LAUNCHED("k_select");
   }
   {
     Scope sc(timer, "commit");
     k_commit<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub);
+    LAUNCHED("k_commit");
   }
   if (c.revert) {
     Scope sc(timer, "revert");
     k_revert_eval<<<g, 256, 0, L.st>>>(c, sub);
+    LAUNCHED("k_revert_eval");
     k_undo<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub, 0);
+    LAUNCHED("k_undo");
   }
   if (c.rollback) {
     Scope sc(timer, "rollback");
     k_undo<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub, 1);
+    LAUNCHED("k_undo");
   }
   {
     Scope sc(timer, "activate");
     k_activate<<<g, 256, 0, L.st>>>(c, round, sub, epoch);
+    LAUNCHED("k_activate");
   }
   return cudaGetLastError();
 }

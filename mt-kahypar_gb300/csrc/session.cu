@@ -48,7 +48,10 @@ static int word_class_of(int k) {
 }
 
 static lpgpu_status cuda_fail(cudaError_t e, const char* what) {
-  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  // keep a more specific message set by a launch helper
+  const std::string prev = g_error;
+  const std::string here = std::string(what) + ": " + cudaGetErrorString(e);
+  set_error(prev.empty() ? here : here + " [" + prev + "]");
   cudaGetLastError();  // clear sticky-free errors
   if (e == cudaErrorMemoryAllocation) return LPGPU_ERR_OOM;
   if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ||
@@ -96,6 +99,7 @@ struct lpgpu_session_s {
   DevBuf<uint8_t> next_flag, status, over;
   DevBuf<int2> rec;
   DevBuf<uint64_t> seg_key, thr;
+  DevBuf<int32_t> saved_part;
   int64_t scan_tmp_n = 0;
   int epoch = 0;
   // results of the last refine
@@ -104,6 +108,7 @@ struct lpgpu_session_s {
   bool timing = false;
   PhaseTimer timer;
   std::vector<lpgpu_phase_time> phase_times;
+  cudaEvent_t slots[16] = {};
 
   Launch launch() const { return Launch{st, num_sms}; }
 
@@ -176,11 +181,12 @@ struct lpgpu_session_s {
   }
   void release_all() {
     release_partition();
-    DevBuf<int64_t>* b64[] = {&net_off, &vtx_off, &sub_off, &scal, &stats, &tile_cnt, &tile_off, &scan_tmp};
+    DevBuf<int64_t>* b64[] = {&net_off, &vtx_off, &sub_off, &stats, &tile_cnt, &tile_off, &scan_tmp};
     for (auto* b : b64) b->release(&footprint);
     DevBuf<int32_t>* b32[] = {&pins, &inets, &w_v, &w_e, &list, &net_epoch, &seg_w};
     for (auto* b : b32) b->release(&footprint);
     next_flag.release(&footprint);
+    saved_part.release(&footprint);
     status.release(&footprint);
     rec.release(&footprint);
     seg_key.release(&footprint);
@@ -190,9 +196,12 @@ struct lpgpu_session_s {
 
 namespace {
 
+// Makes the session's device current for one API call and clears the
+// thread's error text.
 struct DeviceGuard {
   int prev = -1;
   explicit DeviceGuard(int dev) {
+    g_error.clear();
     if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
     if (prev != dev) cudaSetDevice(dev);
   }
@@ -221,16 +230,6 @@ lpgpu_status validate_csr(int64_t n, int64_t m, const int64_t* net_off, const in
   const int64_t P = net_off[m];
   for (int64_t i = 0; i < P; ++i)
     if (pins[i] < 0 || pins[i] >= n) return invalid("pin id out of range");
-  // duplicate pins inside a net are not allowed (the reference's construct
-  // assumes a set); checked with a stamp array
-  {
-    std::vector<int32_t> stamp(n, -1);
-    for (int64_t e = 0; e < m; ++e)
-      for (int64_t i = net_off[e]; i < net_off[e + 1]; ++i) {
-        if (stamp[pins[i]] == (int32_t)e) return invalid("duplicate pin inside a net");
-        stamp[pins[i]] = (int32_t)e;
-      }
-  }
   int64_t tw = 0;
   for (int64_t v = 0; v < n; ++v) {
     const int64_t w = w_v ? w_v[v] : 1;
@@ -312,6 +311,8 @@ lpgpu_status lpgpu_session_destroy(lpgpu_session* s) {
     cudaStreamSynchronize(s->st);
     s->release_all();
     s->scal.release(&s->footprint);
+    for (auto& ev : s->slots)
+      if (ev) cudaEventDestroy(ev);
     cudaStreamDestroy(s->st);
   }
   delete s;
@@ -326,7 +327,9 @@ lpgpu_status lpgpu_session_upload(lpgpu_session* s, int64_t n, int64_t m, const 
   if (vs != LPGPU_OK) return vs;
   DeviceGuard g(s->device);
   CK(cudaStreamSynchronize(s->st));
-  s->release_all();
+  // buffers of the same size are reused; the partition must be set again
+  s->has_part = false;
+  s->has_hg = false;
   s->n = n;
   s->m = m;
   s->P = net_off[m];
@@ -738,6 +741,76 @@ int64_t lpgpu_estimate_footprint(int64_t n, int64_t m, int64_t P, int32_t k, int
   b += 4 * n + 4 * m * (int64_t)k + 4 * m * W;                         // part, Φ, Λ
   b += 8 * (3 * k + 7 * k + 1 + 2 * k) + 2 * k + 8 * 64 + 8 * 8;       // per-block, stats, scalars
   return b;
+}
+
+lpgpu_status lpgpu_session_save_partition(lpgpu_session* s) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  DeviceGuard g(s->device);
+  CK(s->saved_part.alloc(s->n, &s->footprint));
+  if (s->n > 0)
+    CK(cudaMemcpyAsync(s->saved_part.p, s->part.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToDevice, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_restore_partition(lpgpu_session* s) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  if (s->saved_part.count != (size_t)s->n || (s->n > 0 && !s->saved_part.p)) {
+    set_error("no saved partition");
+    return LPGPU_ERR_STATE;
+  }
+  DeviceGuard g(s->device);
+  if (s->n > 0)
+    CK(cudaMemcpyAsync(s->part.p, s->saved_part.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToDevice, s->st));
+  RoundCtx c = s->ctx();
+  CK(launch_init_partition(s->launch(), c));
+  return LPGPU_OK;
+}
+
+int64_t lpgpu_kernel_launches(void) { return kernel_launches(); }
+
+void* lpgpu_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+
+void lpgpu_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+lpgpu_status lpgpu_session_event_record(lpgpu_session* s, int32_t slot) {
+  if (!s || slot < 0 || slot >= 16) return invalid("bad session or event slot");
+  DeviceGuard g(s->device);
+  if (!s->slots[slot]) CK(cudaEventCreate(&s->slots[slot]));
+  CK(cudaEventRecord(s->slots[slot], s->st));
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_event_elapsed(lpgpu_session* s, int32_t a, int32_t b, double* ms) {
+  if (!s || a < 0 || a >= 16 || b < 0 || b >= 16 || !ms) return invalid("bad event slots");
+  if (!s->slots[a] || !s->slots[b]) {
+    set_error("event slot never recorded");
+    return LPGPU_ERR_STATE;
+  }
+  DeviceGuard g(s->device);
+  CK(cudaEventSynchronize(s->slots[b]));
+  float f = 0.f;
+  CK(cudaEventElapsedTime(&f, s->slots[a], s->slots[b]));
+  *ms = f;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_synchronize(lpgpu_session* s) {
+  if (!s) return invalid("null session");
+  DeviceGuard g(s->device);
+  CK(cudaStreamSynchronize(s->st));
+  return LPGPU_OK;
 }
 
 lpgpu_status lpgpu_session_enable_timing(lpgpu_session* s, int32_t enable) {

@@ -67,7 +67,10 @@ SYMBOLS = [
     "lpgpu_session_get_pin_counts", "lpgpu_session_get_connectivity",
     "lpgpu_session_get_incidence", "lpgpu_session_best_moves", "lpgpu_session_gain_cache",
     "lpgpu_session_apply_moves", "lpgpu_session_footprint", "lpgpu_estimate_footprint",
-    "lpgpu_session_enable_timing", "lpgpu_session_phase_times",
+    "lpgpu_session_enable_timing", "lpgpu_session_phase_times", "lpgpu_session_save_partition",
+    "lpgpu_session_restore_partition", "lpgpu_kernel_launches", "lpgpu_host_alloc",
+    "lpgpu_host_free", "lpgpu_session_event_record", "lpgpu_session_event_elapsed",
+    "lpgpu_session_synchronize",
 ]
 
 
@@ -82,6 +85,10 @@ def lib():
         L.lpgpu_status_string.restype = ctypes.c_char_p
         L.lpgpu_estimate_footprint.restype = ctypes.c_int64
         L.lpgpu_estimate_footprint.argtypes = [ctypes.c_int64] * 3 + [ctypes.c_int32] * 2
+        L.lpgpu_kernel_launches.restype = ctypes.c_int64
+        L.lpgpu_host_alloc.restype = ctypes.c_void_p
+        L.lpgpu_host_alloc.argtypes = [ctypes.c_size_t]
+        L.lpgpu_host_free.argtypes = [ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -216,6 +223,24 @@ class Session:
                                                _p(t, I32P), ctypes.byref(d)))
         return d.value
 
+    def save_partition(self):
+        _check(lib().lpgpu_session_save_partition(self._h))
+
+    def restore_partition(self):
+        _check(lib().lpgpu_session_restore_partition(self._h))
+
+    def record(self, slot):
+        _check(lib().lpgpu_session_event_record(self._h, ctypes.c_int32(slot)))
+
+    def elapsed_ms(self, a, b):
+        ms = ctypes.c_double()
+        _check(lib().lpgpu_session_event_elapsed(self._h, ctypes.c_int32(a), ctypes.c_int32(b),
+                                                 ctypes.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        _check(lib().lpgpu_session_synchronize(self._h))
+
     def footprint(self):
         b = ctypes.c_int64()
         _check(lib().lpgpu_session_footprint(self._h, ctypes.byref(b)))
@@ -243,6 +268,37 @@ def refine_km1(hg, k, part, eps=0.03, cfg: Config = None):
                                   _p(wv, I32P), _p(we, I32P), ctypes.c_int32(k), ctypes.c_double(eps),
                                   _p(p, I32P), None if cfg is None else ctypes.byref(cfg), ctypes.byref(r)))
     return p, r
+
+
+class PinnedArray:
+    """A numpy array over page-locked host memory (lpgpu_host_alloc)."""
+
+    def __init__(self, shape, dtype):
+        dtype = np.dtype(dtype)
+        nbytes = max(1, int(np.prod(shape)) * dtype.itemsize)
+        self._ptr = lib().lpgpu_host_alloc(nbytes)
+        if not self._ptr:
+            raise LpgpuError(ERR_OOM, "cudaHostAlloc failed")
+        buf = (ctypes.c_char * nbytes).from_address(self._ptr)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def __del__(self):
+        try:
+            if self._ptr:
+                lib().lpgpu_host_free(self._ptr)
+                self._ptr = None
+        except Exception:
+            pass
+
+
+def pinned_copy(a):
+    p = PinnedArray(a.shape, a.dtype)
+    p.array[...] = a
+    return p
+
+
+def kernel_launches():
+    return int(lib().lpgpu_kernel_launches())
 
 
 def estimate_footprint(n, m, pins, k, subrounds=16):
