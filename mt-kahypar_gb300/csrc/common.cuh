@@ -70,7 +70,7 @@ struct RoundCtx {
   const int32_t* w_e;
   int32_t* part;
   int32_t* phi;
-  uint32_t* conn;
+  uint32_t* conn;        // m x 2W words: Λ(e) (W words), then Λ1(e) (W words)
   int64_t* bw;
   const int64_t* lmax;
   const int64_t* perfect;

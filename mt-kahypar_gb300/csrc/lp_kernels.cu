@@ -213,8 +213,10 @@ __global__ void k_block_weights(RoundCtx c) {
     if (s_w[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_w[b]);
 }
 
-// Φ and Λ from scratch, warp per net with a per-warp k-bin shared histogram
-// (initializePinCountInPart, h:1086-1110), fused with the km1 / cut sums.
+// Φ, Λ and Λ1 (blocks holding exactly one pin of the net) from scratch, warp
+// per net with a per-warp k-bin shared histogram (initializePinCountInPart,
+// h:1086-1110), fused with the km1 / cut sums. Net e's record is
+// conn[e * 2W .. e * 2W + 2W): W words of Λ(e), then W words of Λ1(e).
 __global__ void k_pin_counts(RoundCtx c) {
   extern __shared__ int s_hist[];
   const int k = c.k, W = c.W;
@@ -238,7 +240,11 @@ __global__ void k_pin_counts(RoundCtx c) {
         c.phi[e * k + b] = cnt;
       }
       const unsigned bits = __ballot_sync(FULLMASK, cnt > 0);
-      if (lane == 0) c.conn[e * W + w] = bits;
+      const unsigned ones = __ballot_sync(FULLMASK, cnt == 1);
+      if (lane == 0) {
+        c.conn[e * 2 * W + w] = bits;
+        c.conn[e * 2 * W + W + w] = ones;
+      }
       lam += __popc(bits);
     }
     __syncwarp();
@@ -278,7 +284,7 @@ __global__ void k_metrics(RoundCtx c) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < c.m;
        e += (int64_t)gridDim.x * blockDim.x) {
     int lam = 0;
-    for (int w = 0; w < c.W; ++w) lam += __popc(c.conn[e * c.W + w]);
+    for (int w = 0; w < c.W; ++w) lam += __popc(c.conn[e * 2 * c.W + w]);
     const int64_t we = c.w_e[e];
     km1 += (int64_t)(lam > 1 ? lam - 1 : 0) * we;
     cut += lam > 1 ? we : 0;
@@ -301,7 +307,21 @@ cudaError_t launch_metrics(const Launch& L, const RoundCtx& c) {
   return cudaGetLastError();
 }
 
-// ============================================================ best move
+// ====================================================== sweep / best move
+
+// 32 x 32 bit transpose across a warp (recursive block swap with shuffles):
+// on return lane j holds the word whose bit i is bit j of lane i's input.
+__device__ __forceinline__ uint32_t transpose32(uint32_t x) {
+  const int lane = lane_id();
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const uint32_t m = s == 16 ? 0x0000FFFFu : s == 8 ? 0x00FF00FFu : s == 4 ? 0x0F0F0F0Fu
+                     : s == 2 ? 0x33333333u : 0x55555555u;
+    const uint32_t y = __shfl_xor_sync(FULLMASK, x, s);
+    x = (lane & s) ? ((x & ~m) | ((y >> s) & m)) : ((x & m) | ((y << s) & ~m));
+  }
+  return x;
+}
 
 template <int W>
 __device__ __forceinline__ void load_words(const uint32_t* __restrict__ p, uint32_t (&w)[W]) {
@@ -320,108 +340,298 @@ __device__ __forceinline__ void load_words(const uint32_t* __restrict__ p, uint3
   }
 }
 
-struct BestMove {
-  int to;       // target block, == from when none
-  int gain;     // objective delta (< 0 improving, 0 zero-gain move or none)
-  bool border;
+// Weighted sum over the lanes in `mask` from weight bit-planes:
+// sum_p popc(bits[p] & mask) << p (planes beyond kPlanes recomputed by the caller).
+constexpr int kPlanes = 4;
+
+struct Planes {
+  uint32_t b[kPlanes];
+  int n;  // number of planes in use (<= 31)
 };
 
-// Warp-cooperative Km1Policy::computeMaxGainMoveImpl (gain_policy.h:108-167,
-// disable_randomization) for vertex v, guarded by isBorderNode (h:605-620).
-// Lanes stride over the incident nets: each lane adds its nets' weights into
-// the per-warp shared penalty array `pen` (one int per block, all zero on
-// entry and on exit) for every block of Λ(e) other than `from`, and sums the
-// internal weight of nets with Φ(e, from) > 1. Lanes then stride over blocks
-// and the warp reduces (score, block) to the minimum score with the lowest
-// block id. Feasibility: bw[b] + w(v) <= lmax[b]. With zero_gain, a vertex
-// without an improving move takes the lowest-id feasible block of score 0 if
-// the rebalancing rule of label_propagation_refiner.h:88-95 holds.
-template <int W>
-__device__ __forceinline__ BestMove warp_best_move(const RoundCtx& c, int64_t v, int from,
-                                                   int wv, int* __restrict__ pen,
-                                                   const int64_t* __restrict__ bw,
-                                                   const int64_t* __restrict__ lmax,
-                                                   const int64_t* __restrict__ perfect,
-                                                   int zero_gain, int64_t* deg_out) {
-  const int lane = lane_id();
-  const int k = c.k;
-  const int64_t beg = c.vtx_off[v], end = c.vtx_off[v + 1];
-  *deg_out = end - beg;
-  BestMove r{from, 0, false};
-  if (end - beg > kHighDegree) return r;
-  int internal = 0;
-  bool border = false;
-  const int fw = from >> 5;
-  const uint32_t fbit = 1u << (from & 31);
-  for (int64_t j = beg + lane; j < end; j += 32) {
-    const int e = __ldg(&c.inets[j]);
-    const int we = __ldg(&c.w_e[e]);
-    if (__ldg(&c.phi[(int64_t)e * k + from]) > 1) internal += we;
-    uint32_t words[W];
-    load_words<W>(c.conn + (int64_t)e * W, words);
-    int lam = 0;
+// Bit-planes of a per-lane non-negative weight `w` (all lanes participate).
+__device__ __forceinline__ Planes make_planes(int w, int nplanes) {
+  Planes p;
+  p.n = nplanes;
 #pragma unroll
-    for (int w = 0; w < W; ++w) {
-      uint32_t bits = words[w];
-      lam += __popc(bits);
-      if (w == fw) bits &= ~fbit;
-      while (bits) {
-        const int t = __ffs(bits) - 1;
-        bits &= bits - 1;
-        atomicAdd(&pen[w * 32 + t], we);
-      }
-    }
-    border |= lam > 1;
-  }
-  border = __any_sync(FULLMASK, border);
-  r.border = border;
-  if (!border) return r;  // no block other than `from` was touched
-  internal = warp_sum(internal);
-  __syncwarp();
-  int best_s = INT_MAX, best_b = INT_MAX, zero_b = INT_MAX;
-  for (int b = lane; b < k; b += 32) {
-    const int pb = pen[b];
-    pen[b] = 0;
-    if (b == from || bw[b] + wv > lmax[b]) continue;
-    const int score = internal - pb;
-    if (score < best_s) { best_s = score; best_b = b; }
-    if (score == 0 && zero_b == INT_MAX) zero_b = b;
-  }
-  __syncwarp();
-  const int ms = __reduce_min_sync(FULLMASK, best_s);
-  if (ms < 0) {
-    r.to = __reduce_min_sync(FULLMASK, best_s == ms ? best_b : INT_MAX);
-    r.gain = ms;
-    return r;
-  }
-  if (zero_gain) {
-    const int zb = __reduce_min_sync(FULLMASK, zero_b);
-    if (zb != INT_MAX && bw[from] - 1 > bw[zb] + 1 && bw[zb] < perfect[zb]) r.to = zb;
-  }
-  return r;
+  for (int i = 0; i < kPlanes; ++i) p.b[i] = i < nplanes ? __ballot_sync(FULLMASK, (w >> i) & 1) : 0u;
+  return p;
 }
 
-// Best move of every vertex on the current state (parity / debug path).
+// sum over lanes in mask of w; warp-uniform call (extra planes via ballot).
+__device__ __forceinline__ int plane_sum(const Planes& p, uint32_t mask, int w) {
+  int s = 0;
+#pragma unroll
+  for (int i = 0; i < kPlanes; ++i) s += __popc(p.b[i] & mask) << i;
+  for (int i = kPlanes; i < p.n; ++i) s += __popc(__ballot_sync(FULLMASK, (w >> i) & 1) & mask) << i;
+  return s;
+}
+
+// Decision of Km1Policy::computeMaxGainMoveImpl (gain_policy.h:147-166,
+// disable_randomization) from penalties held by block-owning lanes: lane l
+// owns blocks l + 32 t and pen[t] = sum of w(e) over incident nets with that
+// block in Λ(e). score(b) = internal - pen(b); the move goes to the feasible
+// block (slack(b) >= w(v), b != from) of minimum score < 0, lowest id on ties.
+// Without one, and with zero_gain, the lowest feasible block of score 0 is
+// taken if the rebalancing rule of label_propagation_refiner.h:88-95 holds.
 template <int W>
-__global__ void __launch_bounds__(256) k_best_moves(RoundCtx c, int32_t* to, int32_t* gain,
-                                                    uint8_t* border) {
-  extern __shared__ unsigned char smem_raw[];
-  int64_t* s_bw = reinterpret_cast<int64_t*>(smem_raw);
-  int64_t* s_lmax = s_bw + c.k;
-  int* pen = reinterpret_cast<int*>(s_lmax + c.k) + (threadIdx.x >> 5) * c.k;
-  for (int b = threadIdx.x; b < c.k; b += blockDim.x) { s_bw[b] = c.bw[b]; s_lmax[b] = c.lmax[b]; }
-  for (int b = lane_id(); b < c.k; b += 32) pen[b] = 0;
-  __syncthreads();
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; v < c.n; v += warps) {
-    const int from = c.part[v];
-    int64_t deg;
-    const BestMove bm = warp_best_move<W>(c, v, from, c.w_v[v], pen, s_bw, s_lmax, nullptr, 0, &deg);
-    if (lane_id() == 0) {
-      if (to) to[v] = bm.to;
-      if (gain) gain[v] = bm.gain;
-      if (border) border[v] = bm.border;
+__device__ __forceinline__ void decide(int k, int from, int wv, int internal, int zero_gain,
+                                       const int (&pen)[W], const int (&slack)[W],
+                                       const int64_t* __restrict__ s_bw,
+                                       const int64_t* __restrict__ s_perf, int& to, int& gain) {
+  const int lane = lane_id();
+  int bp = -1, bb = INT_MAX, zb = INT_MAX;
+#pragma unroll
+  for (int t = 0; t < W; ++t) {
+    const int blk = 32 * t + lane;
+    if (blk < k && blk != from && slack[t] >= wv) {
+      if (pen[t] > bp) { bp = pen[t]; bb = blk; }
+      if (zb == INT_MAX && pen[t] == internal) zb = blk;
     }
+  }
+  const int mp = __reduce_max_sync(FULLMASK, bp);
+  if (mp > internal) {
+    to = __reduce_min_sync(FULLMASK, bp == mp ? bb : INT_MAX);
+    gain = internal - mp;
+    return;
+  }
+  if (zero_gain) {
+    const int z = __reduce_min_sync(FULLMASK, zb);
+    if (z != INT_MAX && s_bw[from] - 1 > s_bw[z] + 1 && s_bw[z] < s_perf[z]) {
+      to = z;
+      gain = 0;
+    }
+  }
+}
+
+constexpr int kSweepThreads = 256;
+
+// Sweep: the best move of every active vertex (moveVertex's isBorderNode +
+// computeMaxGainMove, label_propagation_refiner.h:82-95) on the current state.
+//
+// A warp takes a tile of 32 list entries (lane = vertex). Vertices of degree
+// 1..32 are packed greedily into groups of <= 32 incidences (lane = incidence);
+// every incidence lane loads its net's record {Λ(e), Λ1(e)} (one 32-byte
+// sector for k <= 128) and w(e); Λ words are transposed across the warp so
+// that lane l holds, per 32-block word t, the mask of incidences whose net
+// contains block l + 32 t. A vertex's penalty for that block is then a
+// popcount of the mask restricted to its incidence lanes (weighted through
+// bit-planes of w(e)); internal weight (nets with Φ(e, from) > 1, i.e. from
+// not in Λ1(e)) and the border test come from ballots. Vertices of degree
+// > 32 accumulate the same quantities over 32-incidence chunks. Cost per
+// incidence is independent of |Λ(e)|.
+//
+// Outputs: sub-round mode writes rec[pos] = (to, gain) or to = -1 and the
+// per-block candidate totals; query mode (dbg_to != null) writes to / gain /
+// border for every vertex (list = all vertices, no zero-gain moves).
+template <int W>
+__global__ void __launch_bounds__(kSweepThreads) k_sweep(RoundCtx c, int round, int sub,
+                                                          int32_t* dbg_to, int32_t* dbg_gain,
+                                                          uint8_t* dbg_border) {
+  extern __shared__ unsigned char smem_raw[];
+  const int k = c.k;
+  const bool query = dbg_to != nullptr;
+  int64_t* s_bw = reinterpret_cast<int64_t*>(smem_raw);
+  int64_t* s_perf = s_bw + k;
+  ull* s_in_w = reinterpret_cast<ull*>(s_perf + k);
+  ull* s_out_w = s_in_w + k;
+  int* s_slack = reinterpret_cast<int*>(s_out_w + k);
+  unsigned* s_in_cnt = reinterpret_cast<unsigned*>(s_slack + k);
+  unsigned char* s_owner = reinterpret_cast<unsigned char*>(s_in_cnt + k) + (threadIdx.x >> 5) * 32;
+  for (int b = threadIdx.x; b < k; b += blockDim.x) {
+    const int64_t bw = c.bw[b];
+    const int64_t sl = c.lmax[b] - bw;
+    s_bw[b] = bw;
+    s_perf[b] = query ? 0 : c.perfect[b];
+    s_slack[b] = sl < 0 ? -1 : (sl > INT_MAX ? INT_MAX : (int)sl);
+    s_in_w[b] = 0;
+    s_out_w[b] = 0;
+    s_in_cnt[b] = 0;
+  }
+  __syncthreads();
+  const int lane = lane_id();
+  int slack[W];
+#pragma unroll
+  for (int t = 0; t < W; ++t) slack[t] = (32 * t + lane < k) ? s_slack[32 * t + lane] : -1;
+  const int zero_gain = query ? 0 : c.zero_gain;
+  const int64_t beg = query ? 0 : c.sub_off[sub];
+  const int64_t cnt = query ? c.n : c.sub_off[sub + 1] - beg;
+  const int W2 = 2 * W;
+  int64_t pins = 0, cands = 0;
+  const int64_t wstride = ((int64_t)gridDim.x * blockDim.x);
+  for (int64_t tile = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; tile < cnt; tile += wstride) {
+    const int64_t pos = beg + tile + lane;
+    const bool valid = tile + lane < cnt;
+    const int64_t v = valid ? (query ? pos : (int64_t)c.list[pos]) : 0;
+    int64_t o0 = 0;
+    int deg = 0, from = 0, wv = 0;
+    if (valid) {
+      o0 = c.vtx_off[v];
+      const int64_t d = c.vtx_off[v + 1] - o0;
+      pins += d;
+      deg = d > kHighDegree ? -1 : (int)d;  // -1: never a border vertex
+      from = c.part[v];
+      wv = c.w_v[v];
+    }
+    int my_to = from, my_gain = 0;
+    bool my_border = false;
+
+    // ---- vertices of degree 1..32, packed into groups of <= 32 incidences
+    const bool small = deg >= 1 && deg <= 32;
+    const int dsm = small ? deg : 0;
+    int incl = dsm;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(FULLMASK, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int excl = incl - dsm;
+    unsigned rem = __ballot_sync(FULLMASK, small);
+    while (rem) {
+      const int q = __ffs(rem) - 1;
+      const int start = __shfl_sync(FULLMASK, excl, q);
+      const bool inpack = ((rem >> lane) & 1u) && incl - start <= 32;
+      const unsigned pmask = __ballot_sync(FULLMASK, inpack);
+      const int D = __shfl_sync(FULLMASK, incl, 31 - __clz(pmask)) - start;
+      const int st = excl - start;
+      __syncwarp();
+      if (inpack) s_owner[__popc(pmask & lanemask_lt())] = (unsigned char)lane;
+      const unsigned starts = __reduce_or_sync(FULLMASK, inpack ? (1u << st) : 0u);
+      __syncwarp();
+      const bool has = lane < D;
+      const int ow = has ? s_owner[__popc(starts & ((2u << lane) - 1u)) - 1] : 0;
+      const int64_t o_ow = __shfl_sync(FULLMASK, o0, ow);
+      const int st_ow = __shfl_sync(FULLMASK, st, ow);
+      const int from_ow = __shfl_sync(FULLMASK, from, ow);
+      uint32_t words[W];
+#pragma unroll
+      for (int t = 0; t < W; ++t) words[t] = 0;
+      int we = 0, ic = 0, lam = 0;
+      if (has) {
+        const int64_t e = __ldg(&c.inets[o_ow + lane - st_ow]);
+        we = __ldg(&c.w_e[e]);
+        const uint32_t* rec = c.conn + e * W2;
+        load_words<W>(rec, words);
+        const uint32_t l1 = __ldg(rec + W + (from_ow >> 5));
+        ic = ((l1 >> (from_ow & 31)) & 1u) ? 0 : we;
+#pragma unroll
+        for (int t = 0; t < W; ++t) lam += __popc(words[t]);
+      }
+      const unsigned bm = __ballot_sync(FULLMASK, lam > 1);
+      uint32_t col[W];
+#pragma unroll
+      for (int t = 0; t < W; ++t) col[t] = transpose32(words[t]);
+      const unsigned wor = __reduce_or_sync(FULLMASK, (unsigned)we);
+      const int nplanes = 32 - __clz(wor);
+      const Planes wp = make_planes(we, nplanes);
+      const Planes ip = make_planes(ic, nplanes);
+      unsigned pm = pmask;
+      while (pm) {
+        const int j = __ffs(pm) - 1;
+        pm &= pm - 1;
+        const int stj = __shfl_sync(FULLMASK, st, j);
+        const int dj = __shfl_sync(FULLMASK, deg, j);
+        const unsigned mj = (dj == 32) ? FULLMASK : (((1u << dj) - 1u) << stj);
+        if ((bm & mj) == 0) continue;  // not a border vertex
+        const int fromj = __shfl_sync(FULLMASK, from, j);
+        const int wvj = __shfl_sync(FULLMASK, wv, j);
+        const int internal = plane_sum(ip, mj, ic);
+        int pen[W];
+#pragma unroll
+        for (int t = 0; t < W; ++t) pen[t] = plane_sum(wp, col[t] & mj, we);
+        int to = fromj, gain = 0;
+        decide<W>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
+        if (lane == j) {
+          my_to = to;
+          my_gain = gain;
+          my_border = true;
+        }
+      }
+      rem &= ~pmask;
+    }
+
+    // ---- vertices of degree 33..kHighDegree, one at a time in 32-incidence chunks
+    unsigned bigm = __ballot_sync(FULLMASK, deg > 32);
+    while (bigm) {
+      const int j = __ffs(bigm) - 1;
+      bigm &= bigm - 1;
+      const int64_t oj = __shfl_sync(FULLMASK, o0, j);
+      const int dj = __shfl_sync(FULLMASK, deg, j);
+      const int fromj = __shfl_sync(FULLMASK, from, j);
+      const int wvj = __shfl_sync(FULLMASK, wv, j);
+      int pen[W];
+#pragma unroll
+      for (int t = 0; t < W; ++t) pen[t] = 0;
+      int internal = 0;
+      bool border = false;
+      for (int base = 0; base < dj; base += 32) {
+        const bool has = base + lane < dj;
+        uint32_t words[W];
+#pragma unroll
+        for (int t = 0; t < W; ++t) words[t] = 0;
+        int we = 0, ic = 0, lam = 0;
+        if (has) {
+          const int64_t e = __ldg(&c.inets[oj + base + lane]);
+          we = __ldg(&c.w_e[e]);
+          const uint32_t* rec = c.conn + e * W2;
+          load_words<W>(rec, words);
+          const uint32_t l1 = __ldg(rec + W + (fromj >> 5));
+          ic = ((l1 >> (fromj & 31)) & 1u) ? 0 : we;
+#pragma unroll
+          for (int t = 0; t < W; ++t) lam += __popc(words[t]);
+        }
+        border |= __any_sync(FULLMASK, lam > 1);
+        const unsigned wor = __reduce_or_sync(FULLMASK, (unsigned)we);
+        const int nplanes = 32 - __clz(wor);
+        const Planes wp = make_planes(we, nplanes);
+        internal += __reduce_add_sync(FULLMASK, (unsigned)ic);
+#pragma unroll
+        for (int t = 0; t < W; ++t) pen[t] += plane_sum(wp, transpose32(words[t]), we);
+      }
+      if (!border) continue;
+      int to = fromj, gain = 0;
+      decide<W>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
+      if (lane == j) {
+        my_to = to;
+        my_gain = gain;
+        my_border = true;
+      }
+    }
+
+    if (valid) {
+      if (query) {
+        dbg_to[v] = my_to;
+        if (dbg_gain) dbg_gain[v] = my_gain;
+        if (dbg_border) dbg_border[v] = my_border;
+      } else {
+        int2 r = make_int2(-1, 0);
+        if (my_to != from) {
+          r = make_int2(my_to, my_gain);
+          atomicAdd(&s_in_w[my_to], (ull)(int64_t)wv);
+          atomicAdd(&s_in_cnt[my_to], 1u);
+          atomicAdd(&s_out_w[from], (ull)(int64_t)wv);
+          ++cands;
+        }
+        c.rec[pos] = r;
+      }
+    }
+  }
+  if (query) return;
+  pins = block_sum_i64(pins);
+  cands = block_sum_i64(cands);
+  if (threadIdx.x == 0) {
+    int64_t* st = c.stats + (int64_t)round * kStats;
+    atomicAdd(reinterpret_cast<ull*>(&st[kStPins]), (ull)pins);
+    atomicAdd(reinterpret_cast<ull*>(&st[kStCands]), (ull)cands);
+    if (blockIdx.x == 0) atomicAdd(reinterpret_cast<ull*>(&st[kStActive]), (ull)cnt);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < k; b += blockDim.x) {
+    if (s_in_cnt[b]) {
+      atomicAdd(reinterpret_cast<ull*>(&c.in_w[b]), s_in_w[b]);
+      atomicAdd(reinterpret_cast<ull*>(&c.in_cnt[b]), (ull)s_in_cnt[b]);
+    }
+    if (s_out_w[b]) atomicAdd(reinterpret_cast<ull*>(&c.cand_out[b]), s_out_w[b]);
   }
 }
 
@@ -443,18 +653,36 @@ static int word_class(int W) {
   return w;
 }
 
+static int occupancy(const void* kern, int threads, size_t smem) {
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, threads, smem) != cudaSuccess ||
+      blocks < 1)
+    blocks = 1;
+  return blocks;
+}
+
+static size_t sweep_smem(int k) {
+  return sizeof(int64_t) * 4 * k + sizeof(int) * k + sizeof(unsigned) * k + 32 * (kSweepThreads / 32);
+}
+
+static cudaError_t launch_sweep(const Launch& L, const RoundCtx& c, int round, int sub,
+                                int32_t* to, int32_t* gain, uint8_t* border) {
+  if (word_class(c.W) != c.W) return cudaErrorInvalidValue;
+  const size_t smem = sweep_smem(c.k);
+  LPGPU_DISPATCH_W(c.W, {
+    auto kern = k_sweep<kW>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int per_sm = occupancy((const void*)kern, kSweepThreads, smem);
+    kern<<<grid_for(L, c.n * 4, kSweepThreads, per_sm), kSweepThreads, smem, L.st>>>(c, round, sub, to, gain, border);
+    LAUNCHED("k_sweep");
+  });
+  return cudaSuccess;
+}
+
 cudaError_t launch_best_moves(const Launch& L, const RoundCtx& c, int32_t* to, int32_t* gain,
                               uint8_t* border) {
   if (c.n == 0) return cudaSuccess;
-  if (word_class(c.W) != c.W) return cudaErrorInvalidValue;
-  const size_t smem = sizeof(int64_t) * 2 * c.k + sizeof(int) * c.k * 8;
-  LPGPU_DISPATCH_W(c.W, {
-    auto kern = k_best_moves<kW>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<grid_for(L, c.n * 32, 256), 256, smem, L.st>>>(c, to, gain, border);
-    LAUNCHED("k_best_moves");
-  });
-  return cudaGetLastError();
+  return launch_sweep(L, c, 0, 0, to, gain, border);
 }
 
 // ============================================================ gain cache
@@ -477,7 +705,7 @@ __global__ void __launch_bounds__(256) k_gain_cache(RoundCtx c, int32_t* benefit
       if (c.phi[(int64_t)e * c.k + pv] == 1) ben += we;
       inc += we;
       for (int w = 0; w < c.W; ++w) {
-        uint32_t bits = c.conn[(int64_t)e * c.W + w];
+        uint32_t bits = c.conn[(int64_t)e * 2 * c.W + w];
         while (bits) {
           const int t = __ffs(bits) - 1;
           bits &= bits - 1;
@@ -508,13 +736,16 @@ cudaError_t launch_gain_cache(const Launch& L, const RoundCtx& c, int32_t* benef
 
 // ================================================================ commit
 
-// Moves v from `f` to `t` on Φ and Λ: per incident net one atomic decrement of
-// Φ(e,f) and one atomic increment of Φ(e,t); Λ bits toggle on the 1->0 and
-// 0->1 transitions seen by the atomics (updatePinCountOfHyperedge,
-// h:1133-1167). Returns this lane's share of the attributed delta
-// (km1Delta, hypergraph_common.h:133-140): -w(e) when Φ(e,f) drops to 0,
-// +w(e) when Φ(e,t) rises to 1. The per-move split depends on interleaving;
-// the sum over all concurrent moves is exactly the km1 change.
+// Moves v from `f` to `t` on Φ, Λ and Λ1: per incident net one atomic
+// decrement of Φ(e,f) and one atomic increment of Φ(e,t)
+// (updatePinCountOfHyperedge, h:1133-1167). Each atomic returns the old count,
+// so every transition is seen exactly once: Λ bits toggle on 1->0 / 0->1 and
+// Λ1 bits toggle whenever the count enters or leaves 1. Concurrent moves on
+// one net therefore leave Λ and Λ1 consistent with the final counts. Returns
+// this lane's share of the attributed delta (km1Delta,
+// hypergraph_common.h:133-140): -w(e) when Φ(e,f) drops to 0, +w(e) when
+// Φ(e,t) rises to 1. The per-move split depends on interleaving; the sum over
+// all concurrent moves is exactly the km1 change.
 __device__ __forceinline__ int64_t warp_commit_vertex(const RoundCtx& c, int64_t v, int f, int t) {
   int64_t att = 0;
   const int k = c.k, W = c.W;
@@ -522,16 +753,19 @@ __device__ __forceinline__ int64_t warp_commit_vertex(const RoundCtx& c, int64_t
   for (int64_t j = c.vtx_off[v] + lane_id(); j < c.vtx_off[v + 1]; j += 32) {
     const int64_t e = c.inets[j];
     const int we = c.w_e[e];
+    uint32_t* rec = c.conn + e * 2 * W;
     const int of = atomicSub(&c.phi[e * k + f], 1);
     if (of == 1) {
-      atomicXor(&c.conn[e * W + (f >> 5)], fbit);
+      atomicXor(&rec[f >> 5], fbit);
       att -= we;
     }
+    if (of == 1 || of == 2) atomicXor(&rec[W + (f >> 5)], fbit);
     const int ot = atomicAdd(&c.phi[e * k + t], 1);
     if (ot == 0) {
-      atomicXor(&c.conn[e * W + (t >> 5)], tbit);
+      atomicXor(&rec[t >> 5], tbit);
       att += we;
     }
+    if (ot == 0 || ot == 1) atomicXor(&rec[W + (t >> 5)], tbit);
   }
   return att;
 }
@@ -586,7 +820,7 @@ __global__ void k_mark_border(RoundCtx c) {
     if (e - b <= kHighDegree) {
       for (int64_t j = b; j < e && !f; ++j) {
         int lam = 0;
-        for (int w = 0; w < c.W; ++w) lam += __popc(c.conn[(int64_t)c.inets[j] * c.W + w]);
+        for (int w = 0; w < c.W; ++w) lam += __popc(c.conn[(int64_t)c.inets[j] * 2 * c.W + w]);
         f = lam > 1;
       }
     }
@@ -740,74 +974,6 @@ cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int
 
 // ============================================================= sub-round
 
-constexpr int kSweepThreads = 256;
-
-// Sweep: best move of every active vertex of the sub-round on the current
-// state (moveVertex's isBorderNode + computeMaxGainMove,
-// label_propagation_refiner.h:82-95). Writes rec[pos] = (to, gain) or to = -1,
-// and per-block candidate totals (in_w / in_cnt by target, out_w by source).
-template <int W>
-__global__ void __launch_bounds__(kSweepThreads) k_sweep(RoundCtx c, int round, int sub) {
-  extern __shared__ unsigned char smem_raw[];
-  const int k = c.k;
-  int64_t* s_bw = reinterpret_cast<int64_t*>(smem_raw);
-  int64_t* s_lmax = s_bw + k;
-  int64_t* s_perf = s_lmax + k;
-  ull* s_in_w = reinterpret_cast<ull*>(s_perf + k);
-  ull* s_out_w = s_in_w + k;  // candidate weight by source block
-  unsigned* s_in_cnt = reinterpret_cast<unsigned*>(s_out_w + k);
-  int* pen = reinterpret_cast<int*>(s_in_cnt + k) + (threadIdx.x >> 5) * k;
-  for (int b = threadIdx.x; b < k; b += blockDim.x) {
-    s_bw[b] = c.bw[b];
-    s_lmax[b] = c.lmax[b];
-    s_perf[b] = c.perfect[b];
-    s_in_w[b] = 0;
-    s_out_w[b] = 0;
-    s_in_cnt[b] = 0;
-  }
-  for (int b = lane_id(); b < k; b += 32) pen[b] = 0;
-  __syncthreads();
-  const int64_t beg = c.sub_off[sub], cnt = c.sub_off[sub + 1] - beg;
-  int64_t pins = 0, cands = 0;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < cnt; i += warps) {
-    const int64_t pos = beg + i;
-    const int64_t v = c.list[pos];
-    const int from = c.part[v];
-    const int wv = c.w_v[v];
-    int64_t deg;
-    const BestMove bm = warp_best_move<W>(c, v, from, wv, pen, s_bw, s_lmax, s_perf, c.zero_gain, &deg);
-    if (lane_id() == 0) {
-      pins += deg;
-      int2 r = make_int2(-1, 0);
-      if (bm.to != from) {
-        r = make_int2(bm.to, bm.gain);
-        atomicAdd(&s_in_w[bm.to], (ull)(int64_t)wv);
-        atomicAdd(&s_in_cnt[bm.to], 1u);
-        atomicAdd(&s_out_w[from], (ull)(int64_t)wv);
-        ++cands;
-      }
-      c.rec[pos] = r;
-    }
-  }
-  pins = block_sum_i64(pins);
-  cands = block_sum_i64(cands);
-  if (threadIdx.x == 0) {
-    int64_t* st = c.stats + (int64_t)round * kStats;
-    atomicAdd(reinterpret_cast<ull*>(&st[kStPins]), (ull)pins);
-    atomicAdd(reinterpret_cast<ull*>(&st[kStCands]), (ull)cands);
-    if (blockIdx.x == 0) atomicAdd(reinterpret_cast<ull*>(&st[kStActive]), (ull)cnt);
-  }
-  __syncthreads();
-  for (int b = threadIdx.x; b < k; b += blockDim.x) {
-    if (s_in_cnt[b]) {
-      atomicAdd(reinterpret_cast<ull*>(&c.in_w[b]), s_in_w[b]);
-      atomicAdd(reinterpret_cast<ull*>(&c.in_cnt[b]), (ull)s_in_cnt[b]);
-    }
-    if (s_out_w[b]) atomicAdd(reinterpret_cast<ull*>(&c.cand_out[b]), s_out_w[b]);
-  }
-}
-
 // Plan of the target-side selection (one CTA, blockDim >= k): a block
 // overflows when the candidates into it weigh more than its slack; overflowing
 // blocks get a segment for their candidates. Also decides whether the
@@ -888,49 +1054,111 @@ __global__ void k_bin_moves(RoundCtx c, int sub, int by_from) {
 }
 
 // Gain-sorted prefix per block without sorting: radix selection (8 bits per
-// pass, most significant first) of the first key whose inclusive weighted
-// prefix exceeds the budget. Keys below the threshold are accepted. One CTA
-// per block; blocks that do not overflow exit.
-__global__ void __launch_bounds__(1024) k_select(RoundCtx c, int by_from) {
+// pass, most significant differing byte first) of the first key whose
+// inclusive weighted prefix exceeds the budget; keys below it are accepted.
+// One CTA per block; blocks that do not overflow exit. Bytes shared by all
+// keys of the segment are skipped, each warp keeps a private 256-bin
+// histogram (32-bit when the segment's weight fits), and one warp scans the
+// bins.
+constexpr int kSelThreads = 512;
+
+__global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c, int by_from) {
   const int b = blockIdx.x;
   const uint8_t* over = by_from ? c.over_from : c.over_to;
   if (!over[b]) return;
-  __shared__ ull hist[256];
-  __shared__ uint64_t s_prefix, s_mask;
+  constexpr int NW = kSelThreads / 32;
+  __shared__ unsigned hist[NW][256];
+  __shared__ uint64_t s_min[NW], s_max[NW];
+  __shared__ uint64_t s_prefix;
   __shared__ int64_t s_budget;
+  __shared__ int s_sel;
+  __shared__ int64_t s_below;
+  const int lane = lane_id(), wid = threadIdx.x >> 5;
   const int64_t off = c.seg_off[b];
-  const int64_t cnt = (by_from ? c.acc_cnt[b] : c.in_cnt[b]);
+  const int64_t cnt = by_from ? c.acc_cnt[b] : c.in_cnt[b];
   const uint64_t* keys = c.seg_key + off;
   const int32_t* ws = c.seg_w + off;
+  // common prefix of all keys of the segment
+  uint64_t mn = ~0ull, mx = 0;
+  for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+    const uint64_t k = keys[i];
+    mn = k < mn ? k : mn;
+    mx = k > mx ? k : mx;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const uint64_t a = __shfl_xor_sync(FULLMASK, mn, o), z = __shfl_xor_sync(FULLMASK, mx, o);
+    mn = a < mn ? a : mn;
+    mx = z > mx ? z : mx;
+  }
+  if (lane == 0) { s_min[wid] = mn; s_max[wid] = mx; }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    s_prefix = 0;
-    s_mask = 0;
+    for (int w = 1; w < NW; ++w) {
+      mn = s_min[w] < mn ? s_min[w] : mn;
+      mx = s_max[w] > mx ? s_max[w] : mx;
+    }
+    s_min[0] = mn;
+    s_max[0] = mx;
     s_budget = by_from ? c.bw[b] - 1 : c.lmax[b] - c.bw[b];
   }
-  for (int shift = 56; shift >= 0; shift -= 8) {
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  mn = s_min[0];
+  mx = s_max[0];
+  const uint64_t diff = mn ^ mx;
+  const int top = diff ? (63 - __clzll((long long)diff)) >> 3 : 0;  // highest differing byte
+  uint64_t prefix = top == 7 ? 0 : (mn & ~((1ull << (8 * (top + 1))) - 1));
+  uint64_t mask = top == 7 ? 0 : ~((1ull << (8 * (top + 1))) - 1);
+  for (int byte = top; byte >= 0; --byte) {
+    const int shift = 8 * byte;
+    for (int i = threadIdx.x; i < NW * 256; i += blockDim.x) (&hist[0][0])[i] = 0;
     __syncthreads();
-    const uint64_t prefix = s_prefix, mask = s_mask;
     for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
-      const uint64_t key = keys[i];
-      if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255], (ull)(int64_t)ws[i]);
+      const uint64_t k = keys[i];
+      if ((k & mask) == prefix) atomicAdd(&hist[wid][(k >> shift) & 255], (unsigned)ws[i]);
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int64_t cum = 0, budget = s_budget;
-      int sel = 255;
-      for (int d = 0; d < 256; ++d) {
-        const int64_t h = (int64_t)hist[d];
-        if (cum + h > budget) { sel = d; break; }
-        cum += h;
+    if (wid == 0) {
+      // lane l owns bins 8l .. 8l+7; find the first bin where the running sum exceeds the budget
+      int64_t h[8], sum = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        int64_t t = 0;
+        for (int w = 0; w < NW; ++w) t += hist[w][8 * lane + j];
+        h[j] = t;
+        sum += t;
       }
-      s_prefix = prefix | ((uint64_t)sel << shift);
-      s_mask = mask | (255ull << shift);
-      s_budget = budget - cum;
+      int64_t run = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(FULLMASK, run, o);
+        if (lane >= o) run += y;
+      }
+      int64_t ex = run - sum;
+      const int64_t budget = s_budget;
+      int sel = -1;
+      int64_t below = 0;
+      int64_t acc = ex;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (sel < 0 && acc + h[j] > budget) { sel = 8 * lane + j; below = acc; }
+        acc += h[j];
+      }
+      const unsigned found = __ballot_sync(FULLMASK, sel >= 0);
+      const int first = found ? __ffs(found) - 1 : 31;
+      if (lane == first) {
+        s_sel = found ? sel : 255;
+        s_below = found ? below : acc;
+      }
     }
+    __syncthreads();
+    const int sel = s_sel;
+    prefix |= (uint64_t)sel << shift;
+    mask |= 255ull << shift;
+    if (threadIdx.x == 0) s_budget -= s_below;
     __syncthreads();
   }
-  if (threadIdx.x == 0) (by_from ? c.thr_from : c.thr_to)[b] = s_prefix;
+  if (threadIdx.x == 0) (by_from ? c.thr_from : c.thr_to)[b] = prefix;
 }
 
 // Weight and count of target-accepted moves per source block. Runs only when
@@ -1053,7 +1281,7 @@ __global__ void k_revert_eval(RoundCtx c, int sub) {
   const int lane = lane_id();
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
   const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
-  const int k = c.k, W = c.W;
+  const int W = c.W;
   for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
        base += stride) {
     const int64_t pos = base + lane;
@@ -1068,11 +1296,13 @@ __global__ void k_revert_eval(RoundCtx c, int sub) {
       const int t = r.x, f = r.y;
       const uint32_t fbit = 1u << (f & 31);
       int score = 0;
+      const uint32_t tbit = 1u << (t & 31);
       for (int64_t q = c.vtx_off[v] + lane; q < c.vtx_off[v + 1]; q += 32) {
         const int64_t e = c.inets[q];
         const int we = c.w_e[e];
-        if (c.phi[e * k + t] > 1) score += we;
-        if (c.conn[e * W + (f >> 5)] & fbit) score -= we;
+        const uint32_t* rec = c.conn + e * 2 * W;
+        if (!(rec[W + (t >> 5)] & tbit)) score += we;   // Φ(e, t) > 1
+        if (rec[f >> 5] & fbit) score -= we;            // f in Λ(e)
       }
       score = warp_sum(score);
       if (lane == 0 && score < 0) c.status[pj] = 2;
@@ -1155,23 +1385,26 @@ __global__ void k_activate(RoundCtx c, int round, int sub, int epoch) {
       mask &= mask - 1;
       const int64_t v = c.list[base + j];
       if (lane == 0) c.next_flag[v] = 1;
-      for (int64_t q = c.vtx_off[v] + lane; q < c.vtx_off[v + 1]; q += 32) {
-        const int64_t e = c.inets[q];
-        const int64_t b0 = c.net_off[e], b1 = c.net_off[e + 1];
-        if (b1 - b0 > c.act_threshold) continue;
-        if (atomicExch(&c.net_epoch[e], epoch) == epoch) continue;
-        for (int64_t p = b0; p < b1; ++p) c.next_flag[c.pins[p]] = 1;
+      const int64_t o0 = c.vtx_off[v], o1 = c.vtx_off[v + 1];
+      for (int64_t q0 = o0; q0 < o1; q0 += 32) {
+        // lane-parallel filter of the incident nets, then warp-parallel marking of their pins
+        int64_t e = -1;
+        if (q0 + lane < o1) {
+          e = c.inets[q0 + lane];
+          const int64_t sz = c.net_off[e + 1] - c.net_off[e];
+          if (sz > c.act_threshold || atomicExch(&c.net_epoch[e], epoch) == epoch) e = -1;
+        }
+        unsigned todo = __ballot_sync(FULLMASK, e >= 0);
+        while (todo) {
+          const int src = __ffs(todo) - 1;
+          todo &= todo - 1;
+          const int64_t ej = __shfl_sync(FULLMASK, e, src);
+          const int64_t b0 = c.net_off[ej], b1 = c.net_off[ej + 1];
+          for (int64_t p = b0 + lane; p < b1; p += 32) c.next_flag[c.pins[p]] = 1;
+        }
       }
     }
   }
-}
-
-static int occupancy(const void* kern, int threads, size_t smem) {
-  int blocks = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, threads, smem) != cudaSuccess ||
-      blocks < 1)
-    blocks = 1;
-  return blocks;
 }
 
 cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int sub, int epoch,
@@ -1181,15 +1414,8 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
   if (word_class(c.W) != c.W) return cudaErrorInvalidValue;
   {
     Scope sc(timer, "sweep");
-    const size_t smem = sizeof(int64_t) * 5 * k + sizeof(unsigned) * k +
-                        sizeof(int) * k * (kSweepThreads / 32);
-    LPGPU_DISPATCH_W(c.W, {
-      auto kern = k_sweep<kW>;
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      const int per_sm = occupancy((const void*)kern, kSweepThreads, smem);
-      kern<<<grid_for(L, n * 32, kSweepThreads, per_sm), kSweepThreads, smem, L.st>>>(c, round, sub);
-      LAUNCHED("k_sweep");
-    });
+    cudaError_t e = launch_sweep(L, c, round, sub, nullptr, nullptr, nullptr);
+    if (e != cudaSuccess) return e;
   }
   const int g = grid_for(L, n, 256, 4);
   {
@@ -1198,7 +1424,7 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
     LAUNCHED("k_plan_to");
     k_bin_moves<<<g, 256, 0, L.st>>>(c, sub, 0);
     LAUNCHED("k_bin_moves");
-    k_select<<<k, 1024, 0, L.st>>>(c, 0);
+    k_select<<<k, kSelThreads, 0, L.st>>>(c, 0);
     LAUNCHED("k_select");
     k_accept_out<<<g, 256, sizeof(ull) * 2 * k, L.st>>>(c, sub);
     LAUNCHED("k_accept_out");
@@ -1206,7 +1432,7 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
     LAUNCHED("k_plan_from");
     k_bin_moves<<<g, 256, 0, L.st>>>(c, sub, 1);
     LAUNCHED("k_bin_moves");
-    k_select<<<k, 1024, 0, L.st>>>(c, 1);
+    k_select<<<k, kSelThreads, 0, L.st>>>(c, 1);
     LAUNCHED("k_select");
   }
   {

@@ -415,7 +415,7 @@ lpgpu_status lpgpu_session_set_partition(lpgpu_session* s, int32_t k, double eps
   int64_t* fp = &s->footprint;
   CK(s->part.alloc(s->n, fp));
   CK(s->phi.alloc((size_t)s->m * k, fp));
-  CK(s->conn.alloc((size_t)s->m * s->W, fp));
+  CK(s->conn.alloc((size_t)s->m * 2 * s->W, fp));
   CK(s->bw.alloc(k, fp));
   CK(s->lmax.alloc(k, fp));
   CK(s->perfect.alloc(k, fp));
@@ -616,8 +616,8 @@ lpgpu_status lpgpu_session_get_connectivity(lpgpu_session* s, uint32_t* words) {
   DeviceGuard g(s->device);
   const int wc = word_count(s->k);
   if (s->m > 0) {
-    // device rows have W >= wc words; copy the first wc of every row
-    CK(cudaMemcpy2DAsync(words, sizeof(uint32_t) * wc, s->conn.p, sizeof(uint32_t) * s->W,
+    // device rows hold 2W words (W >= wc words of Λ, then Λ1); copy the first wc of every row
+    CK(cudaMemcpy2DAsync(words, sizeof(uint32_t) * wc, s->conn.p, sizeof(uint32_t) * 2 * s->W,
                          sizeof(uint32_t) * wc, s->m, cudaMemcpyDeviceToHost, s->st));
   }
   CK(cudaStreamSynchronize(s->st));
@@ -738,7 +738,7 @@ int64_t lpgpu_estimate_footprint(int64_t n, int64_t m, int64_t P, int32_t k, int
   b += 4 * m + 4 * n + n + n + 8 * n + 8 * n + 4 * n;                  // epoch, list, flags, status, rec, seg
   b += 8 * (kMaxSubrounds + 1) + 2 * 8 * kMaxSubrounds * tiles;        // sub-round bins
   b += 8 * (scan_tmp_elems(std::max(n + 1, kMaxSubrounds * tiles)) + 1);
-  b += 4 * n + 4 * m * (int64_t)k + 4 * m * W;                         // part, Φ, Λ
+  b += 4 * n + 4 * m * (int64_t)k + 8 * m * W;                         // part, Φ, Λ + Λ1
   b += 8 * (3 * k + 7 * k + 1 + 2 * k) + 2 * k + 8 * 64 + 8 * 8;       // per-block, stats, scalars
   return b;
 }
