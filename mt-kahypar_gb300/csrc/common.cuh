@@ -52,7 +52,9 @@ enum Scalar : int {
   kError = 5,      // device-side error flag
   kApplyDelta = 6, // apply_moves delta
   kDeltaRb = 7,    // delta of a sub-round rollback
-  kScalars = 8
+  kEpoch = 8,      // activation stamp of the current round
+  kDone = 9,       // arrival counter of the last-CTA pattern
+  kScalars = 16
 };
 
 // Per-round statistics slots (lpgpu_round_stats order).
@@ -78,7 +80,7 @@ struct RoundCtx {
   int32_t* list;
   int64_t* sub_off;      // S + 1 offsets into list
   uint8_t* next_flag;    // n
-  int32_t* net_epoch;    // m
+  int32_t* net_epoch;    // m: round stamp of nets to expand
   // per list position
   int2* rec;             // (to, gain); to < 0: no candidate
   uint8_t* status;       // 0 none, 1 moved, 2 reverted, 3 rolled back
@@ -136,8 +138,8 @@ cudaError_t launch_mark_list(const Launch& L, const RoundCtx& c, const int32_t* 
 cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int S,
                               int64_t* tile_cnt, int64_t* tile_off, int64_t* scan_tmp,
                               int64_t scan_tmp_elems, PhaseTimer* timer);
-cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int sub, int epoch,
-                            PhaseTimer* timer);
+cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int sub, PhaseTimer* timer);
+cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, PhaseTimer* timer);
 
 // Optional per-phase CUDA-event timing.
 struct PhaseTimer {

@@ -265,7 +265,7 @@ __global__ void k_pin_counts(RoundCtx c) {
 cudaError_t launch_init_partition(const Launch& L, const RoundCtx& c) {
   cudaError_t e;
   if ((e = cudaMemsetAsync(c.bw, 0, sizeof(int64_t) * c.k, L.st)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(c.scal, 0, sizeof(int64_t) * kScalars, L.st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(c.scal + kKm1, 0, sizeof(int64_t) * 2, L.st)) != cudaSuccess) return e;
   if (c.n > 0) {
     k_block_weights<<<grid_for(L, c.n, 256), 256, sizeof(ull) * c.k, L.st>>>(c);
     LAUNCHED("k_block_weights");
@@ -405,6 +405,9 @@ __device__ __forceinline__ void decide(int k, int from, int wv, int internal, in
 }
 
 constexpr int kSweepThreads = 256;
+
+__device__ bool last_cta(int64_t* counter);
+__device__ void plan_to(const RoundCtx& c);
 
 // Sweep: the best move of every active vertex (moveVertex's isBorderNode +
 // computeMaxGainMove, label_propagation_refiner.h:82-95) on the current state.
@@ -633,6 +636,7 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(RoundCtx c, int round, 
     }
     if (s_out_w[b]) atomicAdd(reinterpret_cast<ull*>(&c.cand_out[b]), s_out_w[b]);
   }
+  if (last_cta(&c.scal[kDone])) plan_to(c);
 }
 
 #define LPGPU_DISPATCH_W(W, ...)          \
@@ -902,12 +906,13 @@ __global__ void __launch_bounds__(1024) k_bin_scatter(uint8_t* __restrict__ flag
 }
 
 __global__ void k_sub_offsets(const int64_t* __restrict__ tile_off, const int64_t* __restrict__ tile_cnt,
-                              int S, int64_t tiles, int64_t* __restrict__ sub_off) {
+                              int S, int64_t tiles, int64_t* __restrict__ sub_off, int64_t* scal) {
   const int s = threadIdx.x;
   if (s < S) sub_off[s] = tile_off[s * tiles];
   if (s == 0) {
     const int64_t last = (int64_t)S * tiles - 1;
     sub_off[S] = tile_off[last] + tile_cnt[last];
+    scal[kEpoch] += 1;  // new round: fresh activation stamp
   }
 }
 
@@ -967,56 +972,86 @@ cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int
   if (e != cudaSuccess) return e;
   k_bin_scatter<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_off, c.list);
   LAUNCHED("k_bin_scatter");
-  k_sub_offsets<<<1, 64, 0, L.st>>>(tile_off, tile_cnt, S, tiles, c.sub_off);
+  k_sub_offsets<<<1, 64, 0, L.st>>>(tile_off, tile_cnt, S, tiles, c.sub_off, c.scal);
   LAUNCHED("k_sub_offsets");
   return cudaGetLastError();
 }
 
 // ============================================================= sub-round
 
-// Plan of the target-side selection (one CTA, blockDim >= k): a block
-// overflows when the candidates into it weigh more than its slack; overflowing
-// blocks get a segment for their candidates. Also decides whether the
-// source-side check can be skipped: if, for every block, all candidates
-// leaving it weigh less than its weight, no block can become empty.
-__global__ void __launch_bounds__(1024) k_plan_to(RoundCtx c) {
-  const int b = threadIdx.x;
-  bool over = false, maybe_from = false;
-  int64_t cnt = 0;
-  if (b < c.k) {
-    over = c.in_w[b] > c.lmax[b] - c.bw[b];
-    maybe_from = c.cand_out[b] >= c.bw[b];
-    cnt = over ? c.in_cnt[b] : 0;
-    c.over_to[b] = over;
-    c.thr_to[b] = ~0ull;
-    c.thr_from[b] = ~0ull;
-    c.over_from[b] = 0;
-    c.acc_w[b] = 0;
-    c.acc_cnt[b] = 0;
+// Last-CTA detection: every CTA calls this once at its end (after its global
+// writes); the CTA that arrives last gets true and resets the counter.
+__device__ bool last_cta(int64_t* counter) {
+  __shared__ bool s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const ull prev = atomicAdd(reinterpret_cast<ull*>(counter), 1ull);
+    s_last = prev == (ull)(gridDim.x - 1);
+    if (s_last) {
+      *counter = 0;
+      __threadfence();
+    }
   }
-  int64_t total;
-  const int64_t off = block_scan_excl_i64(cnt, &total);
-  if (b < c.k) {
-    c.seg_off[b] = off;
-    c.cursor[b] = off;
+  __syncthreads();
+  return s_last;
+}
+
+// Plan of the target-side selection, run by the last CTA of the sweep: a block
+// overflows when the candidates into it weigh more than its slack;
+// overflowing blocks get a segment for their candidates. The source-side
+// check is armed only if, for some block, all candidates leaving it weigh at
+// least its weight (otherwise no block can become empty).
+__device__ void plan_to(const RoundCtx& c) {
+  const int k = c.k;
+  __shared__ int64_t s_run;
+  __shared__ int s_any_over, s_any_from;
+  if (threadIdx.x == 0) {
+    s_run = 0;
+    s_any_over = 0;
+    s_any_from = 0;
   }
-  const int any_over = __syncthreads_or(over);
-  const int any_from = __syncthreads_or(maybe_from);
-  if (b == 0) {
-    c.scal[kAnyOverTo] = any_over;
-    c.scal[kAnyOverFrom] = any_from;  // refined by k_plan_from
+  __syncthreads();
+  for (int b0 = 0; b0 < k; b0 += blockDim.x) {
+    const int b = b0 + threadIdx.x;
+    bool over = false, maybe_from = false;
+    int64_t cnt = 0;
+    if (b < k) {
+      // atomics of the other CTAs are visible: they fenced before arriving
+      const int64_t in_w = *(volatile int64_t*)&c.in_w[b];
+      const int64_t out_w = *(volatile int64_t*)&c.cand_out[b];
+      over = in_w > c.lmax[b] - c.bw[b];
+      maybe_from = out_w >= c.bw[b];
+      cnt = over ? *(volatile int64_t*)&c.in_cnt[b] : 0;
+      c.over_to[b] = over;
+      c.thr_to[b] = ~0ull;
+      c.thr_from[b] = ~0ull;
+      c.over_from[b] = 0;
+    }
+    int64_t total;
+    const int64_t off = block_scan_excl_i64(cnt, &total) + s_run;
+    if (b < k) {
+      c.seg_off[b] = off;
+      c.cursor[b] = off;
+    }
+    if (over) s_any_over = 1;
+    if (maybe_from) s_any_from = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) s_run += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    c.scal[kAnyOverTo] = s_any_over;
+    c.scal[kAnyOverFrom] = s_any_from;
     c.scal[kDeltaSub] = 0;
     c.scal[kDeltaRb] = 0;
   }
 }
 
-// Places the candidates of overflowing blocks into per-block segments.
-// by_from = 0: candidates grouped by target block;
-// by_from = 1: target-accepted candidates grouped by source block.
-__global__ void k_bin_moves(RoundCtx c, int sub, int by_from) {
-  if (c.scal[by_from ? kAnyOverFrom : kAnyOverTo] == 0) return;
+// Places the candidates of overflowing target blocks into per-block segments.
+__global__ void k_bin_moves(RoundCtx c, int sub) {
+  if (c.scal[kAnyOverTo] == 0) return;
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
-  const uint8_t* over = by_from ? c.over_from : c.over_to;
   for (int64_t base = beg + (blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane_id());
        base < end; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t pos = base + lane_id();
@@ -1025,15 +1060,10 @@ __global__ void k_bin_moves(RoundCtx c, int sub, int by_from) {
     int w = 0;
     if (pos < end) {
       const int2 r = c.rec[pos];
-      if (r.x >= 0) {
+      if (r.x >= 0 && c.over_to[r.x]) {
         const int32_t v = c.list[pos];
         key = move_key(r.y, v);
-        const int from = c.part[v];
-        if (!by_from) {
-          if (over[r.x]) grp = r.x;
-        } else if (key < c.thr_to[r.x] && over[from]) {
-          grp = from;
-        }
+        grp = r.x;
         w = c.w_v[v];
       }
     }
@@ -1053,37 +1083,28 @@ __global__ void k_bin_moves(RoundCtx c, int sub, int by_from) {
   }
 }
 
-// Gain-sorted prefix per block without sorting: radix selection (8 bits per
+// Gain-sorted prefix without sorting, by one CTA: radix selection (8 bits per
 // pass, most significant differing byte first) of the first key whose
-// inclusive weighted prefix exceeds the budget; keys below it are accepted.
-// One CTA per block; blocks that do not overflow exit. Bytes shared by all
-// keys of the segment are skipped, each warp keeps a private 256-bin
-// histogram (32-bit when the segment's weight fits), and one warp scans the
-// bins.
+// inclusive weighted prefix exceeds `budget`; keys below it are accepted.
+// Bytes shared by all keys are skipped, each warp keeps a private 256-bin
+// histogram (32-bit: vertex weights total at most INT32_MAX), and one warp
+// scans the bins. Returns the threshold to every thread.
 constexpr int kSelThreads = 512;
 
-__global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c, int by_from) {
-  const int b = blockIdx.x;
-  const uint8_t* over = by_from ? c.over_from : c.over_to;
-  if (!over[b]) return;
+__device__ uint64_t cta_radix_select(const uint64_t* __restrict__ keys, const int32_t* __restrict__ ws,
+                                     int64_t cnt, int64_t budget0) {
   constexpr int NW = kSelThreads / 32;
   __shared__ unsigned hist[NW][256];
   __shared__ uint64_t s_min[NW], s_max[NW];
-  __shared__ uint64_t s_prefix;
   __shared__ int64_t s_budget;
   __shared__ int s_sel;
   __shared__ int64_t s_below;
   const int lane = lane_id(), wid = threadIdx.x >> 5;
-  const int64_t off = c.seg_off[b];
-  const int64_t cnt = by_from ? c.acc_cnt[b] : c.in_cnt[b];
-  const uint64_t* keys = c.seg_key + off;
-  const int32_t* ws = c.seg_w + off;
-  // common prefix of all keys of the segment
   uint64_t mn = ~0ull, mx = 0;
   for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
-    const uint64_t k = keys[i];
-    mn = k < mn ? k : mn;
-    mx = k > mx ? k : mx;
+    const uint64_t key = keys[i];
+    mn = key < mn ? key : mn;
+    mx = key > mx ? key : mx;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -1091,6 +1112,7 @@ __global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c, int by_from)
     mn = a < mn ? a : mn;
     mx = z > mx ? z : mx;
   }
+  __syncthreads();
   if (lane == 0) { s_min[wid] = mn; s_max[wid] = mx; }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1100,26 +1122,26 @@ __global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c, int by_from)
     }
     s_min[0] = mn;
     s_max[0] = mx;
-    s_budget = by_from ? c.bw[b] - 1 : c.lmax[b] - c.bw[b];
+    s_budget = budget0;
   }
   __syncthreads();
   mn = s_min[0];
   mx = s_max[0];
   const uint64_t diff = mn ^ mx;
   const int top = diff ? (63 - __clzll((long long)diff)) >> 3 : 0;  // highest differing byte
-  uint64_t prefix = top == 7 ? 0 : (mn & ~((1ull << (8 * (top + 1))) - 1));
-  uint64_t mask = top == 7 ? 0 : ~((1ull << (8 * (top + 1))) - 1);
+  uint64_t mask = top == 7 ? 0ull : ~((1ull << (8 * (top + 1))) - 1);
+  uint64_t prefix = mn & mask;
   for (int byte = top; byte >= 0; --byte) {
     const int shift = 8 * byte;
     for (int i = threadIdx.x; i < NW * 256; i += blockDim.x) (&hist[0][0])[i] = 0;
     __syncthreads();
     for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
-      const uint64_t k = keys[i];
-      if ((k & mask) == prefix) atomicAdd(&hist[wid][(k >> shift) & 255], (unsigned)ws[i]);
+      const uint64_t key = keys[i];
+      if ((key & mask) == prefix) atomicAdd(&hist[wid][(key >> shift) & 255], (unsigned)ws[i]);
     }
     __syncthreads();
     if (wid == 0) {
-      // lane l owns bins 8l .. 8l+7; find the first bin where the running sum exceeds the budget
+      // lane l owns bins 8l .. 8l+7: first bin whose running sum exceeds the budget
       int64_t h[8], sum = 0;
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
@@ -1134,11 +1156,9 @@ __global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c, int by_from)
         const int64_t y = __shfl_up_sync(FULLMASK, run, o);
         if (lane >= o) run += y;
       }
-      int64_t ex = run - sum;
       const int64_t budget = s_budget;
       int sel = -1;
-      int64_t below = 0;
-      int64_t acc = ex;
+      int64_t below = 0, acc = run - sum;
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         if (sel < 0 && acc + h[j] > budget) { sel = 8 * lane + j; below = acc; }
@@ -1152,27 +1172,43 @@ __global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c, int by_from)
       }
     }
     __syncthreads();
-    const int sel = s_sel;
-    prefix |= (uint64_t)sel << shift;
+    prefix |= (uint64_t)s_sel << shift;
     mask |= 255ull << shift;
+    __syncthreads();
     if (threadIdx.x == 0) s_budget -= s_below;
     __syncthreads();
   }
-  if (threadIdx.x == 0) (by_from ? c.thr_from : c.thr_to)[b] = prefix;
+  return prefix;
 }
 
-// Weight and count of target-accepted moves per source block. Runs only when
-// the plan found a block that might become empty.
-__global__ void k_accept_out(RoundCtx c, int sub) {
+// Target-side selection: one CTA per block; blocks that do not overflow exit.
+__global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c) {
+  const int b = blockIdx.x;
+  if (!c.over_to[b]) return;
+  const int64_t off = c.seg_off[b];
+  const uint64_t thr = cta_radix_select(c.seg_key + off, c.seg_w + off, c.in_cnt[b],
+                                        c.lmax[b] - c.bw[b]);
+  if (threadIdx.x == 0) c.thr_to[b] = thr;
+}
+
+// Source-side selection (changeNodePart's from_weight_after > 0,
+// partitioned_hypergraph.h:551), only when armed by the plan: one CTA sums
+// the target-accepted weight leaving each block; blocks that would become
+// empty get their accepted moves ordered the same way and keep the longest
+// prefix that leaves weight >= 1.
+__global__ void __launch_bounds__(kSelThreads) k_from_side(RoundCtx c, int sub) {
   if (c.scal[kAnyOverFrom] == 0) return;
-  extern __shared__ ull s_acc[];
-  ull* s_w = s_acc;
-  ull* s_n = s_acc + c.k;
-  for (int b = threadIdx.x; b < c.k; b += blockDim.x) { s_w[b] = 0; s_n[b] = 0; }
+  extern __shared__ ull s_fs[];
+  const int k = c.k;
+  ull* s_w = s_fs;
+  ull* s_n = s_fs + k;
+  ull* s_cur = s_fs + 2 * k;
+  __shared__ int s_any;
+  for (int b = threadIdx.x; b < k; b += blockDim.x) { s_w[b] = 0; s_n[b] = 0; }
+  if (threadIdx.x == 0) s_any = 0;
   __syncthreads();
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
-  for (int64_t pos = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pos < end;
-       pos += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t pos = beg + threadIdx.x; pos < end; pos += blockDim.x) {
     const int2 r = c.rec[pos];
     if (r.x < 0) continue;
     const int32_t v = c.list[pos];
@@ -1183,46 +1219,79 @@ __global__ void k_accept_out(RoundCtx c, int sub) {
     }
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < c.k; b += blockDim.x) {
-    if (s_n[b]) {
-      atomicAdd(reinterpret_cast<ull*>(&c.acc_w[b]), s_w[b]);
-      atomicAdd(reinterpret_cast<ull*>(&c.acc_cnt[b]), s_n[b]);
+  if (threadIdx.x == 0) {
+    ull run = 0;
+    for (int b = 0; b < k; ++b) {
+      const bool over = c.bw[b] - (int64_t)s_w[b] < 1 && s_n[b] > 0;
+      c.over_from[b] = over;
+      c.seg_off[b] = (int64_t)run;
+      s_cur[b] = run;
+      if (over) {
+        run += s_n[b];
+        s_any = 1;
+      }
     }
+  }
+  __syncthreads();
+  if (!s_any) return;
+  for (int64_t pos = beg + threadIdx.x; pos < end; pos += blockDim.x) {
+    const int2 r = c.rec[pos];
+    if (r.x < 0) continue;
+    const int32_t v = c.list[pos];
+    const uint64_t key = move_key(r.y, v);
+    const int f = c.part[v];
+    if (key < c.thr_to[r.x] && c.over_from[f]) {
+      const ull slot = atomicAdd(&s_cur[f], 1ull);
+      c.seg_key[slot] = key;
+      c.seg_w[slot] = c.w_v[v];
+    }
+  }
+  __syncthreads();
+  for (int b = 0; b < k; ++b) {
+    if (!c.over_from[b]) continue;  // uniform across the CTA
+    const int64_t off = c.seg_off[b];
+    const uint64_t thr = cta_radix_select(c.seg_key + off, c.seg_w + off, (int64_t)s_n[b], c.bw[b] - 1);
+    if (threadIdx.x == 0) c.thr_from[b] = thr;
+    __syncthreads();
   }
 }
 
-// Plan of the source-side selection (one CTA): a block overflows when the
-// target-accepted moves leaving it would leave it empty (changeNodePart's
-// from_weight_after > 0, partitioned_hypergraph.h:551).
-__global__ void __launch_bounds__(1024) k_plan_from(RoundCtx c) {
-  if (c.scal[kAnyOverFrom] == 0) return;  // uniform across the CTA
-  const int b = threadIdx.x;
-  bool over = false;
-  int64_t cnt = 0;
-  if (b < c.k) {
-    over = c.bw[b] - c.acc_w[b] < 1;
-    cnt = over ? c.acc_cnt[b] : 0;
-    c.over_from[b] = over;
+// Activation of a kept move (moveVertex, label_propagation_refiner.h:112-128):
+// the vertex becomes active for the next round and its nets with
+// |e| <= threshold are stamped with the round's epoch; k_expand_nets marks
+// their pins at the end of the round (each net expanded once per round).
+__device__ __forceinline__ void warp_activate(const RoundCtx& c, int64_t v, int epoch) {
+  if (lane_id() == 0) c.next_flag[v] = 1;
+  for (int64_t q = c.vtx_off[v] + lane_id(); q < c.vtx_off[v + 1]; q += 32) {
+    const int64_t e = c.inets[q];
+    if (c.net_off[e + 1] - c.net_off[e] <= c.act_threshold) c.net_epoch[e] = epoch;
   }
-  int64_t total;
-  const int64_t off = block_scan_excl_i64(cnt, &total);
-  if (b < c.k) {
-    c.seg_off[b] = off;
-    c.cursor[b] = off;
+}
+
+// Books the sub-round's delta into the round statistics and clears the
+// sweep accumulators for the next sub-round (last CTA of the last kernel).
+__device__ void close_subround(const RoundCtx& c, int round) {
+  if (threadIdx.x == 0) {
+    c.stats[(int64_t)round * kStats + kStDelta] += c.scal[kDeltaSub] + c.scal[kDeltaRb];
   }
-  const int any = __syncthreads_or(over);
-  if (b == 0) c.scal[kAnyOverFrom] = any;
+  for (int b = threadIdx.x; b < c.k; b += blockDim.x) {
+    c.in_w[b] = 0;
+    c.in_cnt[b] = 0;
+    c.cand_out[b] = 0;
+  }
 }
 
 // Commit of the accepted moves (changeNodePart, h:539-563, without the
 // per-move weight check: the selection already guarantees both bounds).
 // Marks status[pos] = 1 for committed moves and overwrites rec[pos].y with
-// the source block (the gain is no longer needed).
-__global__ void k_commit(RoundCtx c, int round, int sub) {
+// the source block (the gain is no longer needed). With `last`, the moves
+// are final: they are activated and the sub-round is closed.
+__global__ void k_commit(RoundCtx c, int round, int sub, int last) {
   extern __shared__ ull s_dw[];
   for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_dw[b] = 0;
   __syncthreads();
   const int lane = lane_id();
+  const int epoch = (int)c.scal[kEpoch];
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
   int64_t att = 0, moved = 0;
   const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
@@ -1252,6 +1321,7 @@ __global__ void k_commit(RoundCtx c, int round, int sub) {
       const int fj = __shfl_sync(FULLMASK, f, j);
       const int tj = __shfl_sync(FULLMASK, r.x, j);
       att += warp_commit_vertex(c, vj, fj, tj);
+      if (last) warp_activate(c, vj, epoch);
       if (lane == 0) {
         c.part[vj] = tj;
         const int64_t wv = c.w_v[vj];
@@ -1270,6 +1340,7 @@ __global__ void k_commit(RoundCtx c, int round, int sub) {
   __syncthreads();
   for (int b = threadIdx.x; b < c.k; b += blockDim.x)
     if (s_dw[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_dw[b]);
+  if (last && last_cta(&c.scal[kDone])) close_subround(c, round);
 }
 
 // Hindsight check, evaluated for all committed moves on the post-commit state
@@ -1294,9 +1365,8 @@ __global__ void k_revert_eval(RoundCtx c, int sub) {
       const int64_t v = c.list[pj];
       const int2 r = c.rec[pj];  // (to, from)
       const int t = r.x, f = r.y;
-      const uint32_t fbit = 1u << (f & 31);
+      const uint32_t fbit = 1u << (f & 31), tbit = 1u << (t & 31);
       int score = 0;
-      const uint32_t tbit = 1u << (t & 31);
       for (int64_t q = c.vtx_off[v] + lane; q < c.vtx_off[v + 1]; q += 32) {
         const int64_t e = c.inets[q];
         const int we = c.w_e[e];
@@ -1310,154 +1380,132 @@ __global__ void k_revert_eval(RoundCtx c, int sub) {
   }
 }
 
-// Undo of the moves marked 2 (revert) or, when the sub-round's delta is
-// positive, of all moves still marked 1 (rollback, status 3).
-__global__ void k_undo(RoundCtx c, int round, int sub, int rollback) {
-  if (rollback && c.scal[kDeltaSub] <= 0) return;
+// mode 0: undo of the moves marked 2 by the hindsight check; mode 1
+// (rollback): when the sub-round's delta is positive, undo of all moves still
+// marked 1 (status 3). With `last`, the moves that stay are activated and the
+// sub-round is closed.
+__global__ void k_undo(RoundCtx c, int round, int sub, int rollback, int last) {
+  const bool roll = rollback && c.scal[kDeltaSub] > 0;  // kDeltaSub is not written here
   extern __shared__ ull s_dw[];
   for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_dw[b] = 0;
   __syncthreads();
   const int lane = lane_id();
+  const int epoch = (int)c.scal[kEpoch];
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
   const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
-  const uint8_t want = rollback ? 1 : 2;
   int64_t att = 0, undone = 0;
-  for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
-       base += stride) {
-    const int64_t pos = base + lane;
-    const bool sel = pos < end && c.status[pos] == want;
-    unsigned mask = __ballot_sync(FULLMASK, sel);
-    while (mask) {
-      const int j = __ffs(mask) - 1;
-      mask &= mask - 1;
-      const int64_t pj = base + j;
-      const int64_t v = c.list[pj];
-      const int2 r = c.rec[pj];  // (to, from)
-      att += warp_commit_vertex(c, v, r.x, r.y);
-      if (lane == 0) {
-        c.part[v] = r.y;
-        const int64_t wv = c.w_v[v];
-        atomicAdd(&s_dw[r.y], (ull)wv);
-        atomicAdd(&s_dw[r.x], (ull)(-wv));
-        if (rollback) c.status[pj] = 3;
-        ++undone;
+  if (!rollback || roll || last) {
+    for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
+         base += stride) {
+      const int64_t pos = base + lane;
+      const uint8_t st = pos < end ? c.status[pos] : 0;
+      const bool sel = rollback ? (roll && st == 1) : st == 2;
+      const bool keep = last && st == 1 && !sel;
+      unsigned mask = __ballot_sync(FULLMASK, sel);
+      while (mask) {
+        const int j = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int64_t pj = base + j;
+        const int64_t v = c.list[pj];
+        const int2 r = c.rec[pj];  // (to, from)
+        att += warp_commit_vertex(c, v, r.x, r.y);
+        if (lane == 0) {
+          c.part[v] = r.y;
+          const int64_t wv = c.w_v[v];
+          atomicAdd(&s_dw[r.y], (ull)wv);
+          atomicAdd(&s_dw[r.x], (ull)(-wv));
+          if (rollback) c.status[pj] = 3;
+          ++undone;
+        }
+      }
+      unsigned kmask = __ballot_sync(FULLMASK, keep);
+      while (kmask) {
+        const int j = __ffs(kmask) - 1;
+        kmask &= kmask - 1;
+        warp_activate(c, c.list[base + j], epoch);
       }
     }
   }
   att = block_sum_i64(att);
   undone = block_sum_i64(undone);
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && undone) {
     atomicAdd(reinterpret_cast<ull*>(&c.scal[rollback ? kDeltaRb : kDeltaSub]), (ull)att);
-    int64_t* st = c.stats + (int64_t)round * kStats;
-    atomicAdd(reinterpret_cast<ull*>(&st[kStMoved]), (ull)(-undone));
-    atomicAdd(reinterpret_cast<ull*>(&st[kStReverted]), (ull)undone);
+    int64_t* stt = c.stats + (int64_t)round * kStats;
+    atomicAdd(reinterpret_cast<ull*>(&stt[kStMoved]), (ull)(-undone));
+    atomicAdd(reinterpret_cast<ull*>(&stt[kStReverted]), (ull)undone);
   }
   __syncthreads();
   for (int b = threadIdx.x; b < c.k; b += blockDim.x)
     if (s_dw[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_dw[b]);
+  if (last && last_cta(&c.scal[kDone])) close_subround(c, round);
 }
 
-// Neighbour activation of the kept moves (moveVertex, label_propagation_refiner.h:112-128):
-// the vertex and the pins of its nets with |e| <= threshold become active for
-// the next round; each net is expanded once per round (epoch stamp).
-// CTA 0 also books the sub-round delta and clears the sweep accumulators.
-__global__ void k_activate(RoundCtx c, int round, int sub, int epoch) {
-  if (blockIdx.x == 0) {
-    if (threadIdx.x == 0) {
-      c.stats[(int64_t)round * kStats + kStDelta] += c.scal[kDeltaSub] + c.scal[kDeltaRb];
-    }
-    for (int b = threadIdx.x; b < c.k; b += blockDim.x) {
-      c.in_w[b] = 0;
-      c.in_cnt[b] = 0;
-      c.cand_out[b] = 0;
-    }
-  }
+// End of a round: the pins of every net stamped with the round's epoch
+// become active for the next round.
+__global__ void k_expand_nets(RoundCtx c) {
+  const int epoch = (int)c.scal[kEpoch];
   const int lane = lane_id();
-  const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
-  const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
-  for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
-       base += stride) {
-    const int64_t pos = base + lane;
-    const bool moved = pos < end && c.status[pos] == 1;
-    unsigned mask = __ballot_sync(FULLMASK, moved);
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < c.m;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = base + lane;
+    const bool hit = e < c.m && c.net_epoch[e] == epoch;
+    unsigned mask = __ballot_sync(FULLMASK, hit);
     while (mask) {
       const int j = __ffs(mask) - 1;
       mask &= mask - 1;
-      const int64_t v = c.list[base + j];
-      if (lane == 0) c.next_flag[v] = 1;
-      const int64_t o0 = c.vtx_off[v], o1 = c.vtx_off[v + 1];
-      for (int64_t q0 = o0; q0 < o1; q0 += 32) {
-        // lane-parallel filter of the incident nets, then warp-parallel marking of their pins
-        int64_t e = -1;
-        if (q0 + lane < o1) {
-          e = c.inets[q0 + lane];
-          const int64_t sz = c.net_off[e + 1] - c.net_off[e];
-          if (sz > c.act_threshold || atomicExch(&c.net_epoch[e], epoch) == epoch) e = -1;
-        }
-        unsigned todo = __ballot_sync(FULLMASK, e >= 0);
-        while (todo) {
-          const int src = __ffs(todo) - 1;
-          todo &= todo - 1;
-          const int64_t ej = __shfl_sync(FULLMASK, e, src);
-          const int64_t b0 = c.net_off[ej], b1 = c.net_off[ej + 1];
-          for (int64_t p = b0 + lane; p < b1; p += 32) c.next_flag[c.pins[p]] = 1;
-        }
-      }
+      const int64_t ej = base + j;
+      for (int64_t p = c.net_off[ej] + lane; p < c.net_off[ej + 1]; p += 32) c.next_flag[c.pins[p]] = 1;
     }
   }
 }
 
-cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int sub, int epoch,
-                            PhaseTimer* timer) {
+cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, PhaseTimer* timer) {
+  if (c.m == 0) return cudaSuccess;
+  Scope sc(timer, "expand");
+  k_expand_nets<<<grid_for(L, c.m, 256, 4), 256, 0, L.st>>>(c);
+  LAUNCHED("k_expand_nets");
+  return cudaSuccess;
+}
+
+cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int sub, PhaseTimer* timer) {
   const int k = c.k;
   const int64_t n = c.n;
-  if (word_class(c.W) != c.W) return cudaErrorInvalidValue;
   {
     Scope sc(timer, "sweep");
     cudaError_t e = launch_sweep(L, c, round, sub, nullptr, nullptr, nullptr);
     if (e != cudaSuccess) return e;
   }
-  const int g = grid_for(L, n, 256, 4);
+  const int g = grid_for(L, n, 256, 2);
   {
     Scope sc(timer, "select");
-    k_plan_to<<<1, 1024, 0, L.st>>>(c);
-    LAUNCHED("k_plan_to");
-    k_bin_moves<<<g, 256, 0, L.st>>>(c, sub, 0);
+    k_bin_moves<<<g, 256, 0, L.st>>>(c, sub);
     LAUNCHED("k_bin_moves");
-    k_select<<<k, kSelThreads, 0, L.st>>>(c, 0);
+    k_select<<<k, kSelThreads, 0, L.st>>>(c);
     LAUNCHED("k_select");
-    k_accept_out<<<g, 256, sizeof(ull) * 2 * k, L.st>>>(c, sub);
-    LAUNCHED("k_accept_out");
-    k_plan_from<<<1, 1024, 0, L.st>>>(c);
-    LAUNCHED("k_plan_from");
-    k_bin_moves<<<g, 256, 0, L.st>>>(c, sub, 1);
-    LAUNCHED("k_bin_moves");
-    k_select<<<k, kSelThreads, 0, L.st>>>(c, 1);
-    LAUNCHED("k_select");
+    const size_t fs_smem = sizeof(ull) * 3 * k;
+    cudaFuncSetAttribute(k_from_side, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs_smem);
+    k_from_side<<<1, kSelThreads, fs_smem, L.st>>>(c, sub);
+    LAUNCHED("k_from_side");
   }
+  const int last_commit = !c.revert && !c.rollback;
   {
     Scope sc(timer, "commit");
-    k_commit<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub);
+    k_commit<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub, last_commit);
     LAUNCHED("k_commit");
   }
   if (c.revert) {
     Scope sc(timer, "revert");
     k_revert_eval<<<g, 256, 0, L.st>>>(c, sub);
     LAUNCHED("k_revert_eval");
-    k_undo<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub, 0);
+    k_undo<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub, 0, !c.rollback);
     LAUNCHED("k_undo");
   }
   if (c.rollback) {
     Scope sc(timer, "rollback");
-    k_undo<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub, 1);
+    k_undo<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub, 1, 1);
     LAUNCHED("k_undo");
   }
-  {
-    Scope sc(timer, "activate");
-    k_activate<<<g, 256, 0, L.st>>>(c, round, sub, epoch);
-    LAUNCHED("k_activate");
-  }
-  return cudaGetLastError();
+  return cudaSuccess;
 }
 
 }  // namespace lpgpu

@@ -101,7 +101,6 @@ struct lpgpu_session_s {
   DevBuf<uint64_t> seg_key, thr;
   DevBuf<int32_t> saved_part;
   int64_t scan_tmp_n = 0;
-  int epoch = 0;
   // results of the last refine
   std::vector<lpgpu_round_stats> last_stats;
   // timing
@@ -109,6 +108,9 @@ struct lpgpu_session_s {
   PhaseTimer timer;
   std::vector<lpgpu_phase_time> phase_times;
   cudaEvent_t slots[16] = {};
+  // cached CUDA graph of the refine sequence and the parameters baked into it
+  cudaGraphExec_t graph = nullptr;
+  std::vector<unsigned char> graph_key;
 
   Launch launch() const { return Launch{st, num_sms}; }
 
@@ -236,6 +238,8 @@ lpgpu_status validate_csr(int64_t n, int64_t m, const int64_t* net_off, const in
     if (w < 0) return invalid("vertex weights must be >= 0");
     tw += w;
   }
+  if (tw > INT32_MAX)
+    return invalid("total vertex weight exceeds int32 (the reference's HypernodeWeight)");
   *total_vw = tw;
   return LPGPU_OK;
 }
@@ -313,6 +317,7 @@ lpgpu_status lpgpu_session_destroy(lpgpu_session* s) {
     s->scal.release(&s->footprint);
     for (auto& ev : s->slots)
       if (ev) cudaEventDestroy(ev);
+    if (s->graph) cudaGraphExecDestroy(s->graph);
     cudaStreamDestroy(s->st);
   }
   delete s;
@@ -378,7 +383,6 @@ lpgpu_status lpgpu_session_upload(lpgpu_session* s, int64_t n, int64_t m, const 
     }
     CK(cudaMemsetAsync(s->net_epoch.p, 0, sizeof(int32_t) * m, st));
   }
-  s->epoch = 0;
   CK(launch_build_incidence(s->launch(), n, m, s->net_off.p, s->pins.p, s->vtx_off.p, s->inets.p,
                             reinterpret_cast<int64_t*>(s->seg_key.p), s->scan_tmp.p, s->scan_tmp_n));
   CK(cudaStreamSynchronize(st));
@@ -482,8 +486,6 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
   int64_t* fp = &s->footprint;
   CK(s->stats.alloc(std::max(1, R) * kStats, fp));
   cudaStream_t st = s->st;
-  CK(cudaMemsetAsync(s->stats.p, 0, sizeof(int64_t) * std::max(1, R) * kStats, st));
-  CK(cudaMemsetAsync(s->blk64.p, 0, sizeof(int64_t) * (7 * s->k + 1), st));
   int64_t km1_before = 0;
   lpgpu_status ms = read_metrics(s, &km1_before, nullptr);
   if (ms != LPGPU_OK) return ms;
@@ -494,20 +496,77 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
   if (num_nodes > 0) {
     CK(dnodes.alloc(num_nodes, &tmpfp));
     CK(cudaMemcpyAsync(dnodes.p, nodes, sizeof(int32_t) * num_nodes, cudaMemcpyHostToDevice, st));
-    CK(launch_mark_list(L, c, dnodes.p, num_nodes));
-  } else {
-    if (s->n > 0) CK(cudaMemsetAsync(s->next_flag.p, 0, s->n, st));
-    CK(launch_mark_all(L, c, cfg.rebalancing));
   }
   PhaseTimer* tm = s->timing ? &s->timer : nullptr;
-  if (tm) tm->reset();
-  for (int r = 0; r < R; ++r) {
-    CK(launch_bin_active(L, c, r, S, s->tile_cnt.p, s->tile_off.p, s->scan_tmp.p, s->scan_tmp_n, tm));
-    ++s->epoch;
-    for (int sub = 0; sub < S; ++sub) CK(launch_subround(L, c, r, sub, s->epoch, tm));
+  // The whole refine is a fixed sequence of launches whose element counts live
+  // in device memory, so it is captured once as a CUDA graph and replayed.
+  auto enqueue = [&]() -> cudaError_t {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(s->stats.p, 0, sizeof(int64_t) * std::max(1, R) * kStats, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(s->blk64.p, 0, sizeof(int64_t) * (7 * s->k + 1), st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(s->scal.p, 0, sizeof(int64_t) * kScalars, st)) != cudaSuccess) return e;
+    if (s->m > 0 && (e = cudaMemsetAsync(s->net_epoch.p, 0, sizeof(int32_t) * s->m, st)) != cudaSuccess) return e;
+    if (num_nodes > 0) {
+      if ((e = launch_mark_list(L, c, dnodes.p, num_nodes)) != cudaSuccess) return e;
+    } else {
+      if (s->n > 0 && (e = cudaMemsetAsync(s->next_flag.p, 0, s->n, st)) != cudaSuccess) return e;
+      if ((e = launch_mark_all(L, c, cfg.rebalancing)) != cudaSuccess) return e;
+    }
+    for (int r = 0; r < R; ++r) {
+      if ((e = launch_bin_active(L, c, r, S, s->tile_cnt.p, s->tile_off.p, s->scan_tmp.p, s->scan_tmp_n, tm)) != cudaSuccess)
+        return e;
+      for (int sub = 0; sub < S; ++sub)
+        if ((e = launch_subround(L, c, r, sub, tm)) != cudaSuccess) return e;
+      if (r + 1 < R && (e = launch_expand_nets(L, c, tm)) != cudaSuccess) return e;
+    }
+    // drop flags left by the last round
+    if (s->n > 0 && (e = cudaMemsetAsync(s->next_flag.p, 0, s->n, st)) != cudaSuccess) return e;
+    return cudaSuccess;
+  };
+  if (num_nodes > 0) {
+    if (tm) tm->reset();
+    CK(enqueue());
+  } else {
+    // key: every pointer and parameter baked into the captured launches
+    struct Key {
+      RoundCtx c;
+      int R, S, timing;
+      int64_t* p[3];
+      int64_t scan_n;
+    } key;
+    std::memset(&key, 0, sizeof(key));
+    key.c = c;
+    key.R = R;
+    key.S = S;
+    key.timing = tm != nullptr;
+    key.p[0] = s->tile_cnt.p;
+    key.p[1] = s->tile_off.p;
+    key.p[2] = s->scan_tmp.p;
+    key.scan_n = s->scan_tmp_n;
+    std::vector<unsigned char> kb(reinterpret_cast<unsigned char*>(&key),
+                                  reinterpret_cast<unsigned char*>(&key) + sizeof(key));
+    if (!s->graph || s->graph_key != kb) {
+      if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+      }
+      if (tm) tm->reset();
+      cudaGraph_t g0 = nullptr;
+      CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+      const cudaError_t ce = enqueue();
+      const cudaError_t ee = cudaStreamEndCapture(st, &g0);
+      if (ce != cudaSuccess) {
+        if (g0) cudaGraphDestroy(g0);
+        return cuda_fail(ce, "enqueue refine (capture)");
+      }
+      CK(ee);
+      const cudaError_t ie = cudaGraphInstantiate(&s->graph, g0, 0);
+      cudaGraphDestroy(g0);
+      CK(ie);
+      s->graph_key = kb;
+    }
+    CK(cudaGraphLaunch(s->graph, st));
   }
-  // drop flags left by the last round
-  if (s->n > 0) CK(cudaMemsetAsync(s->next_flag.p, 0, s->n, st));
   std::vector<int64_t> hs(std::max(1, R) * kStats);
   CK(cudaMemcpyAsync(hs.data(), s->stats.p, sizeof(int64_t) * hs.size(), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
