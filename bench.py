@@ -237,11 +237,10 @@ def gpu_arm(args):
     s.upload(hg)
     s.set_partition(inst.k, inst.part, lmax=inst.lmax, perfect=inst.perfect)
     s.save_partition()
-    s.enable_timing(True)
 
     def step():
         s.restore_partition()
-        return s.refine(cfg), s.round_stats(), s.phase_times()
+        return s.refine(cfg)
 
     for _ in range(max(3, args.warmup)):
         step()
@@ -249,23 +248,36 @@ def gpu_arm(args):
     dist.barrier()
     s.synchronize()
     clocks.start()
+    # timed region 1: whole steps (CUDA-graph replay), device time between events
     launches0 = lpgpu.kernel_launches()
     s.record(0)
     pins = 0
-    sweep_ms = 0.0
-    sweep_launches = 0
-    sweep_alg = 0
     results = []
     for _ in range(args.steps):
-        r, stats, phases = step()
+        r = step()
         pins += r.pins_processed
-        sweep_ms += phases["sweep"][1]
-        sweep_launches += phases["sweep"][0]
-        sweep_alg += sweep_bytes(stats, inst.k)
         results.append(r)
     s.record(1)
     elapsed_ms = s.elapsed_ms(0, 1)
     launches = lpgpu.kernel_launches() - launches0
+    # timed region 2: the same steps with CUDA events around every phase
+    # (direct launches) for the per-kernel roofline of the sweep
+    s.enable_timing(True)
+    sweep_ms = 0.0
+    sweep_launches = 0
+    sweep_alg = 0
+    phase_tot = {}
+    for _ in range(args.steps):
+        step()
+        stats, phases = s.round_stats(), s.phase_times()
+        sweep_ms += phases["sweep"][1]
+        sweep_launches += phases["sweep"][0]
+        sweep_alg += sweep_bytes(stats, inst.k)
+        for name, (cnt, ms) in phases.items():
+            a = phase_tot.setdefault(name, [0, 0.0])
+            a[0] += cnt
+            a[1] += ms
+    s.enable_timing(False)
     clk = clocks.stop()
     dist.barrier()
     max_ms = dist.reduce(elapsed_ms, "max")
@@ -300,6 +312,7 @@ def gpu_arm(args):
             "config": dict(config_dict(args, inst, cfg), parallelism=f"replicas{world}"),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk,
+            "phases_ms_per_step": {k: round(v[1] / args.steps, 3) for k, v in sorted(phase_tot.items())},
             "quality": {"km1_before": r0.km1_before, "km1_after": r0.km1_after, "delta": r0.delta,
                         "moves": r0.moves, "imbalance": r0.imbalance, "rounds": r0.rounds}}
     if rank == 0:

@@ -107,6 +107,9 @@ struct RoundCtx {
 
 // Kernels launched by this thread through the library so far.
 int64_t kernel_launches();
+// Adjusts the count (graph capture records kernels without running them;
+// each graph replay runs them).
+void add_kernel_launches(int64_t n);
 
 // Launch helpers (lp_kernels.cu). All launch on `st`; none synchronizes.
 struct Launch {

@@ -77,6 +77,7 @@ static int grid_for(const Launch& L, int64_t work_items, int threads, int per_sm
 // earlier call) through the library's error text.
 static thread_local int64_t t_launches = 0;
 int64_t kernel_launches() { return t_launches; }
+void add_kernel_launches(int64_t n) { t_launches += n; }
 
 static cudaError_t launched(const char* name) {
   ++t_launches;

@@ -111,6 +111,7 @@ struct lpgpu_session_s {
   // cached CUDA graph of the refine sequence and the parameters baked into it
   cudaGraphExec_t graph = nullptr;
   std::vector<unsigned char> graph_key;
+  int64_t graph_kernels = 0;  // kernel nodes in the cached graph
 
   Launch launch() const { return Launch{st, num_sms}; }
 
@@ -204,6 +205,7 @@ struct DeviceGuard {
   int prev = -1;
   explicit DeviceGuard(int dev) {
     g_error.clear();
+    cudaGetLastError();  // drop a stale non-sticky error of an earlier unchecked call
     if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
     if (prev != dev) cudaSetDevice(dev);
   }
@@ -523,7 +525,8 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
     if (s->n > 0 && (e = cudaMemsetAsync(s->next_flag.p, 0, s->n, st)) != cudaSuccess) return e;
     return cudaSuccess;
   };
-  if (num_nodes > 0) {
+  if (num_nodes > 0 || tm) {
+    // direct launches: explicit node lists, and per-phase event timing
     if (tm) tm->reset();
     CK(enqueue());
   } else {
@@ -538,7 +541,7 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
     key.c = c;
     key.R = R;
     key.S = S;
-    key.timing = tm != nullptr;
+    key.timing = 0;
     key.p[0] = s->tile_cnt.p;
     key.p[1] = s->tile_off.p;
     key.p[2] = s->scan_tmp.p;
@@ -550,11 +553,13 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
         cudaGraphExecDestroy(s->graph);
         s->graph = nullptr;
       }
-      if (tm) tm->reset();
       cudaGraph_t g0 = nullptr;
+      const int64_t l0 = kernel_launches();
       CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
       const cudaError_t ce = enqueue();
       const cudaError_t ee = cudaStreamEndCapture(st, &g0);
+      s->graph_kernels = kernel_launches() - l0;
+      add_kernel_launches(-s->graph_kernels);  // recorded, not run
       if (ce != cudaSuccess) {
         if (g0) cudaGraphDestroy(g0);
         return cuda_fail(ce, "enqueue refine (capture)");
@@ -566,6 +571,7 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
       s->graph_key = kb;
     }
     CK(cudaGraphLaunch(s->graph, st));
+    add_kernel_launches(s->graph_kernels);
   }
   std::vector<int64_t> hs(std::max(1, R) * kStats);
   CK(cudaMemcpyAsync(hs.data(), s->stats.p, sizeof(int64_t) * hs.size(), cudaMemcpyDeviceToHost, st));
@@ -575,7 +581,7 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
     std::map<int, lpgpu_phase_time> acc;
     for (auto& rec : tm->recs) {
       float ms_ = 0.f;
-      cudaEventElapsedTime(&ms_, rec.a, rec.b);
+      CK(cudaEventElapsedTime(&ms_, rec.a, rec.b));
       auto& a = acc[rec.phase];
       a.launches += 1;
       a.ms += ms_;
