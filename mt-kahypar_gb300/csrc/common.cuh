@@ -102,6 +102,7 @@ struct RoundCtx {
   int64_t* stats;        // rounds x kStats
   // parameters
   int32_t zero_gain, revert, rollback;
+  int32_t unit_nets;     // every net weight is 1
   int64_t act_threshold;
 };
 

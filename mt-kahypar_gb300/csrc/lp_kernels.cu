@@ -375,26 +375,48 @@ __device__ __forceinline__ int plane_sum(const Planes& p, uint32_t mask, int w) 
 // block (slack(b) >= w(v), b != from) of minimum score < 0, lowest id on ties.
 // Without one, and with zero_gain, the lowest feasible block of score 0 is
 // taken if the rebalancing rule of label_propagation_refiner.h:88-95 holds.
-template <int W>
+template <int W, bool PACKED>
 __device__ __forceinline__ void decide(int k, int from, int wv, int internal, int zero_gain,
                                        const int (&pen)[W], const int (&slack)[W],
                                        const int64_t* __restrict__ s_bw,
                                        const int64_t* __restrict__ s_perf, int& to, int& gain) {
   const int lane = lane_id();
-  int bp = -1, bb = INT_MAX, zb = INT_MAX;
+  int zb = INT_MAX;
+  if constexpr (PACKED) {
+    // penalties below 2^20: one max over (pen << 11 | 2047 - blk) gives the
+    // largest penalty and, on ties, the lowest block; 0 = no feasible block
+    unsigned key = 0;
 #pragma unroll
-  for (int t = 0; t < W; ++t) {
-    const int blk = 32 * t + lane;
-    if (blk < k && blk != from && slack[t] >= wv) {
-      if (pen[t] > bp) { bp = pen[t]; bb = blk; }
-      if (zb == INT_MAX && pen[t] == internal) zb = blk;
+    for (int t = 0; t < W; ++t) {
+      const int blk = 32 * t + lane;
+      if (blk < k && blk != from && slack[t] >= wv) {
+        const unsigned kk = ((unsigned)pen[t] << 11) | (unsigned)(2047 - blk);
+        key = kk > key ? kk : key;
+        if (zb == INT_MAX && pen[t] == internal) zb = blk;
+      }
     }
-  }
-  const int mp = __reduce_max_sync(FULLMASK, bp);
-  if (mp > internal) {
-    to = __reduce_min_sync(FULLMASK, bp == mp ? bb : INT_MAX);
-    gain = internal - mp;
-    return;
+    const unsigned mk = __reduce_max_sync(FULLMASK, key);
+    if (mk != 0 && (int)(mk >> 11) > internal) {
+      to = 2047 - (int)(mk & 2047u);
+      gain = internal - (int)(mk >> 11);
+      return;
+    }
+  } else {
+    int bp = -1, bb = INT_MAX;
+#pragma unroll
+    for (int t = 0; t < W; ++t) {
+      const int blk = 32 * t + lane;
+      if (blk < k && blk != from && slack[t] >= wv) {
+        if (pen[t] > bp) { bp = pen[t]; bb = blk; }
+        if (zb == INT_MAX && pen[t] == internal) zb = blk;
+      }
+    }
+    const int mp = __reduce_max_sync(FULLMASK, bp);
+    if (mp > internal) {
+      to = __reduce_min_sync(FULLMASK, bp == mp ? bb : INT_MAX);
+      gain = internal - mp;
+      return;
+    }
   }
   if (zero_gain) {
     const int z = __reduce_min_sync(FULLMASK, zb);
@@ -428,8 +450,8 @@ __device__ void plan_to(const RoundCtx& c);
 // Outputs: sub-round mode writes rec[pos] = (to, gain) or to = -1 and the
 // per-block candidate totals; query mode (dbg_to != null) writes to / gain /
 // border for every vertex (list = all vertices, no zero-gain moves).
-template <int W>
-__global__ void __launch_bounds__(kSweepThreads) k_sweep(RoundCtx c, int round, int sub,
+template <int W, bool UNIT>
+__global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(RoundCtx c, int round, int sub,
                                                           int32_t* dbg_to, int32_t* dbg_gain,
                                                           uint8_t* dbg_border) {
   extern __shared__ unsigned char smem_raw[];
@@ -512,8 +534,8 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(RoundCtx c, int round, 
       for (int t = 0; t < W; ++t) words[t] = 0;
       int we = 0, ic = 0, lam = 0;
       if (has) {
-        const int64_t e = __ldg(&c.inets[o_ow + lane - st_ow]);
-        we = __ldg(&c.w_e[e]);
+        const int64_t e = __ldcs(&c.inets[o_ow + lane - st_ow]);
+        we = UNIT ? 1 : __ldg(&c.w_e[e]);
         const uint32_t* rec = c.conn + e * W2;
         load_words<W>(rec, words);
         const uint32_t l1 = __ldg(rec + W + (from_ow >> 5));
@@ -525,10 +547,11 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(RoundCtx c, int round, 
       uint32_t col[W];
 #pragma unroll
       for (int t = 0; t < W; ++t) col[t] = transpose32(words[t]);
-      const unsigned wor = __reduce_or_sync(FULLMASK, (unsigned)we);
-      const int nplanes = 32 - __clz(wor);
-      const Planes wp = make_planes(we, nplanes);
-      const Planes ip = make_planes(ic, nplanes);
+      int nplanes = 1;
+      if constexpr (!UNIT) nplanes = 32 - __clz(__reduce_or_sync(FULLMASK, (unsigned)we));
+      const Planes wp = make_planes(we, UNIT ? 0 : nplanes);
+      const Planes ip = make_planes(ic, UNIT ? 0 : nplanes);
+      const unsigned icb = __ballot_sync(FULLMASK, ic != 0);
       unsigned pm = pmask;
       while (pm) {
         const int j = __ffs(pm) - 1;
@@ -539,12 +562,19 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(RoundCtx c, int round, 
         if ((bm & mj) == 0) continue;  // not a border vertex
         const int fromj = __shfl_sync(FULLMASK, from, j);
         const int wvj = __shfl_sync(FULLMASK, wv, j);
-        const int internal = plane_sum(ip, mj, ic);
+        int internal;
         int pen[W];
+        if constexpr (UNIT) {
+          internal = __popc(icb & mj);
 #pragma unroll
-        for (int t = 0; t < W; ++t) pen[t] = plane_sum(wp, col[t] & mj, we);
+          for (int t = 0; t < W; ++t) pen[t] = __popc(col[t] & mj);
+        } else {
+          internal = plane_sum(ip, mj, ic);
+#pragma unroll
+          for (int t = 0; t < W; ++t) pen[t] = plane_sum(wp, col[t] & mj, we);
+        }
         int to = fromj, gain = 0;
-        decide<W>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
+        decide<W, UNIT>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
         if (lane == j) {
           my_to = to;
           my_gain = gain;
@@ -575,8 +605,8 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(RoundCtx c, int round, 
         for (int t = 0; t < W; ++t) words[t] = 0;
         int we = 0, ic = 0, lam = 0;
         if (has) {
-          const int64_t e = __ldg(&c.inets[oj + base + lane]);
-          we = __ldg(&c.w_e[e]);
+          const int64_t e = __ldcs(&c.inets[oj + base + lane]);
+          we = UNIT ? 1 : __ldg(&c.w_e[e]);
           const uint32_t* rec = c.conn + e * W2;
           load_words<W>(rec, words);
           const uint32_t l1 = __ldg(rec + W + (fromj >> 5));
@@ -585,16 +615,21 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(RoundCtx c, int round, 
           for (int t = 0; t < W; ++t) lam += __popc(words[t]);
         }
         border |= __any_sync(FULLMASK, lam > 1);
-        const unsigned wor = __reduce_or_sync(FULLMASK, (unsigned)we);
-        const int nplanes = 32 - __clz(wor);
-        const Planes wp = make_planes(we, nplanes);
         internal += __reduce_add_sync(FULLMASK, (unsigned)ic);
+        if constexpr (UNIT) {
 #pragma unroll
-        for (int t = 0; t < W; ++t) pen[t] += plane_sum(wp, transpose32(words[t]), we);
+          for (int t = 0; t < W; ++t) pen[t] += __popc(transpose32(words[t]));
+        } else {
+          const int nplanes = 32 - __clz(__reduce_or_sync(FULLMASK, (unsigned)we));
+          const Planes wp = make_planes(we, nplanes);
+#pragma unroll
+          for (int t = 0; t < W; ++t) pen[t] += plane_sum(wp, transpose32(words[t]), we);
+        }
       }
       if (!border) continue;
       int to = fromj, gain = 0;
-      decide<W>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
+      // big vertices can exceed the packed-key penalty range
+      decide<W, false>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
       if (lane == j) {
         my_to = to;
         my_gain = gain;
@@ -675,7 +710,7 @@ static cudaError_t launch_sweep(const Launch& L, const RoundCtx& c, int round, i
   if (word_class(c.W) != c.W) return cudaErrorInvalidValue;
   const size_t smem = sweep_smem(c.k);
   LPGPU_DISPATCH_W(c.W, {
-    auto kern = k_sweep<kW>;
+    auto kern = c.unit_nets ? k_sweep<kW, true> : k_sweep<kW, false>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int per_sm = occupancy((const void*)kern, kSweepThreads, smem);
     kern<<<grid_for(L, c.n * 4, kSweepThreads, per_sm), kSweepThreads, smem, L.st>>>(c, round, sub, to, gain, border);
@@ -1257,18 +1292,6 @@ __global__ void __launch_bounds__(kSelThreads) k_from_side(RoundCtx c, int sub) 
   }
 }
 
-// Activation of a kept move (moveVertex, label_propagation_refiner.h:112-128):
-// the vertex becomes active for the next round and its nets with
-// |e| <= threshold are stamped with the round's epoch; k_expand_nets marks
-// their pins at the end of the round (each net expanded once per round).
-__device__ __forceinline__ void warp_activate(const RoundCtx& c, int64_t v, int epoch) {
-  if (lane_id() == 0) c.next_flag[v] = 1;
-  for (int64_t q = c.vtx_off[v] + lane_id(); q < c.vtx_off[v + 1]; q += 32) {
-    const int64_t e = c.inets[q];
-    if (c.net_off[e + 1] - c.net_off[e] <= c.act_threshold) c.net_epoch[e] = epoch;
-  }
-}
-
 // Books the sub-round's delta into the round statistics and clears the
 // sweep accumulators for the next sub-round (last CTA of the last kernel).
 __device__ void close_subround(const RoundCtx& c, int round) {
@@ -1282,16 +1305,118 @@ __device__ void close_subround(const RoundCtx& c, int round) {
   }
 }
 
+// Incidence packing shared by the kernels that walk the incidences of a set
+// of vertices (one per lane). Vertices of degree 1..32 are packed greedily
+// into groups of <= 32 incidences (lane = incidence, contiguous per vertex);
+// longer vertices are walked alone in 32-incidence chunks. For every group
+// `body(has, ow, j, seg_end)` runs on all lanes: lane `has` holds incidence j
+// (index into inets) of the vertex held by lane `ow`. The return value is, on
+// each selected lane, the sum over its vertex's incidences of the ints
+// returned by body (segmented sums inside a group).
+template <typename Body>
+__device__ __forceinline__ int packed_incidences(bool sel, int64_t o0, int deg,
+                                                 unsigned char* __restrict__ s_owner, Body&& body) {
+  const int lane = lane_id();
+  int my_total = 0;
+  const bool small = sel && deg >= 1 && deg <= 32;
+  const int dsm = small ? deg : 0;
+  int incl = dsm;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(FULLMASK, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int excl = incl - dsm;
+  unsigned rem = __ballot_sync(FULLMASK, small);
+  while (rem) {
+    const int q = __ffs(rem) - 1;
+    const int start = __shfl_sync(FULLMASK, excl, q);
+    const bool inpack = ((rem >> lane) & 1u) && incl - start <= 32;
+    const unsigned pmask = __ballot_sync(FULLMASK, inpack);
+    const int D = __shfl_sync(FULLMASK, incl, 31 - __clz(pmask)) - start;
+    const int st = excl - start;
+    __syncwarp();
+    if (inpack) s_owner[__popc(pmask & lanemask_lt())] = (unsigned char)lane;
+    const unsigned starts = __reduce_or_sync(FULLMASK, inpack ? (1u << st) : 0u);
+    __syncwarp();
+    const bool has = lane < D;
+    const int ow = has ? s_owner[__popc(starts & ((2u << lane) - 1u)) - 1] : lane;
+    const int64_t o_ow = __shfl_sync(FULLMASK, o0, ow);
+    const int st_ow = __shfl_sync(FULLMASK, st, ow);
+    const int d_ow = __shfl_sync(FULLMASK, deg, ow);
+    const int seg_end = has ? st_ow + d_ow : lane + 1;
+    int x = body(has, ow, has ? o_ow + lane - st_ow : (int64_t)0);
+    // segmented suffix sums: the first lane of every vertex gets its total
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_down_sync(FULLMASK, x, o);
+      if (lane + o < seg_end) x += y;
+    }
+    const int tot = __shfl_sync(FULLMASK, x, inpack ? st : 0);
+    if (inpack) my_total = tot;
+    rem &= ~pmask;
+  }
+  unsigned bigm = __ballot_sync(FULLMASK, sel && deg > 32);
+  while (bigm) {
+    const int j = __ffs(bigm) - 1;
+    bigm &= bigm - 1;
+    const int64_t oj = __shfl_sync(FULLMASK, o0, j);
+    const int dj = __shfl_sync(FULLMASK, deg, j);
+    int acc = 0;
+    for (int base = 0; base < dj; base += 32) {
+      const bool has = base + lane < dj;
+      acc += body(has, j, has ? oj + base + lane : (int64_t)0);
+    }
+    acc = warp_sum(acc);
+    if (lane == j) my_total = acc;
+  }
+  return my_total;
+}
+
+// One incidence of a move from f to t: atomic decrement of Φ(e,f) and
+// increment of Φ(e,t) with the Λ / Λ1 toggles of warp_commit_vertex; returns
+// the attributed delta of this incidence.
+__device__ __forceinline__ int commit_incidence(const RoundCtx& c, int64_t e, int f, int t) {
+  const int W = c.W;
+  const int we = c.unit_nets ? 1 : c.w_e[e];
+  uint32_t* rec = c.conn + e * 2 * W;
+  const uint32_t fbit = 1u << (f & 31), tbit = 1u << (t & 31);
+  int att = 0;
+  const int of = atomicSub(&c.phi[e * c.k + f], 1);
+  if (of == 1) {
+    atomicXor(&rec[f >> 5], fbit);
+    att -= we;
+  }
+  if (of == 1 || of == 2) atomicXor(&rec[W + (f >> 5)], fbit);
+  const int ot = atomicAdd(&c.phi[e * c.k + t], 1);
+  if (ot == 0) {
+    atomicXor(&rec[t >> 5], tbit);
+    att += we;
+  }
+  if (ot == 0 || ot == 1) atomicXor(&rec[W + (t >> 5)], tbit);
+  return att;
+}
+
+// Activation stamp of one incident net of a kept move (see k_expand_nets).
+__device__ __forceinline__ void activate_incidence(const RoundCtx& c, int64_t e, int epoch) {
+  if (c.net_off[e + 1] - c.net_off[e] <= c.act_threshold) c.net_epoch[e] = epoch;
+}
+
+constexpr int kPackThreads = 256;
+
 // Commit of the accepted moves (changeNodePart, h:539-563, without the
 // per-move weight check: the selection already guarantees both bounds).
 // Marks status[pos] = 1 for committed moves and overwrites rec[pos].y with
 // the source block (the gain is no longer needed). With `last`, the moves
-// are final: they are activated and the sub-round is closed.
-__global__ void k_commit(RoundCtx c, int round, int sub, int last) {
+// are final: they are activated (moveVertex, label_propagation_refiner.h:112-128)
+// and the sub-round is closed.
+__global__ void __launch_bounds__(kPackThreads, 4) k_commit(RoundCtx c, int round, int sub, int last) {
   extern __shared__ ull s_dw[];
+  __shared__ unsigned char s_own[kPackThreads];
   for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_dw[b] = 0;
   __syncthreads();
   const int lane = lane_id();
+  unsigned char* own = s_own + (threadIdx.x & ~31);
   const int epoch = (int)c.scal[kEpoch];
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
   int64_t att = 0, moved = 0;
@@ -1301,7 +1426,8 @@ __global__ void k_commit(RoundCtx c, int round, int sub, int last) {
     const int64_t pos = base + lane;
     int2 r = make_int2(-1, 0);
     int32_t v = 0;
-    int f = 0;
+    int f = 0, deg = 0;
+    int64_t o0 = 0;
     bool acc = false;
     if (pos < end) {
       r = c.rec[pos];
@@ -1310,26 +1436,33 @@ __global__ void k_commit(RoundCtx c, int round, int sub, int last) {
         f = c.part[v];
         const uint64_t key = move_key(r.y, v);
         acc = key < c.thr_to[r.x] && key < c.thr_from[f];
-        if (acc) c.rec[pos].y = f;
+        if (acc) {
+          c.rec[pos].y = f;
+          o0 = c.vtx_off[v];
+          deg = (int)(c.vtx_off[v + 1] - o0);
+        }
       }
       c.status[pos] = acc ? 1 : 0;
     }
-    unsigned mask = __ballot_sync(FULLMASK, acc);
-    while (mask) {
-      const int j = __ffs(mask) - 1;
-      mask &= mask - 1;
-      const int32_t vj = __shfl_sync(FULLMASK, v, j);
-      const int fj = __shfl_sync(FULLMASK, f, j);
-      const int tj = __shfl_sync(FULLMASK, r.x, j);
-      att += warp_commit_vertex(c, vj, fj, tj);
-      if (last) warp_activate(c, vj, epoch);
-      if (lane == 0) {
-        c.part[vj] = tj;
-        const int64_t wv = c.w_v[vj];
-        atomicAdd(&s_dw[tj], (ull)wv);
-        atomicAdd(&s_dw[fj], (ull)(-wv));
-        ++moved;
+    const int tot = packed_incidences(acc, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
+      const int fo = __shfl_sync(FULLMASK, f, ow);
+      const int to = __shfl_sync(FULLMASK, r.x, ow);
+      int a = 0;
+      if (has) {
+        const int64_t e = c.inets[j];
+        a = commit_incidence(c, e, fo, to);
+        if (last) activate_incidence(c, e, epoch);
       }
+      return a;
+    });
+    if (acc) {
+      att += tot;
+      c.part[v] = r.x;
+      if (last) c.next_flag[v] = 1;
+      const int64_t wv = c.w_v[v];
+      atomicAdd(&s_dw[r.x], (ull)wv);
+      atomicAdd(&s_dw[f], (ull)(-wv));
+      ++moved;
     }
   }
   att = block_sum_i64(att);
@@ -1349,8 +1482,10 @@ __global__ void k_commit(RoundCtx c, int round, int sub, int last) {
 // when moving the vertex back to f now strictly improves km1. This is the
 // deterministic counterpart of the realised-gain check of moveVertex
 // (label_propagation_refiner.h:100-137).
-__global__ void k_revert_eval(RoundCtx c, int sub) {
+__global__ void __launch_bounds__(kPackThreads, 4) k_revert_eval(RoundCtx c, int sub) {
+  __shared__ unsigned char s_own[kPackThreads];
   const int lane = lane_id();
+  unsigned char* own = s_own + (threadIdx.x & ~31);
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
   const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
   const int W = c.W;
@@ -1358,26 +1493,29 @@ __global__ void k_revert_eval(RoundCtx c, int sub) {
        base += stride) {
     const int64_t pos = base + lane;
     const bool moved = pos < end && c.status[pos] == 1;
-    unsigned mask = __ballot_sync(FULLMASK, moved);
-    while (mask) {
-      const int j = __ffs(mask) - 1;
-      mask &= mask - 1;
-      const int64_t pj = base + j;
-      const int64_t v = c.list[pj];
-      const int2 r = c.rec[pj];  // (to, from)
-      const int t = r.x, f = r.y;
-      const uint32_t fbit = 1u << (f & 31), tbit = 1u << (t & 31);
-      int score = 0;
-      for (int64_t q = c.vtx_off[v] + lane; q < c.vtx_off[v + 1]; q += 32) {
-        const int64_t e = c.inets[q];
-        const int we = c.w_e[e];
-        const uint32_t* rec = c.conn + e * 2 * W;
-        if (!(rec[W + (t >> 5)] & tbit)) score += we;   // Φ(e, t) > 1
-        if (rec[f >> 5] & fbit) score -= we;            // f in Λ(e)
-      }
-      score = warp_sum(score);
-      if (lane == 0 && score < 0) c.status[pj] = 2;
+    int2 r = make_int2(0, 0);  // (to, from)
+    int64_t o0 = 0;
+    int deg = 0;
+    if (moved) {
+      r = c.rec[pos];
+      const int64_t v = c.list[pos];
+      o0 = c.vtx_off[v];
+      deg = (int)(c.vtx_off[v + 1] - o0);
     }
+    const int score = packed_incidences(moved, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
+      const int t = __shfl_sync(FULLMASK, r.x, ow);
+      const int f = __shfl_sync(FULLMASK, r.y, ow);
+      int x = 0;
+      if (has) {
+        const int64_t e = c.inets[j];
+        const int we = c.unit_nets ? 1 : c.w_e[e];
+        const uint32_t* rec = c.conn + e * 2 * W;
+        if (!((rec[W + (t >> 5)] >> (t & 31)) & 1u)) x += we;  // Φ(e, t) > 1
+        if ((rec[f >> 5] >> (f & 31)) & 1u) x -= we;           // f in Λ(e)
+      }
+      return x;
+    });
+    if (moved && score < 0) c.status[pos] = 2;
   }
 }
 
@@ -1385,12 +1523,14 @@ __global__ void k_revert_eval(RoundCtx c, int sub) {
 // (rollback): when the sub-round's delta is positive, undo of all moves still
 // marked 1 (status 3). With `last`, the moves that stay are activated and the
 // sub-round is closed.
-__global__ void k_undo(RoundCtx c, int round, int sub, int rollback, int last) {
+__global__ void __launch_bounds__(kPackThreads, 4) k_undo(RoundCtx c, int round, int sub, int rollback, int last) {
   const bool roll = rollback && c.scal[kDeltaSub] > 0;  // kDeltaSub is not written here
   extern __shared__ ull s_dw[];
+  __shared__ unsigned char s_own[kPackThreads];
   for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_dw[b] = 0;
   __syncthreads();
   const int lane = lane_id();
+  unsigned char* own = s_own + (threadIdx.x & ~31);
   const int epoch = (int)c.scal[kEpoch];
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
   const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
@@ -1402,28 +1542,35 @@ __global__ void k_undo(RoundCtx c, int round, int sub, int rollback, int last) {
       const uint8_t st = pos < end ? c.status[pos] : 0;
       const bool sel = rollback ? (roll && st == 1) : st == 2;
       const bool keep = last && st == 1 && !sel;
-      unsigned mask = __ballot_sync(FULLMASK, sel);
-      while (mask) {
-        const int j = __ffs(mask) - 1;
-        mask &= mask - 1;
-        const int64_t pj = base + j;
-        const int64_t v = c.list[pj];
-        const int2 r = c.rec[pj];  // (to, from)
-        att += warp_commit_vertex(c, v, r.x, r.y);
-        if (lane == 0) {
-          c.part[v] = r.y;
-          const int64_t wv = c.w_v[v];
-          atomicAdd(&s_dw[r.y], (ull)wv);
-          atomicAdd(&s_dw[r.x], (ull)(-wv));
-          if (rollback) c.status[pj] = 3;
-          ++undone;
-        }
+      int2 r = make_int2(0, 0);  // (to, from)
+      int64_t v = 0, o0 = 0;
+      int deg = 0;
+      if (sel || keep) {
+        r = c.rec[pos];
+        v = c.list[pos];
+        o0 = c.vtx_off[v];
+        deg = (int)(c.vtx_off[v + 1] - o0);
       }
-      unsigned kmask = __ballot_sync(FULLMASK, keep);
-      while (kmask) {
-        const int j = __ffs(kmask) - 1;
-        kmask &= kmask - 1;
-        warp_activate(c, c.list[base + j], epoch);
+      const int tot = packed_incidences(sel, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
+        const int t = __shfl_sync(FULLMASK, r.x, ow);
+        const int f = __shfl_sync(FULLMASK, r.y, ow);
+        return has ? commit_incidence(c, c.inets[j], t, f) : 0;
+      });
+      if (sel) {
+        att += tot;
+        c.part[v] = r.y;
+        const int64_t wv = c.w_v[v];
+        atomicAdd(&s_dw[r.y], (ull)wv);
+        atomicAdd(&s_dw[r.x], (ull)(-wv));
+        if (rollback) c.status[pos] = 3;
+        ++undone;
+      }
+      if (last) {
+        packed_incidences(keep, o0, deg, own, [&](bool has, int, int64_t j) -> int {
+          if (has) activate_incidence(c, c.inets[j], epoch);
+          return 0;
+        });
+        if (keep) c.next_flag[v] = 1;
       }
     }
   }
@@ -1476,7 +1623,7 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
     cudaError_t e = launch_sweep(L, c, round, sub, nullptr, nullptr, nullptr);
     if (e != cudaSuccess) return e;
   }
-  const int g = grid_for(L, n, 256, 2);
+  const int g = grid_for(L, n, 256, 8);
   {
     Scope sc(timer, "select");
     k_bin_moves<<<g, 256, 0, L.st>>>(c, sub);

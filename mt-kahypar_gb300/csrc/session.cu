@@ -84,6 +84,7 @@ struct lpgpu_session_s {
   bool has_hg = false;
   int64_t n = 0, m = 0, P = 0;
   int64_t total_vw = 0;
+  bool unit_nets = true;
   DevBuf<int64_t> net_off, vtx_off;
   DevBuf<int32_t> pins, inets, w_v, w_e;
   // partition
@@ -127,6 +128,7 @@ struct lpgpu_session_s {
     c.inets = inets.p;
     c.w_v = w_v.p;
     c.w_e = w_e.p;
+    c.unit_nets = unit_nets ? 1 : 0;
     c.part = part.p;
     c.phi = phi.p;
     c.conn = conn.p;
@@ -341,6 +343,9 @@ lpgpu_status lpgpu_session_upload(lpgpu_session* s, int64_t n, int64_t m, const 
   s->m = m;
   s->P = net_off[m];
   s->total_vw = total;
+  s->unit_nets = true;
+  if (w_e)
+    for (int64_t e = 0; e < m && s->unit_nets; ++e) s->unit_nets = w_e[e] == 1;
   int64_t* fp = &s->footprint;
   const int64_t P = s->P;
   CK(s->net_off.alloc(m + 1, fp));
