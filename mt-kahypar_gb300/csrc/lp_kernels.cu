@@ -435,25 +435,28 @@ __device__ void plan_to(const RoundCtx& c);
 // Sweep: the best move of every active vertex (moveVertex's isBorderNode +
 // computeMaxGainMove, label_propagation_refiner.h:82-95) on the current state.
 //
-// A warp takes a tile of 32 list entries (lane = vertex). Vertices of degree
-// 1..32 are packed greedily into groups of <= 32 incidences (lane = incidence);
-// every incidence lane loads its net's record {Λ(e), Λ1(e)} (one 32-byte
-// sector for k <= 128) and w(e); Λ words are transposed across the warp so
-// that lane l holds, per 32-block word t, the mask of incidences whose net
-// contains block l + 32 t. A vertex's penalty for that block is then a
-// popcount of the mask restricted to its incidence lanes (weighted through
-// bit-planes of w(e)); internal weight (nets with Φ(e, from) > 1, i.e. from
-// not in Λ1(e)) and the border test come from ballots. Vertices of degree
-// > 32 accumulate the same quantities over 32-incidence chunks. Cost per
+// A warp takes a tile of 32 list entries (lane = vertex) and walks the tile's
+// concatenated incidence lists in windows of 32 incidences (lane =
+// incidence); the gathers of B windows are issued before any is consumed.
+// Each incidence lane loads its net's record {Λ(e), Λ1(e)} (one 32-byte
+// sector for k <= 128) and, for weighted nets, w(e); Λ words are transposed
+// across the warp so that lane l holds, per 32-block word t, the mask of
+// incidences whose net contains block l + 32 t. A vertex's penalty for that
+// block is the popcount of the mask restricted to its incidence lanes
+// (through bit-planes of w(e) for weighted nets); its internal weight (nets
+// with Φ(e, from) > 1, i.e. from not in Λ1(e)) and the border test come from
+// ballots. A vertex that straddles windows carries its partial sums. Cost per
 // incidence is independent of |Λ(e)|.
 //
 // Outputs: sub-round mode writes rec[pos] = (to, gain) or to = -1 and the
-// per-block candidate totals; query mode (dbg_to != null) writes to / gain /
-// border for every vertex (list = all vertices, no zero-gain moves).
+// per-block candidate totals, and its last CTA plans the selection; query
+// mode (dbg_to != null) writes to / gain / border for every vertex (list =
+// all vertices, no zero-gain moves).
 template <int W, bool UNIT>
-__global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(RoundCtx c, int round, int sub,
-                                                          int32_t* dbg_to, int32_t* dbg_gain,
-                                                          uint8_t* dbg_border) {
+__global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(RoundCtx c, int round, int sub,
+                                                             int32_t* dbg_to, int32_t* dbg_gain,
+                                                             uint8_t* dbg_border) {
+  constexpr int B = W <= 4 ? 4 : (W <= 8 ? 2 : 1);  // windows whose gathers are issued together
   extern __shared__ unsigned char smem_raw[];
   const int k = c.k;
   const bool query = dbg_to != nullptr;
@@ -486,154 +489,156 @@ __global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(RoundCtx c, int roun
   int64_t pins = 0, cands = 0;
   const int64_t wstride = ((int64_t)gridDim.x * blockDim.x);
   for (int64_t tile = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; tile < cnt; tile += wstride) {
+    // ---- one vertex per lane
     const int64_t pos = beg + tile + lane;
     const bool valid = tile + lane < cnt;
     const int64_t v = valid ? (query ? pos : (int64_t)c.list[pos]) : 0;
     int64_t o0 = 0;
-    int deg = 0, from = 0, wv = 0;
+    int d = 0, from = 0, wv = 0;
     if (valid) {
       o0 = c.vtx_off[v];
-      const int64_t d = c.vtx_off[v + 1] - o0;
-      pins += d;
-      deg = d > kHighDegree ? -1 : (int)d;  // -1: never a border vertex
+      const int64_t dd = c.vtx_off[v + 1] - o0;
+      pins += dd;
+      d = dd > kHighDegree ? 0 : (int)dd;  // isBorderNode is false above the threshold
       from = c.part[v];
       wv = c.w_v[v];
     }
-    int my_to = from, my_gain = 0;
-    bool my_border = false;
-
-    // ---- vertices of degree 1..32, packed into groups of <= 32 incidences
-    const bool small = deg >= 1 && deg <= 32;
-    const int dsm = small ? deg : 0;
-    int incl = dsm;
+    int incl = d;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int y = __shfl_up_sync(FULLMASK, incl, o);
       if (lane >= o) incl += y;
     }
-    const int excl = incl - dsm;
-    unsigned rem = __ballot_sync(FULLMASK, small);
-    while (rem) {
-      const int q = __ffs(rem) - 1;
-      const int start = __shfl_sync(FULLMASK, excl, q);
-      const bool inpack = ((rem >> lane) & 1u) && incl - start <= 32;
-      const unsigned pmask = __ballot_sync(FULLMASK, inpack);
-      const int D = __shfl_sync(FULLMASK, incl, 31 - __clz(pmask)) - start;
-      const int st = excl - start;
-      __syncwarp();
-      if (inpack) s_owner[__popc(pmask & lanemask_lt())] = (unsigned char)lane;
-      const unsigned starts = __reduce_or_sync(FULLMASK, inpack ? (1u << st) : 0u);
-      __syncwarp();
-      const bool has = lane < D;
-      const int ow = has ? s_owner[__popc(starts & ((2u << lane) - 1u)) - 1] : 0;
-      const int64_t o_ow = __shfl_sync(FULLMASK, o0, ow);
-      const int st_ow = __shfl_sync(FULLMASK, st, ow);
-      const int from_ow = __shfl_sync(FULLMASK, from, ow);
-      uint32_t words[W];
+    const int excl = incl - d, eend = incl;
+    const int R = __shfl_sync(FULLMASK, incl, 31);  // incidences of the tile
+    const unsigned nz = __ballot_sync(FULLMASK, d > 0);
+    __syncwarp();
+    if (d > 0) s_owner[__popc(nz & lanemask_lt())] = (unsigned char)lane;
+    __syncwarp();
+    int my_to = from, my_gain = 0;
+    bool my_border = false;
+    // partial sums of the vertex that continues past the current window
+    int carry[W];
 #pragma unroll
-      for (int t = 0; t < W; ++t) words[t] = 0;
-      int we = 0, ic = 0, lam = 0;
-      if (has) {
-        const int64_t e = __ldcs(&c.inets[o_ow + lane - st_ow]);
-        we = UNIT ? 1 : __ldg(&c.w_e[e]);
-        const uint32_t* rec = c.conn + e * W2;
-        load_words<W>(rec, words);
-        const uint32_t l1 = __ldg(rec + W + (from_ow >> 5));
-        ic = ((l1 >> (from_ow & 31)) & 1u) ? 0 : we;
-#pragma unroll
-        for (int t = 0; t < W; ++t) lam += __popc(words[t]);
-      }
-      const unsigned bm = __ballot_sync(FULLMASK, lam > 1);
-      uint32_t col[W];
-#pragma unroll
-      for (int t = 0; t < W; ++t) col[t] = transpose32(words[t]);
-      int nplanes = 1;
-      if constexpr (!UNIT) nplanes = 32 - __clz(__reduce_or_sync(FULLMASK, (unsigned)we));
-      const Planes wp = make_planes(we, UNIT ? 0 : nplanes);
-      const Planes ip = make_planes(ic, UNIT ? 0 : nplanes);
-      const unsigned icb = __ballot_sync(FULLMASK, ic != 0);
-      unsigned pm = pmask;
-      while (pm) {
-        const int j = __ffs(pm) - 1;
-        pm &= pm - 1;
-        const int stj = __shfl_sync(FULLMASK, st, j);
-        const int dj = __shfl_sync(FULLMASK, deg, j);
-        const unsigned mj = (dj == 32) ? FULLMASK : (((1u << dj) - 1u) << stj);
-        if ((bm & mj) == 0) continue;  // not a border vertex
-        const int fromj = __shfl_sync(FULLMASK, from, j);
-        const int wvj = __shfl_sync(FULLMASK, wv, j);
-        int internal;
-        int pen[W];
-        if constexpr (UNIT) {
-          internal = __popc(icb & mj);
-#pragma unroll
-          for (int t = 0; t < W; ++t) pen[t] = __popc(col[t] & mj);
-        } else {
-          internal = plane_sum(ip, mj, ic);
-#pragma unroll
-          for (int t = 0; t < W; ++t) pen[t] = plane_sum(wp, col[t] & mj, we);
-        }
-        int to = fromj, gain = 0;
-        decide<W, UNIT>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
-        if (lane == j) {
-          my_to = to;
-          my_gain = gain;
-          my_border = true;
-        }
-      }
-      rem &= ~pmask;
-    }
+    for (int t = 0; t < W; ++t) carry[t] = 0;
+    int carry_int = 0;
+    bool carry_border = false;
 
-    // ---- vertices of degree 33..kHighDegree, one at a time in 32-incidence chunks
-    unsigned bigm = __ballot_sync(FULLMASK, deg > 32);
-    while (bigm) {
-      const int j = __ffs(bigm) - 1;
-      bigm &= bigm - 1;
-      const int64_t oj = __shfl_sync(FULLMASK, o0, j);
-      const int dj = __shfl_sync(FULLMASK, deg, j);
-      const int fromj = __shfl_sync(FULLMASK, from, j);
-      const int wvj = __shfl_sync(FULLMASK, wv, j);
-      int pen[W];
+    // ---- the tile's incidences in windows of 32 (lane = incidence)
+    for (int wb0 = 0; wb0 < R; wb0 += 32 * B) {
+      uint32_t wd[B][W];
+      int icv[B], lamv[B], wev[B];
 #pragma unroll
-      for (int t = 0; t < W; ++t) pen[t] = 0;
-      int internal = 0;
-      bool border = false;
-      for (int base = 0; base < dj; base += 32) {
-        const bool has = base + lane < dj;
-        uint32_t words[W];
+      for (int u = 0; u < B; ++u) {
+        const int wb = wb0 + 32 * u;
+        const int i = wb + lane;
+        const bool has = i < R;
+        const unsigned starts =
+            __reduce_or_sync(FULLMASK, (d > 0 && excl >= wb && excl < wb + 32) ? (1u << (excl - wb)) : 0u);
+        const int cb = __popc(__ballot_sync(FULLMASK, d > 0 && excl < wb));
+        const int ow = has ? s_owner[cb + __popc(starts & ((2u << lane) - 1u)) - 1] : 0;
+        const int64_t o_ow = __shfl_sync(FULLMASK, o0, ow);
+        const int ex_ow = __shfl_sync(FULLMASK, excl, ow);
+        const int f_ow = __shfl_sync(FULLMASK, from, ow);
 #pragma unroll
-        for (int t = 0; t < W; ++t) words[t] = 0;
-        int we = 0, ic = 0, lam = 0;
+        for (int t = 0; t < W; ++t) wd[u][t] = 0;
+        icv[u] = 0;
+        lamv[u] = 0;
+        wev[u] = 0;
         if (has) {
-          const int64_t e = __ldcs(&c.inets[oj + base + lane]);
-          we = UNIT ? 1 : __ldg(&c.w_e[e]);
+          const int64_t e = __ldcs(&c.inets[o_ow + i - ex_ow]);
+          const int we = UNIT ? 1 : __ldg(&c.w_e[e]);
           const uint32_t* rec = c.conn + e * W2;
-          load_words<W>(rec, words);
-          const uint32_t l1 = __ldg(rec + W + (fromj >> 5));
-          ic = ((l1 >> (fromj & 31)) & 1u) ? 0 : we;
+          load_words<W>(rec, wd[u]);
+          const uint32_t l1 = __ldg(rec + W + (f_ow >> 5));
+          icv[u] = ((l1 >> (f_ow & 31)) & 1u) ? 0 : we;  // Φ(e, from) > 1
+          wev[u] = we;
+          int lam = 0;
 #pragma unroll
-          for (int t = 0; t < W; ++t) lam += __popc(words[t]);
-        }
-        border |= __any_sync(FULLMASK, lam > 1);
-        internal += __reduce_add_sync(FULLMASK, (unsigned)ic);
-        if constexpr (UNIT) {
-#pragma unroll
-          for (int t = 0; t < W; ++t) pen[t] += __popc(transpose32(words[t]));
-        } else {
-          const int nplanes = 32 - __clz(__reduce_or_sync(FULLMASK, (unsigned)we));
-          const Planes wp = make_planes(we, nplanes);
-#pragma unroll
-          for (int t = 0; t < W; ++t) pen[t] += plane_sum(wp, transpose32(words[t]), we);
+          for (int t = 0; t < W; ++t) lam += __popc(wd[u][t]);
+          lamv[u] = lam;
         }
       }
-      if (!border) continue;
-      int to = fromj, gain = 0;
-      // big vertices can exceed the packed-key penalty range
-      decide<W, false>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
-      if (lane == j) {
-        my_to = to;
-        my_gain = gain;
-        my_border = true;
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        const int wb = wb0 + 32 * u;
+        if (wb >= R) break;
+        uint32_t col[W];
+#pragma unroll
+        for (int t = 0; t < W; ++t) col[t] = transpose32(wd[u][t]);
+        const unsigned bm = __ballot_sync(FULLMASK, lamv[u] > 1);
+        const unsigned icb = __ballot_sync(FULLMASK, icv[u] != 0);
+        Planes wp, ip;
+        if constexpr (!UNIT) {
+          const int np = 32 - __clz(__reduce_or_sync(FULLMASK, (unsigned)wev[u]));
+          wp = make_planes(wev[u], np);
+          ip = make_planes(icv[u], np);
+        }
+        // vertices whose last incidence lies in this window
+        unsigned endm = __ballot_sync(FULLMASK, d > 0 && eend > wb && eend <= wb + 32);
+        while (endm) {
+          const int j = __ffs(endm) - 1;
+          endm &= endm - 1;
+          const int exj = __shfl_sync(FULLMASK, excl, j);
+          const int hi = __shfl_sync(FULLMASK, eend, j) - wb;
+          const int lo = exj > wb ? exj - wb : 0;
+          const unsigned mask = (hi == 32 ? FULLMASK : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+          const bool cont = exj < wb;
+          if ((bm & mask) == 0 && !(cont && carry_border)) continue;  // not a border vertex
+          int internal;
+          int pen[W];
+          if constexpr (UNIT) {
+            internal = __popc(icb & mask);
+#pragma unroll
+            for (int t = 0; t < W; ++t) pen[t] = __popc(col[t] & mask);
+          } else {
+            internal = plane_sum(ip, mask, icv[u]);
+#pragma unroll
+            for (int t = 0; t < W; ++t) pen[t] = plane_sum(wp, col[t] & mask, wev[u]);
+          }
+          if (cont) {
+            internal += carry_int;
+#pragma unroll
+            for (int t = 0; t < W; ++t) pen[t] += carry[t];
+          }
+          const int fromj = __shfl_sync(FULLMASK, from, j);
+          const int wvj = __shfl_sync(FULLMASK, wv, j);
+          int to = fromj, gain = 0;
+          decide<W, UNIT>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
+          if (lane == j) {
+            my_to = to;
+            my_gain = gain;
+            my_border = true;
+          }
+        }
+        // the vertex that continues into the next window (at most one)
+        const unsigned openm = __ballot_sync(FULLMASK, d > 0 && excl < wb + 32 && eend > wb + 32);
+        if (openm) {
+          const int j = __ffs(openm) - 1;
+          const int exj = __shfl_sync(FULLMASK, excl, j);
+          const int lo = exj > wb ? exj - wb : 0;
+          const unsigned mask = FULLMASK & ~((1u << lo) - 1u);
+          const bool cont = exj < wb;
+          int pint;
+          if constexpr (UNIT) {
+            pint = __popc(icb & mask);
+          } else {
+            pint = plane_sum(ip, mask, icv[u]);
+          }
+          const bool pb = (bm & mask) != 0;
+#pragma unroll
+          for (int t = 0; t < W; ++t) {
+            int p;
+            if constexpr (UNIT) {
+              p = __popc(col[t] & mask);
+            } else {
+              p = plane_sum(wp, col[t] & mask, wev[u]);
+            }
+            carry[t] = cont ? carry[t] + p : p;
+          }
+          carry_int = cont ? carry_int + pint : pint;
+          carry_border = cont ? (carry_border || pb) : pb;
+        }
       }
     }
 
