@@ -381,6 +381,16 @@ __device__ __forceinline__ void decide(int k, int from, int wv, int internal, in
                                        const int64_t* __restrict__ s_bw,
                                        const int64_t* __restrict__ s_perf, int& to, int& gain) {
   const int lane = lane_id();
+  // quick reject: neither an improving move (pen > internal) nor a zero-gain
+  // candidate (pen == internal) exists when every other block's penalty is
+  // below the internal weight
+  int any = -1;
+#pragma unroll
+  for (int t = 0; t < W; ++t) {
+    const int blk = 32 * t + lane;
+    if (blk != from && pen[t] > any) any = pen[t];
+  }
+  if (__reduce_max_sync(FULLMASK, any) < internal) return;
   int zb = INT_MAX;
   if constexpr (PACKED) {
     // penalties below 2^20: one max over (pen << 11 | 2047 - blk) gives the
