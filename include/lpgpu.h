@@ -235,6 +235,44 @@ LPGPU_API int64_t lpgpu_estimate_footprint(int64_t num_vertices, int64_t num_net
 LPGPU_API void* lpgpu_host_alloc(size_t bytes);
 LPGPU_API void lpgpu_host_free(void* p);
 
+/* ------------------------------------------------- allocation-free metrics */
+
+/* Block weights c(V_b), km1 and cut of a partition, computed from device
+ * buffers the caller already holds, without allocating any device memory.
+ * This entry point has no counterpart in the reference; it exists for callers
+ * that cannot let a library allocate: code running while a CUDA graph is
+ * being captured (cudaMalloc/cudaFree synchronize and cannot be captured),
+ * runtimes that own every byte of device memory through their own pool, and
+ * latency-bound loops that must not block in the allocator.
+ *
+ *   - All array arguments are device pointers: net_offsets (int64, m+1),
+ *     pins (int32), vertex_weights / net_weights (int32, NULL = unit),
+ *     partition (int32, n) and the outputs block_weights (int64, k), km1 and
+ *     cut (one int64 each). Block ids outside [0, k) are ignored.
+ *   - k must be in [1, LPGPU_MAX_K]; larger k is rejected with
+ *     LPGPU_ERR_INVALID_ARG. The cross-block accumulators live in one fixed
+ *     file-scope device array of LPGPU_MAX_K + 2 64-bit words (8 KB), which
+ *     every GPU that loads the library holds until the process exits; no
+ *     cudaMalloc, cudaFree or allocating library routine is called.
+ *   - The work is enqueued on `stream` (a cudaStream_t, NULL = default
+ *     stream) and the call returns without waiting; the outputs are valid once
+ *     the stream reaches that point.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture. Later calls only enqueue kernels.
+ *   - Every call on a device shares the one array: it is cleared at the start
+ *     of each call, so calls in sequence are independent, but calls that
+ *     overlap on the GPU (e.g. on two streams at once) race and give wrong
+ *     results. */
+LPGPU_API lpgpu_status lpgpu_partition_metrics_noalloc(int64_t num_vertices, int64_t num_nets,
+                                                       const int64_t* net_offsets,
+                                                       const int32_t* pins,
+                                                       const int32_t* vertex_weights,
+                                                       const int32_t* net_weights,
+                                                       const int32_t* partition, int32_t k,
+                                                       int64_t* block_weights, int64_t* km1,
+                                                       int64_t* cut, void* stream);
+
 /* ------------------------------------------------------------- timing */
 
 /* CUDA events on the session stream: record into one of 16 slots, read the
