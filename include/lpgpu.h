@@ -150,6 +150,34 @@ LPGPU_API lpgpu_status lpgpu_session_set_partition(lpgpu_session* s, int32_t k, 
                                                    const int64_t* max_part_weights,
                                                    const int64_t* perfect_part_weights);
 
+/* ------------------------------------------------------------ batches
+ *
+ * A batched session holds many independent hypergraphs (instances) as one
+ * union: instance i owns the vertices [instance_vertex_offsets[i],
+ * instance_vertex_offsets[i+1]) and the nets [instance_net_offsets[i],
+ * instance_net_offsets[i+1]) of the union CSR, and every net's pins lie inside
+ * its instance. Each instance has its own k, epsilon, block weights and
+ * bounds. One refine call refines all instances together in the same launches,
+ * and every instance ends exactly as it would if refined alone: sub-rounds are
+ * assigned from instance-local vertex ids and rollbacks are decided per
+ * instance. Block ids passed in and returned are instance-local. This has no
+ * counterpart in the reference, which partitions one hypergraph per call. */
+LPGPU_API lpgpu_status lpgpu_session_upload_batch(lpgpu_session* s, int32_t num_instances,
+                                                  const int64_t* instance_vertex_offsets,
+                                                  const int64_t* instance_net_offsets,
+                                                  const int64_t* net_offsets, const int32_t* pins,
+                                                  const int32_t* vertex_weights,
+                                                  const int32_t* net_weights);
+
+/* Per-instance k (1..LPGPU_MAX_K) and epsilon, and the instance-local block of
+ * every union vertex. Bounds follow Context::setupPartWeights per instance. */
+LPGPU_API lpgpu_status lpgpu_session_set_partition_batch(lpgpu_session* s, const int32_t* instance_k,
+                                                         const double* instance_eps,
+                                                         const int32_t* partition);
+
+/* km1 of every instance (num_instances values; one value for a plain session). */
+LPGPU_API lpgpu_status lpgpu_session_instance_km1(lpgpu_session* s, int64_t* km1);
+
 /* Runs the LP refinement on the device-resident state. Replaces
  * IRefiner::refine of LabelPropagationRefiner<Km1Policy>
  * (label_propagation_refiner.cpp:34-68). refinement_nodes (may be NULL with
@@ -164,7 +192,8 @@ LPGPU_API lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config
 LPGPU_API lpgpu_status lpgpu_session_round_stats(lpgpu_session* s, lpgpu_round_stats* out,
                                                  int32_t max_rounds, int32_t* rounds);
 
-/* Downloads partID for all vertices (PartitionedHypergraph::partID, h:517). */
+/* Downloads partID for all vertices (PartitionedHypergraph::partID, h:517);
+ * instance-local block ids in a batched session. */
 LPGPU_API lpgpu_status lpgpu_session_get_partition(lpgpu_session* s, int32_t* partition);
 
 /* metrics::km1 and metrics::hyperedgeCut (metrics.cpp:29-65) on the device state,
@@ -175,7 +204,8 @@ LPGPU_API lpgpu_status lpgpu_session_metrics(lpgpu_session* s, int64_t* km1, int
 /* Block weights c(V_b) (partWeight, h:599), k values. */
 LPGPU_API lpgpu_status lpgpu_session_get_block_weights(lpgpu_session* s, int64_t* weights);
 
-/* Pin counts Φ(e,b) (pinCountInPart, h:640) as a dense num_nets x k int32 array. */
+/* Pin counts Φ(e,b) (pinCountInPart, h:640) as a dense num_nets x k int32 array
+ * (num_nets x max instance k, local block ids, in a batched session). */
 LPGPU_API lpgpu_status lpgpu_session_get_pin_counts(lpgpu_session* s, int32_t* pin_counts);
 
 /* Connectivity sets Λ(e) (connectivitySet, connectivity_set.h:53-221) as

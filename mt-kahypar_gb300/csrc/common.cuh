@@ -54,6 +54,7 @@ enum Scalar : int {
   kDeltaRb = 7,    // delta of a sub-round rollback
   kEpoch = 8,      // activation stamp of the current round
   kDone = 9,       // arrival counter of the last-CTA pattern
+  kOverCount = 10, // number of overflowing target blocks
   kScalars = 16
 };
 
@@ -104,7 +105,24 @@ struct RoundCtx {
   int32_t zero_gain, revert, rollback;
   int32_t unit_nets;     // every net weight is 1
   int64_t act_threshold;
+  // batched sessions: many independent instances in one union hypergraph.
+  // part[] holds global block ids (instance block offset + local id); Φ and
+  // Λ are indexed by local ids. One instance: batched = 0, kmax = k.
+  int32_t batched;
+  int32_t kmax;           // Φ row stride and largest instance k
+  int32_t num_inst;
+  const int32_t* vinst;     // instance of each vertex
+  const int64_t* inst_voff; // first vertex of each instance (num_inst + 1)
+  const int32_t* inst_boff; // first global block of each instance
+  const int32_t* inst_k;    // blocks of each instance
+  int64_t* inst_delta;      // per-instance summed delta of the current sub-round
+  int32_t* over_ids;        // target blocks that overflow (count in scal[kOverCount])
 };
+
+// Global block offset of vertex v's instance.
+__device__ __forceinline__ int block_offset(const RoundCtx& c, int64_t v) {
+  return c.batched ? c.inst_boff[c.vinst[v]] : 0;
+}
 
 // Kernels launched by this thread through the library so far.
 int64_t kernel_launches();
@@ -127,6 +145,7 @@ cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const 
                                    int64_t* cursor, int64_t* scan_tmp, int64_t scan_tmp_elems);
 cudaError_t launch_init_partition(const Launch& L, const RoundCtx& c);
 cudaError_t launch_metrics(const Launch& L, const RoundCtx& c);
+cudaError_t launch_instance_metrics(const Launch& L, const RoundCtx& c, int64_t* km1_inst);
 cudaError_t launch_best_moves(const Launch& L, const RoundCtx& c, int32_t* to, int32_t* gain,
                               uint8_t* border);
 cudaError_t launch_gain_cache(const Launch& L, const RoundCtx& c, int32_t* benefit,

@@ -202,16 +202,26 @@ cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const 
 // ======================================================== partition init
 
 // c(V_b) = sum of w(v) over v in block b (initializeBlockWeights, h:1067-1084).
+// Batched sessions have too many blocks for shared memory: global atomics.
 __global__ void k_block_weights(RoundCtx c) {
   extern __shared__ ull s_w[];
-  for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_w[b] = 0;
-  __syncthreads();
+  const bool priv = !c.batched;
+  if (priv) {
+    for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_w[b] = 0;
+    __syncthreads();
+  }
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < c.n;
-       v += (int64_t)gridDim.x * blockDim.x)
-    atomicAdd(&s_w[c.part[v]], (ull)(int64_t)c.w_v[v]);
-  __syncthreads();
-  for (int b = threadIdx.x; b < c.k; b += blockDim.x)
-    if (s_w[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_w[b]);
+       v += (int64_t)gridDim.x * blockDim.x) {
+    if (priv)
+      atomicAdd(&s_w[c.part[v]], (ull)(int64_t)c.w_v[v]);
+    else
+      atomicAdd(reinterpret_cast<ull*>(&c.bw[c.part[v]]), (ull)(int64_t)c.w_v[v]);
+  }
+  if (priv) {
+    __syncthreads();
+    for (int b = threadIdx.x; b < c.k; b += blockDim.x)
+      if (s_w[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_w[b]);
+  }
 }
 
 // Φ, Λ and Λ1 (blocks holding exactly one pin of the net) from scratch, warp
@@ -220,7 +230,7 @@ __global__ void k_block_weights(RoundCtx c) {
 // conn[e * 2W .. e * 2W + 2W): W words of Λ(e), then W words of Λ1(e).
 __global__ void k_pin_counts(RoundCtx c) {
   extern __shared__ int s_hist[];
-  const int k = c.k, W = c.W;
+  const int k = c.kmax, W = c.W;
   int* hist = s_hist + (threadIdx.x >> 5) * k;
   const int lane = lane_id();
   for (int b = lane; b < k; b += 32) hist[b] = 0;
@@ -229,7 +239,8 @@ __global__ void k_pin_counts(RoundCtx c) {
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < c.m; e += warps) {
     const int64_t b0 = c.net_off[e], b1 = c.net_off[e + 1];
-    for (int64_t i = b0 + lane; i < b1; i += 32) atomicAdd(&hist[c.part[c.pins[i]]], 1);
+    const int bo = (c.batched && b1 > b0) ? block_offset(c, c.pins[b0]) : 0;
+    for (int64_t i = b0 + lane; i < b1; i += 32) atomicAdd(&hist[c.part[c.pins[i]] - bo], 1);
     __syncwarp();
     int lam = 0;
     for (int w = 0; w < W; ++w) {
@@ -268,11 +279,11 @@ cudaError_t launch_init_partition(const Launch& L, const RoundCtx& c) {
   if ((e = cudaMemsetAsync(c.bw, 0, sizeof(int64_t) * c.k, L.st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(c.scal + kKm1, 0, sizeof(int64_t) * 2, L.st)) != cudaSuccess) return e;
   if (c.n > 0) {
-    k_block_weights<<<grid_for(L, c.n, 256), 256, sizeof(ull) * c.k, L.st>>>(c);
+    k_block_weights<<<grid_for(L, c.n, 256), 256, c.batched ? 0 : sizeof(ull) * c.k, L.st>>>(c);
     LAUNCHED("k_block_weights");
   }
   if (c.m > 0) {
-    const size_t smem = sizeof(int) * c.k * 8;
+    const size_t smem = sizeof(int) * c.kmax * 8;
     k_pin_counts<<<grid_for(L, c.m * 32, 256), 256, smem, L.st>>>(c);
     LAUNCHED("k_pin_counts");
   }
@@ -296,6 +307,29 @@ __global__ void k_metrics(RoundCtx c) {
     atomicAdd(reinterpret_cast<ull*>(&c.scal[kKm1]), (ull)km1);
     atomicAdd(reinterpret_cast<ull*>(&c.scal[kCut]), (ull)cut);
   }
+}
+
+// km1 of every instance of a batched session (net instance = instance of its first pin).
+__global__ void k_instance_metrics(RoundCtx c, int64_t* km1_inst) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < c.m;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b0 = c.net_off[e];
+    if (b0 == c.net_off[e + 1]) continue;
+    int lam = 0;
+    for (int w = 0; w < c.W; ++w) lam += __popc(c.conn[e * 2 * c.W + w]);
+    if (lam > 1)
+      atomicAdd(reinterpret_cast<ull*>(&km1_inst[c.vinst[c.pins[b0]]]), (ull)((int64_t)(lam - 1) * c.w_e[e]));
+  }
+}
+
+cudaError_t launch_instance_metrics(const Launch& L, const RoundCtx& c, int64_t* km1_inst) {
+  cudaError_t e = cudaMemsetAsync(km1_inst, 0, sizeof(int64_t) * c.num_inst, L.st);
+  if (e != cudaSuccess) return e;
+  if (c.m > 0) {
+    k_instance_metrics<<<grid_for(L, c.m, 256), 256, 0, L.st>>>(c, km1_inst);
+    LAUNCHED("k_instance_metrics");
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_metrics(const Launch& L, const RoundCtx& c) {
@@ -468,7 +502,8 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(Round
                                                              uint8_t* dbg_border) {
   constexpr int B = W <= 4 ? 4 : (W <= 8 ? 2 : 1);  // windows whose gathers are issued together
   extern __shared__ unsigned char smem_raw[];
-  const int k = c.k;
+  const bool batched = c.batched != 0;
+  const int k = batched ? 0 : c.k;  // blocks kept in shared memory (none when batched)
   const bool query = dbg_to != nullptr;
   int64_t* s_bw = reinterpret_cast<int64_t*>(smem_raw);
   int64_t* s_perf = s_bw + k;
@@ -492,6 +527,7 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(Round
   int slack[W];
 #pragma unroll
   for (int t = 0; t < W; ++t) slack[t] = (32 * t + lane < k) ? s_slack[32 * t + lane] : -1;
+  int slack_inst = -1;  // batched: instance whose block slack is in `slack`
   const int zero_gain = query ? 0 : c.zero_gain;
   const int64_t beg = query ? 0 : c.sub_off[sub];
   const int64_t cnt = query ? c.n : c.sub_off[sub + 1] - beg;
@@ -504,13 +540,17 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(Round
     const bool valid = tile + lane < cnt;
     const int64_t v = valid ? (query ? pos : (int64_t)c.list[pos]) : 0;
     int64_t o0 = 0;
-    int d = 0, from = 0, wv = 0;
+    int d = 0, from = 0, wv = 0, bo = 0, inst = 0;
     if (valid) {
       o0 = c.vtx_off[v];
       const int64_t dd = c.vtx_off[v + 1] - o0;
       pins += dd;
       d = dd > kHighDegree ? 0 : (int)dd;  // isBorderNode is false above the threshold
-      from = c.part[v];
+      if (batched) {
+        inst = c.vinst[v];
+        bo = c.inst_boff[inst];
+      }
+      from = c.part[v] - bo;  // local block id
       wv = c.w_v[v];
     }
     int incl = d;
@@ -614,7 +654,28 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(Round
           const int fromj = __shfl_sync(FULLMASK, from, j);
           const int wvj = __shfl_sync(FULLMASK, wv, j);
           int to = fromj, gain = 0;
-          decide<W, UNIT>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
+          if (batched) {
+            const int ij = __shfl_sync(FULLMASK, inst, j);
+            const int boj = c.inst_boff[ij];
+            const int kj = c.inst_k[ij];
+            if (ij != slack_inst) {  // warp-uniform: reload the instance's block slack
+              slack_inst = ij;
+#pragma unroll
+              for (int t = 0; t < W; ++t) {
+                const int b = 32 * t + lane;
+                int sl = -1;
+                if (b < kj) {
+                  const int64_t x = c.lmax[boj + b] - c.bw[boj + b];
+                  sl = x < 0 ? -1 : (x > INT_MAX ? INT_MAX : (int)x);
+                }
+                slack[t] = sl;
+              }
+            }
+            decide<W, UNIT>(kj, fromj, wvj, internal, zero_gain, pen, slack, c.bw + boj, c.perfect + boj, to,
+                            gain);
+          } else {
+            decide<W, UNIT>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
+          }
           if (lane == j) {
             my_to = to;
             my_gain = gain;
@@ -660,10 +721,16 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(Round
       } else {
         int2 r = make_int2(-1, 0);
         if (my_to != from) {
-          r = make_int2(my_to, my_gain);
-          atomicAdd(&s_in_w[my_to], (ull)(int64_t)wv);
-          atomicAdd(&s_in_cnt[my_to], 1u);
-          atomicAdd(&s_out_w[from], (ull)(int64_t)wv);
+          r = make_int2(my_to + bo, my_gain);  // global target block
+          if (batched) {
+            atomicAdd(reinterpret_cast<ull*>(&c.in_w[my_to + bo]), (ull)(int64_t)wv);
+            atomicAdd(reinterpret_cast<ull*>(&c.in_cnt[my_to + bo]), 1ull);
+            atomicAdd(reinterpret_cast<ull*>(&c.cand_out[from + bo]), (ull)(int64_t)wv);
+          } else {
+            atomicAdd(&s_in_w[my_to], (ull)(int64_t)wv);
+            atomicAdd(&s_in_cnt[my_to], 1u);
+            atomicAdd(&s_out_w[from], (ull)(int64_t)wv);
+          }
           ++cands;
         }
         c.rec[pos] = r;
@@ -723,7 +790,7 @@ static size_t sweep_smem(int k) {
 static cudaError_t launch_sweep(const Launch& L, const RoundCtx& c, int round, int sub,
                                 int32_t* to, int32_t* gain, uint8_t* border) {
   if (word_class(c.W) != c.W) return cudaErrorInvalidValue;
-  const size_t smem = sweep_smem(c.k);
+  const size_t smem = sweep_smem(c.batched ? 0 : c.k);
   LPGPU_DISPATCH_W(c.W, {
     auto kern = c.unit_nets ? k_sweep<kW, true> : k_sweep<kW, false>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -914,16 +981,30 @@ cudaError_t launch_mark_list(const Launch& L, const RoundCtx& c, const int32_t* 
 
 // Per tile, flagged vertices per sub-round (tile_cnt[s * tiles + tile]).
 // All 32 vertices of an aligned chunk share one sub-round.
+// Batched sessions hash instance-local ids (so that an instance gets the same
+// sub-rounds alone and in a batch): then a chunk may straddle two instances and
+// every vertex computes its own sub-round.
+__device__ __forceinline__ int vertex_subround(const int32_t* vinst, const int64_t* inst_voff, int64_t v,
+                                               int round, int S) {
+  return subround_of(vinst ? v - inst_voff[vinst[v]] : v, round, S);
+}
+
 __global__ void __launch_bounds__(1024) k_bin_count(const uint8_t* __restrict__ flag, int64_t n,
                                                     int round, int S, int64_t tiles,
-                                                    int64_t* __restrict__ tile_cnt) {
+                                                    int64_t* __restrict__ tile_cnt,
+                                                    const int32_t* __restrict__ vinst,
+                                                    const int64_t* __restrict__ inst_voff) {
   __shared__ int s_cnt[kMaxSubrounds];
   if (threadIdx.x < S) s_cnt[threadIdx.x] = 0;
   __syncthreads();
   const int64_t v = blockIdx.x * (int64_t)kTile + threadIdx.x;
   const bool f = v < n && flag[v];
-  const unsigned bal = __ballot_sync(FULLMASK, f);
-  if (lane_id() == 0 && bal) atomicAdd(&s_cnt[subround_of(v, round, S)], __popc(bal));
+  if (vinst) {
+    if (f) atomicAdd(&s_cnt[vertex_subround(vinst, inst_voff, v, round, S)], 1);
+  } else {
+    const unsigned bal = __ballot_sync(FULLMASK, f);
+    if (lane_id() == 0 && bal) atomicAdd(&s_cnt[subround_of(v, round, S)], __popc(bal));
+  }
   __syncthreads();
   if (threadIdx.x < S) tile_cnt[threadIdx.x * tiles + blockIdx.x] = s_cnt[threadIdx.x];
 }
@@ -933,13 +1014,28 @@ __global__ void __launch_bounds__(1024) k_bin_count(const uint8_t* __restrict__ 
 __global__ void __launch_bounds__(1024) k_bin_scatter(uint8_t* __restrict__ flag, int64_t n, int round,
                                                       int S, int64_t tiles,
                                                       const int64_t* __restrict__ tile_off,
-                                                      int32_t* __restrict__ list) {
+                                                      int32_t* __restrict__ list,
+                                                      const int32_t* __restrict__ vinst,
+                                                      const int64_t* __restrict__ inst_voff) {
   __shared__ int s_cnt[32];
   __shared__ int s_sub[32];
   __shared__ int64_t s_base[32];
+  __shared__ unsigned long long s_cur[kMaxSubrounds];
   const int w = threadIdx.x >> 5;
   const int64_t v = blockIdx.x * (int64_t)kTile + threadIdx.x;
   const bool f = v < n && flag[v];
+  if (vinst) {
+    // per-vertex sub-rounds; positions inside a (tile, sub-round) segment are
+    // taken in arrival order (nothing depends on the order inside a list)
+    if (threadIdx.x < S) s_cur[threadIdx.x] = (unsigned long long)tile_off[threadIdx.x * tiles + blockIdx.x];
+    __syncthreads();
+    if (f) {
+      const int sr = vertex_subround(vinst, inst_voff, v, round, S);
+      list[atomicAdd(&s_cur[sr], 1ull)] = (int32_t)v;
+      flag[v] = 0;
+    }
+    return;
+  }
   const unsigned bal = __ballot_sync(FULLMASK, f);
   const int sub = subround_of(blockIdx.x * (int64_t)kTile + w * 32, round, S);
   if (lane_id() == 0) { s_cnt[w] = __popc(bal); s_sub[w] = sub; }
@@ -1017,11 +1113,14 @@ cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int
                               int64_t scan_tmp_elems, PhaseTimer* timer) {
   Scope sc(timer, "bin_active");
   const int64_t tiles = std::max<int64_t>(1, (c.n + kTile - 1) / kTile);
-  k_bin_count<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_cnt);
+  const int32_t* vinst = c.batched ? c.vinst : nullptr;
+  k_bin_count<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_cnt, vinst,
+                                                   c.inst_voff);
   LAUNCHED("k_bin_count");
   cudaError_t e = scan_exclusive_i64(tile_cnt, tile_off, S * tiles, scan_tmp, scan_tmp_elems, L.st);
   if (e != cudaSuccess) return e;
-  k_bin_scatter<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_off, c.list);
+  k_bin_scatter<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_off, c.list,
+                                                     vinst, c.inst_voff);
   LAUNCHED("k_bin_scatter");
   k_sub_offsets<<<1, 64, 0, L.st>>>(tile_off, tile_cnt, S, tiles, c.sub_off, c.scal);
   LAUNCHED("k_sub_offsets");
@@ -1055,10 +1154,11 @@ __device__ bool last_cta(int64_t* counter) {
 // least its weight (otherwise no block can become empty).
 __device__ void plan_to(const RoundCtx& c) {
   const int k = c.k;
-  __shared__ int64_t s_run;
+  __shared__ int64_t s_run, s_nover;
   __shared__ int s_any_over, s_any_from;
   if (threadIdx.x == 0) {
     s_run = 0;
+    s_nover = 0;
     s_any_over = 0;
     s_any_from = 0;
   }
@@ -1085,13 +1185,20 @@ __device__ void plan_to(const RoundCtx& c) {
       c.seg_off[b] = off;
       c.cursor[b] = off;
     }
+    int64_t novers;
+    const int64_t oi = block_scan_excl_i64(over ? 1 : 0, &novers) + s_nover;
+    if (over) c.over_ids[oi] = b;
     if (over) s_any_over = 1;
     if (maybe_from) s_any_from = 1;
     __syncthreads();
-    if (threadIdx.x == 0) s_run += total;
+    if (threadIdx.x == 0) {
+      s_run += total;
+      s_nover += novers;
+    }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
+    c.scal[kOverCount] = s_nover;
     c.scal[kAnyOverTo] = s_any_over;
     c.scal[kAnyOverFrom] = s_any_from;
     c.scal[kDeltaSub] = 0;
@@ -1232,14 +1339,17 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ keys, const in
   return prefix;
 }
 
-// Target-side selection: one CTA per block; blocks that do not overflow exit.
+// Target-side selection: CTAs stride over the overflowing blocks.
 __global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c) {
-  const int b = blockIdx.x;
-  if (!c.over_to[b]) return;
-  const int64_t off = c.seg_off[b];
-  const uint64_t thr = cta_radix_select(c.seg_key + off, c.seg_w + off, c.in_cnt[b],
-                                        c.lmax[b] - c.bw[b]);
-  if (threadIdx.x == 0) c.thr_to[b] = thr;
+  const int64_t nover = c.scal[kOverCount];
+  for (int64_t i = blockIdx.x; i < nover; i += gridDim.x) {
+    const int b = c.over_ids[i];
+    const int64_t off = c.seg_off[b];
+    const uint64_t thr = cta_radix_select(c.seg_key + off, c.seg_w + off, c.in_cnt[b],
+                                          c.lmax[b] - c.bw[b]);
+    if (threadIdx.x == 0) c.thr_to[b] = thr;
+    __syncthreads();
+  }
 }
 
 // Source-side selection (changeNodePart's from_weight_after > 0,
@@ -1249,41 +1359,47 @@ __global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c) {
 // prefix that leaves weight >= 1.
 __global__ void __launch_bounds__(kSelThreads) k_from_side(RoundCtx c, int sub) {
   if (c.scal[kAnyOverFrom] == 0) return;
-  extern __shared__ ull s_fs[];
   const int k = c.k;
-  ull* s_w = s_fs;
-  ull* s_n = s_fs + k;
-  ull* s_cur = s_fs + 2 * k;
   __shared__ int s_any;
-  for (int b = threadIdx.x; b < k; b += blockDim.x) { s_w[b] = 0; s_n[b] = 0; }
-  if (threadIdx.x == 0) s_any = 0;
+  __shared__ int64_t s_run;
+  if (threadIdx.x == 0) {
+    s_any = 0;
+    s_run = 0;
+  }
   __syncthreads();
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
+  // target-accepted weight and count per source block (acc_w / acc_cnt are cleared by the plan)
   for (int64_t pos = beg + threadIdx.x; pos < end; pos += blockDim.x) {
     const int2 r = c.rec[pos];
     if (r.x < 0) continue;
     const int32_t v = c.list[pos];
     if (move_key(r.y, v) < c.thr_to[r.x]) {
       const int f = c.part[v];
-      atomicAdd(&s_w[f], (ull)(int64_t)c.w_v[v]);
-      atomicAdd(&s_n[f], 1ull);
+      atomicAdd(reinterpret_cast<ull*>(&c.acc_w[f]), (ull)(int64_t)c.w_v[v]);
+      atomicAdd(reinterpret_cast<ull*>(&c.acc_cnt[f]), 1ull);
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    ull run = 0;
-    for (int b = 0; b < k; ++b) {
-      const bool over = c.bw[b] - (int64_t)s_w[b] < 1 && s_n[b] > 0;
+  for (int b0 = 0; b0 < k; b0 += blockDim.x) {
+    const int b = b0 + threadIdx.x;
+    bool over = false;
+    int64_t n = 0;
+    if (b < k) {
+      n = c.acc_cnt[b];
+      over = n > 0 && c.bw[b] - c.acc_w[b] < 1;
+    }
+    int64_t total;
+    const int64_t off = block_scan_excl_i64(over ? n : 0, &total) + s_run;
+    if (b < k) {
       c.over_from[b] = over;
-      c.seg_off[b] = (int64_t)run;
-      s_cur[b] = run;
-      if (over) {
-        run += s_n[b];
-        s_any = 1;
-      }
+      c.seg_off[b] = off;
+      c.cursor[b] = off;
     }
+    if (over) s_any = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) s_run += total;
+    __syncthreads();
   }
-  __syncthreads();
   if (!s_any) return;
   for (int64_t pos = beg + threadIdx.x; pos < end; pos += blockDim.x) {
     const int2 r = c.rec[pos];
@@ -1292,7 +1408,7 @@ __global__ void __launch_bounds__(kSelThreads) k_from_side(RoundCtx c, int sub) 
     const uint64_t key = move_key(r.y, v);
     const int f = c.part[v];
     if (key < c.thr_to[r.x] && c.over_from[f]) {
-      const ull slot = atomicAdd(&s_cur[f], 1ull);
+      const ull slot = atomicAdd(reinterpret_cast<ull*>(&c.cursor[f]), 1ull);
       c.seg_key[slot] = key;
       c.seg_w[slot] = c.w_v[v];
     }
@@ -1301,7 +1417,7 @@ __global__ void __launch_bounds__(kSelThreads) k_from_side(RoundCtx c, int sub) 
   for (int b = 0; b < k; ++b) {
     if (!c.over_from[b]) continue;  // uniform across the CTA
     const int64_t off = c.seg_off[b];
-    const uint64_t thr = cta_radix_select(c.seg_key + off, c.seg_w + off, (int64_t)s_n[b], c.bw[b] - 1);
+    const uint64_t thr = cta_radix_select(c.seg_key + off, c.seg_w + off, c.acc_cnt[b], c.bw[b] - 1);
     if (threadIdx.x == 0) c.thr_from[b] = thr;
     __syncthreads();
   }
@@ -1318,6 +1434,8 @@ __device__ void close_subround(const RoundCtx& c, int round) {
     c.in_cnt[b] = 0;
     c.cand_out[b] = 0;
   }
+  if (c.batched)
+    for (int i = threadIdx.x; i < c.num_inst; i += blockDim.x) c.inst_delta[i] = 0;
 }
 
 // Incidence packing shared by the kernels that walk the incidences of a set
@@ -1441,7 +1559,7 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_commit(RoundCtx c, int roun
     const int64_t pos = base + lane;
     int2 r = make_int2(-1, 0);
     int32_t v = 0;
-    int f = 0, deg = 0;
+    int f = 0, deg = 0, bo = 0;
     int64_t o0 = 0;
     bool acc = false;
     if (pos < end) {
@@ -1455,13 +1573,15 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_commit(RoundCtx c, int roun
           c.rec[pos].y = f;
           o0 = c.vtx_off[v];
           deg = (int)(c.vtx_off[v + 1] - o0);
+          bo = block_offset(c, v);
         }
       }
       c.status[pos] = acc ? 1 : 0;
     }
     const int tot = packed_incidences(acc, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
-      const int fo = __shfl_sync(FULLMASK, f, ow);
-      const int to = __shfl_sync(FULLMASK, r.x, ow);
+      const int bow = __shfl_sync(FULLMASK, bo, ow);
+      const int fo = __shfl_sync(FULLMASK, f, ow) - bow;   // local blocks
+      const int to = __shfl_sync(FULLMASK, r.x, ow) - bow;
       int a = 0;
       if (has) {
         const int64_t e = c.inets[j];
@@ -1472,6 +1592,7 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_commit(RoundCtx c, int roun
     });
     if (acc) {
       att += tot;
+      if (c.batched) atomicAdd(reinterpret_cast<ull*>(&c.inst_delta[c.vinst[v]]), (ull)(int64_t)tot);
       c.part[v] = r.x;
       if (last) c.next_flag[v] = 1;
       const int64_t wv = c.w_v[v];
@@ -1508,7 +1629,7 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_revert_eval(RoundCtx c, int
        base += stride) {
     const int64_t pos = base + lane;
     const bool moved = pos < end && c.status[pos] == 1;
-    int2 r = make_int2(0, 0);  // (to, from)
+    int2 r = make_int2(0, 0);  // (to, from), local blocks
     int64_t o0 = 0;
     int deg = 0;
     if (moved) {
@@ -1516,6 +1637,9 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_revert_eval(RoundCtx c, int
       const int64_t v = c.list[pos];
       o0 = c.vtx_off[v];
       deg = (int)(c.vtx_off[v + 1] - o0);
+      const int bo = block_offset(c, v);
+      r.x -= bo;
+      r.y -= bo;
     }
     const int score = packed_incidences(moved, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
       const int t = __shfl_sync(FULLMASK, r.x, ow);
@@ -1539,7 +1663,9 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_revert_eval(RoundCtx c, int
 // marked 1 (status 3). With `last`, the moves that stay are activated and the
 // sub-round is closed.
 __global__ void __launch_bounds__(kPackThreads, 4) k_undo(RoundCtx c, int round, int sub, int rollback, int last) {
-  const bool roll = rollback && c.scal[kDeltaSub] > 0;  // kDeltaSub is not written here
+  // rollback: the sub-round's delta decides (per instance when batched);
+  // kDeltaSub and inst_delta are not written in rollback mode
+  const bool roll = rollback && (c.batched || c.scal[kDeltaSub] > 0);
   extern __shared__ ull s_dw[];
   __shared__ unsigned char s_own[kPackThreads];
   for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_dw[b] = 0;
@@ -1555,24 +1681,37 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_undo(RoundCtx c, int round,
          base += stride) {
       const int64_t pos = base + lane;
       const uint8_t st = pos < end ? c.status[pos] : 0;
-      const bool sel = rollback ? (roll && st == 1) : st == 2;
+      int64_t v = 0;
+      int bo = 0;
+      bool inst_roll = roll;
+      if (st == 1 || st == 2) {
+        v = c.list[pos];
+        if (c.batched) {
+          const int i = c.vinst[v];
+          bo = c.inst_boff[i];
+          inst_roll = rollback && c.inst_delta[i] > 0;  // rollback is decided per instance
+        }
+      }
+      const bool sel = rollback ? (inst_roll && st == 1) : st == 2;
       const bool keep = last && st == 1 && !sel;
-      int2 r = make_int2(0, 0);  // (to, from)
-      int64_t v = 0, o0 = 0;
+      int2 r = make_int2(0, 0);  // (to, from), global blocks
+      int64_t o0 = 0;
       int deg = 0;
       if (sel || keep) {
         r = c.rec[pos];
-        v = c.list[pos];
         o0 = c.vtx_off[v];
         deg = (int)(c.vtx_off[v + 1] - o0);
       }
       const int tot = packed_incidences(sel, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
-        const int t = __shfl_sync(FULLMASK, r.x, ow);
-        const int f = __shfl_sync(FULLMASK, r.y, ow);
+        const int bow = __shfl_sync(FULLMASK, bo, ow);
+        const int t = __shfl_sync(FULLMASK, r.x, ow) - bow;
+        const int f = __shfl_sync(FULLMASK, r.y, ow) - bow;
         return has ? commit_incidence(c, c.inets[j], t, f) : 0;
       });
       if (sel) {
         att += tot;
+        if (c.batched && !rollback)
+          atomicAdd(reinterpret_cast<ull*>(&c.inst_delta[c.vinst[v]]), (ull)(int64_t)tot);
         c.part[v] = r.y;
         const int64_t wv = c.w_v[v];
         atomicAdd(&s_dw[r.y], (ull)wv);
@@ -1643,11 +1782,9 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
     Scope sc(timer, "select");
     k_bin_moves<<<g, 256, 0, L.st>>>(c, sub);
     LAUNCHED("k_bin_moves");
-    k_select<<<k, kSelThreads, 0, L.st>>>(c);
+    k_select<<<(unsigned)std::min<int64_t>(k, 4 * (int64_t)L.num_sms), kSelThreads, 0, L.st>>>(c);
     LAUNCHED("k_select");
-    const size_t fs_smem = sizeof(ull) * 3 * k;
-    cudaFuncSetAttribute(k_from_side, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs_smem);
-    k_from_side<<<1, kSelThreads, fs_smem, L.st>>>(c, sub);
+    k_from_side<<<1, kSelThreads, 0, L.st>>>(c, sub);
     LAUNCHED("k_from_side");
   }
   const int last_commit = !c.revert && !c.rollback;

@@ -102,6 +102,14 @@ struct lpgpu_session_s {
   DevBuf<uint64_t> seg_key, thr;
   DevBuf<int32_t> saved_part;
   int64_t scan_tmp_n = 0;
+  // batched sessions (lpgpu_session_upload_batch): instance ranges and blocks
+  bool batched = false;
+  int32_t num_inst = 0;
+  int32_t kmax = 0;
+  std::vector<int64_t> h_inst_voff, h_inst_noff, h_inst_weight;
+  std::vector<int32_t> h_inst_boff, h_inst_k;
+  DevBuf<int32_t> vinst, inst_boff, inst_k, over_ids;
+  DevBuf<int64_t> inst_voff, inst_delta;
   // results of the last refine
   std::vector<lpgpu_round_stats> last_stats;
   // timing
@@ -139,6 +147,15 @@ struct lpgpu_session_s {
     c.sub_off = sub_off.p;
     c.next_flag = next_flag.p;
     c.net_epoch = net_epoch.p;
+    c.batched = batched ? 1 : 0;
+    c.kmax = batched ? kmax : k;
+    c.num_inst = num_inst;
+    c.vinst = vinst.p;
+    c.inst_voff = inst_voff.p;
+    c.inst_boff = inst_boff.p;
+    c.inst_k = inst_k.p;
+    c.inst_delta = inst_delta.p;
+    c.over_ids = over_ids.p;
     c.rec = rec.p;
     c.status = status.p;
     int64_t* b = blk64.p;
@@ -182,6 +199,10 @@ struct lpgpu_session_s {
     blk64.release(&footprint);
     thr.release(&footprint);
     over.release(&footprint);
+    over_ids.release(&footprint);
+    inst_boff.release(&footprint);
+    inst_k.release(&footprint);
+    inst_delta.release(&footprint);
     has_part = false;
   }
   void release_all() {
@@ -192,6 +213,8 @@ struct lpgpu_session_s {
     for (auto* b : b32) b->release(&footprint);
     next_flag.release(&footprint);
     saved_part.release(&footprint);
+    vinst.release(&footprint);
+    inst_voff.release(&footprint);
     status.release(&footprint);
     rec.release(&footprint);
     seg_key.release(&footprint);
@@ -218,33 +241,53 @@ struct DeviceGuard {
 
 int64_t tiles_for(int64_t n) { return std::max<int64_t>(1, (n + 1023) / 1024); }
 
+// Checks the CSR before upload. With instance ranges (batched sessions), every
+// net's pins must lie in its instance's vertex range, and the int32 bounds of
+// the reference's Gain / HypernodeWeight types apply per instance.
 lpgpu_status validate_csr(int64_t n, int64_t m, const int64_t* net_off, const int32_t* pins,
-                          const int32_t* w_v, const int32_t* w_e, int64_t* total_vw) {
+                          const int32_t* w_v, const int32_t* w_e, int64_t* total_vw,
+                          int32_t num_inst = 1, const int64_t* inst_voff = nullptr,
+                          const int64_t* inst_noff = nullptr) {
   if (n < 0 || m < 0) return invalid("negative vertex or net count");
   if (n > INT32_MAX || m > INT32_MAX) return invalid("vertex and net ids must fit int32");
   if (!net_off || (m > 0 && net_off[m] > 0 && !pins)) return invalid("null CSR pointer");
   if (net_off[0] != 0) return invalid("net_offsets[0] must be 0");
-  int64_t gain_bound = 0;
-  for (int64_t e = 0; e < m; ++e) {
-    const int64_t sz = net_off[e + 1] - net_off[e];
-    if (sz < 0) return invalid("net_offsets must be non-decreasing");
-    if (w_e && w_e[e] < 0) return invalid("net weights must be >= 0");
-    gain_bound += sz * (w_e ? (int64_t)w_e[e] : 1);
+  const int64_t one_v[2] = {0, n}, one_n[2] = {0, m};
+  if (!inst_voff) {
+    inst_voff = one_v;
+    inst_noff = one_n;
+    num_inst = 1;
   }
-  if (gain_bound > INT32_MAX)
-    return invalid("sum of |e| * w(e) exceeds int32: gains would overflow the reference's Gain type");
-  const int64_t P = net_off[m];
-  for (int64_t i = 0; i < P; ++i)
-    if (pins[i] < 0 || pins[i] >= n) return invalid("pin id out of range");
-  int64_t tw = 0;
-  for (int64_t v = 0; v < n; ++v) {
-    const int64_t w = w_v ? w_v[v] : 1;
-    if (w < 0) return invalid("vertex weights must be >= 0");
-    tw += w;
+  int64_t tw_all = 0;
+  for (int32_t i = 0; i < num_inst; ++i) {
+    const int64_t v0 = inst_voff[i], v1 = inst_voff[i + 1], e0 = inst_noff[i], e1 = inst_noff[i + 1];
+    if (v0 < 0 || v1 < v0 || v1 > n || e0 < 0 || e1 < e0 || e1 > m)
+      return invalid("instance offsets must be non-decreasing and within the union");
+    int64_t gain_bound = 0;
+    for (int64_t e = e0; e < e1; ++e) {
+      const int64_t sz = net_off[e + 1] - net_off[e];
+      if (sz < 0) return invalid("net_offsets must be non-decreasing");
+      if (w_e && w_e[e] < 0) return invalid("net weights must be >= 0");
+      gain_bound += sz * (w_e ? (int64_t)w_e[e] : 1);
+      for (int64_t q = net_off[e]; q < net_off[e + 1]; ++q)
+        if (pins[q] < v0 || pins[q] >= v1)
+          return invalid(num_inst > 1 ? "pin id outside its instance's vertex range" : "pin id out of range");
+    }
+    if (gain_bound > INT32_MAX)
+      return invalid("sum of |e| * w(e) exceeds int32: gains would overflow the reference's Gain type");
+    int64_t tw = 0;
+    for (int64_t v = v0; v < v1; ++v) {
+      const int64_t w = w_v ? w_v[v] : 1;
+      if (w < 0) return invalid("vertex weights must be >= 0");
+      tw += w;
+    }
+    if (tw > INT32_MAX)
+      return invalid("total vertex weight exceeds int32 (the reference's HypernodeWeight)");
+    tw_all += tw;
   }
-  if (tw > INT32_MAX)
-    return invalid("total vertex weight exceeds int32 (the reference's HypernodeWeight)");
-  *total_vw = tw;
+  if (inst_voff[0] != 0 || inst_voff[num_inst] != n || inst_noff[0] != 0 || inst_noff[num_inst] != m)
+    return invalid("instance offsets must cover the union exactly");
+  *total_vw = tw_all;
   return LPGPU_OK;
 }
 
@@ -328,11 +371,12 @@ lpgpu_status lpgpu_session_destroy(lpgpu_session* s) {
   return LPGPU_OK;
 }
 
-lpgpu_status lpgpu_session_upload(lpgpu_session* s, int64_t n, int64_t m, const int64_t* net_off,
-                                  const int32_t* pins, const int32_t* w_v, const int32_t* w_e) {
+static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const int64_t* net_off,
+                                const int32_t* pins, const int32_t* w_v, const int32_t* w_e,
+                                int32_t num_inst, const int64_t* inst_voff, const int64_t* inst_noff) {
   if (!s) return invalid("null session");
   int64_t total = 0;
-  lpgpu_status vs = validate_csr(n, m, net_off, pins, w_v, w_e, &total);
+  lpgpu_status vs = validate_csr(n, m, net_off, pins, w_v, w_e, &total, num_inst, inst_voff, inst_noff);
   if (vs != LPGPU_OK) return vs;
   DeviceGuard g(s->device);
   CK(cudaStreamSynchronize(s->st));
@@ -390,11 +434,136 @@ lpgpu_status lpgpu_session_upload(lpgpu_session* s, int64_t n, int64_t m, const 
     }
     CK(cudaMemsetAsync(s->net_epoch.p, 0, sizeof(int32_t) * m, st));
   }
+  // instance ranges of a batched session
+  s->batched = inst_voff != nullptr;
+  s->num_inst = s->batched ? num_inst : 1;
+  s->h_inst_voff.assign(2, 0);
+  s->h_inst_noff.assign(2, 0);
+  s->h_inst_voff[1] = n;
+  s->h_inst_noff[1] = m;
+  s->h_inst_weight.assign(1, total);
+  if (s->batched) {
+    s->h_inst_voff.assign(inst_voff, inst_voff + num_inst + 1);
+    s->h_inst_noff.assign(inst_noff, inst_noff + num_inst + 1);
+    s->h_inst_weight.assign(num_inst, 0);
+    for (int32_t i = 0; i < num_inst; ++i)
+      for (int64_t v = inst_voff[i]; v < inst_voff[i + 1]; ++v) s->h_inst_weight[i] += w_v ? w_v[v] : 1;
+    std::vector<int32_t> vi(n);
+    for (int32_t i = 0; i < num_inst; ++i)
+      for (int64_t v = inst_voff[i]; v < inst_voff[i + 1]; ++v) vi[v] = i;
+    CK(s->vinst.alloc(n, fp));
+    CK(s->inst_voff.alloc(num_inst + 1, fp));
+    if (n > 0) CK(cudaMemcpyAsync(s->vinst.p, vi.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->inst_voff.p, inst_voff, sizeof(int64_t) * (num_inst + 1), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+  } else {
+    s->vinst.release(fp);
+    s->inst_voff.release(fp);
+  }
   CK(launch_build_incidence(s->launch(), n, m, s->net_off.p, s->pins.p, s->vtx_off.p, s->inets.p,
                             reinterpret_cast<int64_t*>(s->seg_key.p), s->scan_tmp.p, s->scan_tmp_n));
   CK(cudaStreamSynchronize(st));
   s->has_hg = true;
   return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_upload(lpgpu_session* s, int64_t n, int64_t m, const int64_t* net_off,
+                                  const int32_t* pins, const int32_t* w_v, const int32_t* w_e) {
+  return upload_impl(s, n, m, net_off, pins, w_v, w_e, 1, nullptr, nullptr);
+}
+
+lpgpu_status lpgpu_session_upload_batch(lpgpu_session* s, int32_t num_instances,
+                                        const int64_t* instance_vertex_offsets,
+                                        const int64_t* instance_net_offsets, const int64_t* net_off,
+                                        const int32_t* pins, const int32_t* w_v, const int32_t* w_e) {
+  if (num_instances < 1 || !instance_vertex_offsets || !instance_net_offsets)
+    return invalid("a batch needs at least one instance and its offsets");
+  const int64_t n = instance_vertex_offsets[num_instances], m = instance_net_offsets[num_instances];
+  return upload_impl(s, n, m, net_off, pins, w_v, w_e, num_instances, instance_vertex_offsets,
+                     instance_net_offsets);
+}
+
+// Allocates the partition state for K global blocks (Φ rows of kmax entries)
+// and builds it from `gpart` (global block ids).
+static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax, const int32_t* gpart,
+                                       const std::vector<int64_t>& hl, const std::vector<int64_t>& hp) {
+  DeviceGuard g(s->device);
+  CK(cudaStreamSynchronize(s->st));
+  s->release_partition();
+  s->k = K;
+  s->kmax = kmax;
+  s->W = word_class_of(kmax);
+  int64_t* fp = &s->footprint;
+  CK(s->part.alloc(s->n, fp));
+  CK(s->phi.alloc((size_t)s->m * kmax, fp));
+  CK(s->conn.alloc((size_t)s->m * 2 * s->W, fp));
+  CK(s->bw.alloc(K, fp));
+  CK(s->lmax.alloc(K, fp));
+  CK(s->perfect.alloc(K, fp));
+  CK(s->blk64.alloc(7 * (size_t)K + 1, fp));
+  CK(s->thr.alloc(2 * (size_t)K, fp));
+  CK(s->over.alloc(2 * (size_t)K, fp));
+  CK(s->over_ids.alloc(K, fp));
+  cudaStream_t st = s->st;
+  if (s->batched) {
+    CK(s->inst_boff.alloc(s->num_inst, fp));
+    CK(s->inst_k.alloc(s->num_inst, fp));
+    CK(s->inst_delta.alloc(s->num_inst, fp));
+    CK(cudaMemcpyAsync(s->inst_boff.p, s->h_inst_boff.data(), sizeof(int32_t) * s->num_inst, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->inst_k.p, s->h_inst_k.data(), sizeof(int32_t) * s->num_inst, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(s->inst_delta.p, 0, sizeof(int64_t) * s->num_inst, st));
+  }
+  if (s->n > 0) CK(cudaMemcpyAsync(s->part.p, gpart, sizeof(int32_t) * s->n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(s->lmax.p, hl.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(s->perfect.p, hp.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(s->blk64.p, 0, sizeof(int64_t) * (7 * (size_t)K + 1), st));
+  RoundCtx c = s->ctx();
+  CK(launch_init_partition(s->launch(), c));
+  CK(cudaStreamSynchronize(st));
+  s->h_perfect = hp;
+  s->has_part = true;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_set_partition_batch(lpgpu_session* s, const int32_t* instance_k,
+                                               const double* instance_eps, const int32_t* partition) {
+  if (!s) return invalid("null session");
+  if (!s->has_hg || !s->batched) {
+    set_error("set_partition_batch needs a batched upload");
+    return LPGPU_ERR_STATE;
+  }
+  if (!instance_k || !instance_eps || (s->n > 0 && !partition)) return invalid("null argument");
+  const int32_t I = s->num_inst;
+  std::vector<int32_t> boff(I);
+  int64_t K = 0;
+  int32_t kmax = 1;
+  for (int32_t i = 0; i < I; ++i) {
+    if (instance_k[i] < 1 || instance_k[i] > LPGPU_MAX_K) return invalid("instance k must be in [1, 1024]");
+    boff[i] = (int32_t)K;
+    K += instance_k[i];
+    kmax = std::max(kmax, instance_k[i]);
+  }
+  if (K > INT32_MAX / 8) return invalid("too many blocks in one batch");
+  std::vector<int32_t> gpart(s->n);
+  std::vector<int64_t> hl(K), hp(K);
+  for (int32_t i = 0; i < I; ++i) {
+    int64_t tw = 0;
+    for (int64_t v = s->h_inst_voff[i]; v < s->h_inst_voff[i + 1]; ++v) {
+      if (partition[v] < 0 || partition[v] >= instance_k[i]) return invalid("block id out of range");
+      gpart[v] = partition[v] + boff[i];
+    }
+    // total weight of the instance for Context::setupPartWeights (context.cpp:237-250)
+    tw = s->h_inst_weight[i];
+    const int64_t perfect = std::max<int64_t>(1, (int64_t)std::ceil((double)tw / (double)instance_k[i]));
+    const int64_t lmax = (int64_t)((1.0 + instance_eps[i]) * (double)perfect);
+    for (int32_t b = 0; b < instance_k[i]; ++b) {
+      hp[boff[i] + b] = perfect;
+      hl[boff[i] + b] = lmax;
+    }
+  }
+  s->h_inst_boff = boff;
+  s->h_inst_k.assign(instance_k, instance_k + I);
+  return set_partition_impl(s, (int32_t)K, kmax, gpart.data(), hl, hp);
 }
 
 lpgpu_status lpgpu_session_set_partition(lpgpu_session* s, int32_t k, double eps,
@@ -403,6 +572,10 @@ lpgpu_status lpgpu_session_set_partition(lpgpu_session* s, int32_t k, double eps
   if (!s) return invalid("null session");
   if (!s->has_hg) {
     set_error("set_partition before upload");
+    return LPGPU_ERR_STATE;
+  }
+  if (s->batched) {
+    set_error("batched session: use lpgpu_session_set_partition_batch");
     return LPGPU_ERR_STATE;
   }
   if (k < 1 || k > LPGPU_MAX_K) return invalid("k must be in [1, 1024]");
@@ -418,32 +591,7 @@ lpgpu_status lpgpu_session_set_partition(lpgpu_session* s, int32_t k, double eps
     hl[b] = max_w ? max_w[b] : lmax;
     if (hp[b] < 1) hp[b] = 1;
   }
-  DeviceGuard g(s->device);
-  CK(cudaStreamSynchronize(s->st));
-  s->release_partition();
-  s->k = k;
-  s->W = word_class_of(k);
-  int64_t* fp = &s->footprint;
-  CK(s->part.alloc(s->n, fp));
-  CK(s->phi.alloc((size_t)s->m * k, fp));
-  CK(s->conn.alloc((size_t)s->m * 2 * s->W, fp));
-  CK(s->bw.alloc(k, fp));
-  CK(s->lmax.alloc(k, fp));
-  CK(s->perfect.alloc(k, fp));
-  CK(s->blk64.alloc(7 * k + 1, fp));
-  CK(s->thr.alloc(2 * k, fp));
-  CK(s->over.alloc(2 * k, fp));
-  cudaStream_t st = s->st;
-  if (s->n > 0) CK(cudaMemcpyAsync(s->part.p, partition, sizeof(int32_t) * s->n, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(s->lmax.p, hl.data(), sizeof(int64_t) * k, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(s->perfect.p, hp.data(), sizeof(int64_t) * k, cudaMemcpyHostToDevice, st));
-  CK(cudaMemsetAsync(s->blk64.p, 0, sizeof(int64_t) * (7 * k + 1), st));
-  RoundCtx c = s->ctx();
-  CK(launch_init_partition(s->launch(), c));
-  CK(cudaStreamSynchronize(st));
-  s->h_perfect = hp;
-  s->has_part = true;
-  return LPGPU_OK;
+  return set_partition_impl(s, k, k, partition, hl, hp);
 }
 
 static lpgpu_status read_metrics(lpgpu_session* s, int64_t* km1, int64_t* cut) {
@@ -513,6 +661,8 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
     if ((e = cudaMemsetAsync(s->blk64.p, 0, sizeof(int64_t) * (7 * s->k + 1), st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(s->scal.p, 0, sizeof(int64_t) * kScalars, st)) != cudaSuccess) return e;
     if (s->m > 0 && (e = cudaMemsetAsync(s->net_epoch.p, 0, sizeof(int32_t) * s->m, st)) != cudaSuccess) return e;
+    if (s->batched && (e = cudaMemsetAsync(s->inst_delta.p, 0, sizeof(int64_t) * s->num_inst, st)) != cudaSuccess)
+      return e;
     if (num_nodes > 0) {
       if ((e = launch_mark_list(L, c, dnodes.p, num_nodes)) != cudaSuccess) return e;
     } else {
@@ -648,6 +798,28 @@ lpgpu_status lpgpu_session_get_partition(lpgpu_session* s, int32_t* partition) {
   DeviceGuard g(s->device);
   if (s->n > 0) CK(cudaMemcpyAsync(partition, s->part.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
+  if (s->batched)  // global block ids back to instance-local ids
+    for (int32_t i = 0; i < s->num_inst; ++i)
+      for (int64_t v = s->h_inst_voff[i]; v < s->h_inst_voff[i + 1]; ++v) partition[v] -= s->h_inst_boff[i];
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_instance_km1(lpgpu_session* s, int64_t* km1) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  if (!km1) return invalid("null output");
+  DeviceGuard g(s->device);
+  if (!s->batched) {
+    return read_metrics(s, km1, nullptr);
+  }
+  int64_t fp = 0;
+  DevBuf<int64_t> d;
+  CK(d.alloc(s->num_inst, &fp));
+  RoundCtx c = s->ctx();
+  CK(launch_instance_metrics(s->launch(), c, d.p));
+  CK(cudaMemcpyAsync(km1, d.p, sizeof(int64_t) * s->num_inst, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  d.release(&fp);
   return LPGPU_OK;
 }
 
@@ -675,7 +847,7 @@ lpgpu_status lpgpu_session_get_pin_counts(lpgpu_session* s, int32_t* pc) {
   if (ps != LPGPU_OK) return ps;
   DeviceGuard g(s->device);
   if (s->m > 0)
-    CK(cudaMemcpyAsync(pc, s->phi.p, sizeof(int32_t) * s->m * s->k, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemcpyAsync(pc, s->phi.p, sizeof(int32_t) * s->m * s->kmax, cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
   return LPGPU_OK;
 }
@@ -684,7 +856,7 @@ lpgpu_status lpgpu_session_get_connectivity(lpgpu_session* s, uint32_t* words) {
   lpgpu_status ps = need_part(s);
   if (ps != LPGPU_OK) return ps;
   DeviceGuard g(s->device);
-  const int wc = word_count(s->k);
+  const int wc = word_count(s->kmax);
   if (s->m > 0) {
     // device rows hold 2W words (W >= wc words of Λ, then Λ1); copy the first wc of every row
     CK(cudaMemcpy2DAsync(words, sizeof(uint32_t) * wc, s->conn.p, sizeof(uint32_t) * 2 * s->W,
@@ -710,6 +882,10 @@ lpgpu_status lpgpu_session_get_incidence(lpgpu_session* s, int64_t* vtx_off, int
 lpgpu_status lpgpu_session_best_moves(lpgpu_session* s, int32_t* to, int32_t* gain, uint8_t* border) {
   lpgpu_status ps = need_part(s);
   if (ps != LPGPU_OK) return ps;
+  if (s->batched) {
+    set_error("this query needs a single-instance session");
+    return LPGPU_ERR_STATE;
+  }
   DeviceGuard g(s->device);
   int64_t fp = 0;
   DevBuf<int32_t> dto, dgain;
@@ -734,6 +910,10 @@ lpgpu_status lpgpu_session_best_moves(lpgpu_session* s, int32_t* to, int32_t* ga
 lpgpu_status lpgpu_session_gain_cache(lpgpu_session* s, int32_t* benefit, int32_t* penalty) {
   lpgpu_status ps = need_part(s);
   if (ps != LPGPU_OK) return ps;
+  if (s->batched) {
+    set_error("this query needs a single-instance session");
+    return LPGPU_ERR_STATE;
+  }
   DeviceGuard g(s->device);
   int64_t fp = 0;
   DevBuf<int32_t> db, dp;
@@ -755,6 +935,10 @@ lpgpu_status lpgpu_session_apply_moves(lpgpu_session* s, int64_t count, const in
                                        const int32_t* fs, const int32_t* ts, int64_t* delta) {
   lpgpu_status ps = need_part(s);
   if (ps != LPGPU_OK) return ps;
+  if (s->batched) {
+    set_error("this call needs a single-instance session");
+    return LPGPU_ERR_STATE;
+  }
   if (count < 0 || (count > 0 && (!vs || !fs || !ts))) return invalid("bad move list");
   DeviceGuard g(s->device);
   std::vector<int32_t> part(s->n);

@@ -70,7 +70,8 @@ SYMBOLS = [
     "lpgpu_session_enable_timing", "lpgpu_session_phase_times", "lpgpu_session_save_partition",
     "lpgpu_session_restore_partition", "lpgpu_kernel_launches", "lpgpu_host_alloc",
     "lpgpu_host_free", "lpgpu_session_event_record", "lpgpu_session_event_elapsed",
-    "lpgpu_session_synchronize",
+    "lpgpu_session_synchronize", "lpgpu_session_upload_batch", "lpgpu_session_set_partition_batch",
+    "lpgpu_session_instance_km1", "lpgpu_partition_metrics_noalloc",
 ]
 
 
@@ -145,6 +146,39 @@ class Session:
                                           _p(no, I64P), _p(pi, I32P), _p(wv, I32P), _p(we, I32P)))
         self._keep = None
         return self
+
+    def upload_batch(self, hgs):
+        """Uploads a list of hypergraphs as one batched union (instance order kept)."""
+        nv = np.array([0] + [h.n for h in hgs], np.int64).cumsum()
+        ne = np.array([0] + [h.m for h in hgs], np.int64).cumsum()
+        pin_base = np.array([0] + [h.num_pins for h in hgs], np.int64).cumsum()
+        net_off = np.concatenate([hgs[0].net_off[:1]] + [h.net_off[1:] + pin_base[i] for i, h in enumerate(hgs)])
+        pins = np.concatenate([h.pins.astype(np.int64) + nv[i] for i, h in enumerate(hgs)]).astype(np.int32)
+        w_v = np.concatenate([h.w_v for h in hgs]).astype(np.int32)
+        w_e = np.concatenate([h.w_e for h in hgs]).astype(np.int32)
+        self.n, self.m = int(nv[-1]), int(ne[-1])
+        self.inst_voff, self.inst_noff = nv, ne
+        self.num_inst = len(hgs)
+        _check(lib().lpgpu_session_upload_batch(self._h, ctypes.c_int32(len(hgs)), _p(nv, I64P), _p(ne, I64P),
+                                                _p(np.ascontiguousarray(net_off, np.int64), I64P),
+                                                _p(pins, I32P), _p(w_v, I32P), _p(w_e, I32P)))
+        return self
+
+    def set_partition_batch(self, ks, parts, eps=0.03):
+        """Per-instance k and instance-local partitions (list of arrays)."""
+        ks = np.ascontiguousarray(ks, np.int32)
+        ep = np.ascontiguousarray(np.broadcast_to(np.asarray(eps, np.float64), ks.shape), np.float64)
+        part = np.ascontiguousarray(np.concatenate(parts), np.int32)
+        self.k = int(ks.max())
+        _check(lib().lpgpu_session_set_partition_batch(self._h, _p(ks, I32P),
+                                                       ep.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                       _p(part, I32P)))
+        return self
+
+    def instance_km1(self):
+        out = np.empty(getattr(self, "num_inst", 1), np.int64)
+        _check(lib().lpgpu_session_instance_km1(self._h, _p(out, I64P)))
+        return out
 
     def set_partition(self, k, part, eps=0.03, lmax=None, perfect=None):
         self.k = int(k)

@@ -1,0 +1,76 @@
+"""Batched sessions: many independent hypergraphs refined in the same launches.
+Every instance must end exactly as when refined alone (device and oracle)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _instances(seed, count):
+    from lpgpu import gen
+    out = []
+    rng = np.random.default_rng(seed)
+    for i in range(count):
+        n = int(rng.integers(40, 700))           # sizes not aligned to 32 on purpose
+        m = int(n * rng.uniform(0.8, 1.4))
+        k = int(rng.choice([2, 3, 4, 7, 16, 33]))
+        out.append(gen.random_small(1000 * seed + i, n=n, m=m, k=k, max_size=9, weighted=bool(i % 2)))
+    return out
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_batch_equals_instances_alone(lp, orc, seed):
+    insts = _instances(seed, 12)
+    cfg = lp.default_config(rounds=5, subrounds=4)
+    with lp.Session(0) as s:
+        s.upload_batch([x.hg for x in insts])
+        s.set_partition_batch([x.k for x in insts], [x.part for x in insts], eps=0.03)
+        before = s.instance_km1()
+        r = s.refine(cfg)
+        part = s.partition()
+        after = s.instance_km1()
+        total_km1 = s.metrics()[0]
+    assert r.km1_after == r.km1_before + r.delta == total_km1 == after.sum()
+    off = np.cumsum([0] + [x.hg.n for x in insts])
+    for i, x in enumerate(insts):
+        with lp.Session(0) as one:
+            one.upload(x.hg)
+            one.set_partition(x.k, x.part, eps=0.03)
+            km0 = one.metrics()[0]
+            one.refine(cfg)
+            alone = one.partition()
+            km1 = one.metrics()[0]
+        assert np.array_equal(part[off[i]:off[i + 1]], alone), f"instance {i}"
+        assert (before[i], after[i]) == (km0, km1)
+        ref, _ = orc.lp_sync(x.hg, x.k, x.lmax, x.part, perfect=x.perfect, rounds=5, subrounds=4,
+                             revert=1, rollback=1, zero_gain=1)
+        assert np.array_equal(alone, ref)
+
+
+def test_batch_state_and_errors(lp, orc):
+    insts = _instances(7, 5)
+    with lp.Session(0) as s:
+        s.upload_batch([x.hg for x in insts])
+        with pytest.raises(lp.LpgpuError) as e:
+            s.set_partition(2, np.zeros(s.n, np.int32))
+        assert e.value.status == lp.ERR_STATE
+        s.set_partition_batch([x.k for x in insts], [x.part for x in insts])
+        with pytest.raises(lp.LpgpuError):
+            s.best_moves()
+        bw = s.block_weights()
+        kk = 0
+        for x in insts:
+            _, _, obw = orc.init_partition(x.hg, x.k, x.part)
+            assert np.array_equal(bw[kk:kk + x.k], obw)
+            kk += x.k
+    with lp.Session(0) as s:
+        bad = [insts[0].hg, insts[1].hg]
+        from lpgpu import gen
+        # a net that reaches into the next instance is rejected
+        h = bad[0]
+        pins = h.pins.copy()
+        pins[0] = h.n  # first vertex of the next instance in union ids
+        broken = gen.Hypergraph(h.n, h.m, h.net_off, pins, h.w_v, h.w_e)
+        with pytest.raises(lp.LpgpuError) as e:
+            s.upload_batch([broken, bad[1]])
+        assert e.value.status == lp.ERR_INVALID_ARG
