@@ -870,7 +870,7 @@ cudaError_t launch_gain_cache(const Launch& L, const RoundCtx& c, int32_t* benef
 // all concurrent moves is exactly the km1 change.
 __device__ __forceinline__ int64_t warp_commit_vertex(const RoundCtx& c, int64_t v, int f, int t) {
   int64_t att = 0;
-  const int k = c.k, W = c.W;
+  const int k = c.kmax, W = c.W;
   const uint32_t fbit = 1u << (f & 31), tbit = 1u << (t & 31);
   for (int64_t j = c.vtx_off[v] + lane_id(); j < c.vtx_off[v + 1]; j += 32) {
     const int64_t e = c.inets[j];
@@ -1515,13 +1515,13 @@ __device__ __forceinline__ int commit_incidence(const RoundCtx& c, int64_t e, in
   uint32_t* rec = c.conn + e * 2 * W;
   const uint32_t fbit = 1u << (f & 31), tbit = 1u << (t & 31);
   int att = 0;
-  const int of = atomicSub(&c.phi[e * c.k + f], 1);
+  const int of = atomicSub(&c.phi[e * c.kmax + f], 1);  // Φ rows hold kmax entries
   if (of == 1) {
     atomicXor(&rec[f >> 5], fbit);
     att -= we;
   }
   if (of == 1 || of == 2) atomicXor(&rec[W + (f >> 5)], fbit);
-  const int ot = atomicAdd(&c.phi[e * c.k + t], 1);
+  const int ot = atomicAdd(&c.phi[e * c.kmax + t], 1);
   if (ot == 0) {
     atomicXor(&rec[t >> 5], tbit);
     att += we;
@@ -1546,7 +1546,10 @@ constexpr int kPackThreads = 256;
 __global__ void __launch_bounds__(kPackThreads, 4) k_commit(RoundCtx c, int round, int sub, int last) {
   extern __shared__ ull s_dw[];
   __shared__ unsigned char s_own[kPackThreads];
-  for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_dw[b] = 0;
+  // block-weight deltas: shared memory for one instance, global atomics for a batch
+  ull* dw = c.batched ? reinterpret_cast<ull*>(c.bw) : s_dw;
+  const int kdw = c.batched ? 0 : c.k;
+  for (int b = threadIdx.x; b < kdw; b += blockDim.x) s_dw[b] = 0;
   __syncthreads();
   const int lane = lane_id();
   unsigned char* own = s_own + (threadIdx.x & ~31);
@@ -1596,8 +1599,8 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_commit(RoundCtx c, int roun
       c.part[v] = r.x;
       if (last) c.next_flag[v] = 1;
       const int64_t wv = c.w_v[v];
-      atomicAdd(&s_dw[r.x], (ull)wv);
-      atomicAdd(&s_dw[f], (ull)(-wv));
+      atomicAdd(&dw[r.x], (ull)wv);
+      atomicAdd(&dw[f], (ull)(-wv));
       ++moved;
     }
   }
@@ -1608,7 +1611,7 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_commit(RoundCtx c, int roun
     atomicAdd(reinterpret_cast<ull*>(&c.stats[(int64_t)round * kStats + kStMoved]), (ull)moved);
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < c.k; b += blockDim.x)
+  for (int b = threadIdx.x; b < kdw; b += blockDim.x)
     if (s_dw[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_dw[b]);
   if (last && last_cta(&c.scal[kDone])) close_subround(c, round);
 }
@@ -1668,7 +1671,9 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_undo(RoundCtx c, int round,
   const bool roll = rollback && (c.batched || c.scal[kDeltaSub] > 0);
   extern __shared__ ull s_dw[];
   __shared__ unsigned char s_own[kPackThreads];
-  for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_dw[b] = 0;
+  ull* dw = c.batched ? reinterpret_cast<ull*>(c.bw) : s_dw;
+  const int kdw = c.batched ? 0 : c.k;
+  for (int b = threadIdx.x; b < kdw; b += blockDim.x) s_dw[b] = 0;
   __syncthreads();
   const int lane = lane_id();
   unsigned char* own = s_own + (threadIdx.x & ~31);
@@ -1714,8 +1719,8 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_undo(RoundCtx c, int round,
           atomicAdd(reinterpret_cast<ull*>(&c.inst_delta[c.vinst[v]]), (ull)(int64_t)tot);
         c.part[v] = r.y;
         const int64_t wv = c.w_v[v];
-        atomicAdd(&s_dw[r.y], (ull)wv);
-        atomicAdd(&s_dw[r.x], (ull)(-wv));
+        atomicAdd(&dw[r.y], (ull)wv);
+        atomicAdd(&dw[r.x], (ull)(-wv));
         if (rollback) c.status[pos] = 3;
         ++undone;
       }
@@ -1737,7 +1742,7 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_undo(RoundCtx c, int round,
     atomicAdd(reinterpret_cast<ull*>(&stt[kStReverted]), (ull)undone);
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < c.k; b += blockDim.x)
+  for (int b = threadIdx.x; b < kdw; b += blockDim.x)
     if (s_dw[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_dw[b]);
   if (last && last_cta(&c.scal[kDone])) close_subround(c, round);
 }
@@ -1771,6 +1776,7 @@ cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, PhaseTimer* t
 
 cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int sub, PhaseTimer* timer) {
   const int k = c.k;
+  const size_t dw_smem = c.batched ? 0 : sizeof(ull) * k;  // shared block-weight deltas
   const int64_t n = c.n;
   {
     Scope sc(timer, "sweep");
@@ -1790,19 +1796,19 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
   const int last_commit = !c.revert && !c.rollback;
   {
     Scope sc(timer, "commit");
-    k_commit<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub, last_commit);
+    k_commit<<<g, 256, dw_smem, L.st>>>(c, round, sub, last_commit);
     LAUNCHED("k_commit");
   }
   if (c.revert) {
     Scope sc(timer, "revert");
     k_revert_eval<<<g, 256, 0, L.st>>>(c, sub);
     LAUNCHED("k_revert_eval");
-    k_undo<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub, 0, !c.rollback);
+    k_undo<<<g, 256, dw_smem, L.st>>>(c, round, sub, 0, !c.rollback);
     LAUNCHED("k_undo");
   }
   if (c.rollback) {
     Scope sc(timer, "rollback");
-    k_undo<<<g, 256, sizeof(ull) * k, L.st>>>(c, round, sub, 1, 1);
+    k_undo<<<g, 256, dw_smem, L.st>>>(c, round, sub, 1, 1);
     LAUNCHED("k_undo");
   }
   return cudaSuccess;
