@@ -1178,6 +1178,8 @@ __device__ void plan_to(const RoundCtx& c) {
       c.thr_to[b] = ~0ull;
       c.thr_from[b] = ~0ull;
       c.over_from[b] = 0;
+      c.acc_w[b] = 0;  // source-side sums of this sub-round start from zero
+      c.acc_cnt[b] = 0;
     }
     int64_t total;
     const int64_t off = block_scan_excl_i64(cnt, &total) + s_run;
