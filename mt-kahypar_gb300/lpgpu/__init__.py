@@ -118,7 +118,7 @@ class Session:
     def __init__(self, device: int = 0):
         self._h = ctypes.c_void_p()
         _check(lib().lpgpu_session_create(ctypes.c_int32(device), ctypes.byref(self._h)))
-        self.n = self.m = self.k = 0
+        self.n = self.m = self.k = self.num_blocks = 0
 
     def close(self):
         if self._h:
@@ -169,7 +169,8 @@ class Session:
         ks = np.ascontiguousarray(ks, np.int32)
         ep = np.ascontiguousarray(np.broadcast_to(np.asarray(eps, np.float64), ks.shape), np.float64)
         part = np.ascontiguousarray(np.concatenate(parts), np.int32)
-        self.k = int(ks.max())
+        self.k = int(ks.max())          # Φ row width (largest instance k)
+        self.num_blocks = int(ks.sum())  # global blocks: block weights come one per block
         _check(lib().lpgpu_session_set_partition_batch(self._h, _p(ks, I32P),
                                                        ep.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                                        _p(part, I32P)))
@@ -182,6 +183,7 @@ class Session:
 
     def set_partition(self, k, part, eps=0.03, lmax=None, perfect=None):
         self.k = int(k)
+        self.num_blocks = int(k)
         p = np.ascontiguousarray(part, np.int32)
         lm = None if lmax is None else np.ascontiguousarray(lmax, np.int64)
         pf = None if perfect is None else np.ascontiguousarray(perfect, np.int64)
@@ -214,7 +216,7 @@ class Session:
         return km1.value, cut.value, imb.value
 
     def block_weights(self):
-        out = np.empty(self.k, np.int64)
+        out = np.empty(self.num_blocks, np.int64)
         _check(lib().lpgpu_session_get_block_weights(self._h, _p(out, I64P)))
         return out
 
