@@ -49,7 +49,12 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
-    ap.add_argument("--workload", choices=["rownet", "plain_large", "plain_small"], default="rownet")
+    ap.add_argument("--workload", choices=["rownet", "plain_large", "plain_small", "batch", "served"],
+                    default="rownet")
+    ap.add_argument("--instances", type=int, default=None,
+                    help="batch: instances (default 4096); served: requests (default 256)")
+    ap.add_argument("--rate", type=float, default=2000.0, help="served: Poisson arrival rate (req/s)")
+    ap.add_argument("--slots", type=int, default=2, help="served: concurrent batched sessions")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--subrounds", type=int, default=16)
     ap.add_argument("--no-baseline", action="store_true", help="skip the CPU baseline leg")
@@ -360,10 +365,130 @@ def e2e_leg(args, inst, cfg, device, dist):
             "path": "lpgpu_session_upload + set_partition + refine + get_partition from pinned host buffers"}
 
 
+def batch_arm(args):
+    """Many small hypergraphs (vertex counts log-uniform in [1,024, 65,536], nets 1.1x,
+    geometric net sizes, k in {2,4,8,16}): one batched session refining all of them
+    together vs. the plain loop (one instance per call sequence), both end to end
+    from host buffers (upload, set partition, 5 rounds, download). Per-instance km1
+    must be identical."""
+    import lpgpu
+    from lpgpu import gen
+    insts = gen.generate_many("batch_instance", args.seed, args.instances or 4096)  # before any CUDA call
+    lpgpu.build()
+    hgs = [x.hg for x in insts]
+    ks = [x.k for x in insts]
+    parts = [x.part for x in insts]
+    cfg = lpgpu.default_config(rounds=5, subrounds=args.subrounds)
+    pins_total = sum(h.num_pins for h in hgs)
+
+    def batched_once(s):
+        s.upload_batch(hgs)
+        s.set_partition_batch(ks, parts, eps=0.03)
+        r = s.refine(cfg)
+        s.partition()
+        return r.pins_processed, s.instance_km1()
+
+    with lpgpu.Session(0) as s:
+        for _ in range(max(1, args.warmup)):
+            batched_once(s)
+        t0 = time.perf_counter()
+        bp = 0
+        for _ in range(args.steps):
+            p, km_b = batched_once(s)
+            bp += p
+        t_batch = (time.perf_counter() - t0) / args.steps
+        # device-resident refine only (inputs in HBM): one refine per step from the same start
+        s.save_partition()
+        for _ in range(2):
+            s.restore_partition()
+            s.refine(cfg)
+        s.synchronize()
+        s.record(0)
+        for _ in range(args.steps):
+            s.restore_partition()
+            r = s.refine(cfg)
+        s.record(1)
+        t_dev = s.elapsed_ms(0, 1) / 1e3 / args.steps
+        dev_pins = r.pins_processed
+
+    best_plain = None
+    for flags in (0, lpgpu.FLAG_NO_GRAPH):
+        pcfg = lpgpu.default_config(rounds=5, subrounds=args.subrounds, flags=flags)
+        with lpgpu.Session(0) as s:
+            km_p = np.zeros(len(insts), np.int64)
+            pp = 0
+            t0 = time.perf_counter()
+            for i, x in enumerate(insts):
+                s.upload(x.hg)
+                s.set_partition(x.k, x.part, eps=0.03)
+                r = s.refine(pcfg)
+                s.partition()
+                km_p[i] = r.km1_after
+                pp += r.pins_processed
+            t_plain = time.perf_counter() - t0
+        if best_plain is None or t_plain < best_plain[0]:
+            best_plain = (t_plain, flags, km_p, pp)
+    t_plain, flags, km_p, pp = best_plain
+    same = bool(np.array_equal(km_b, km_p))
+    line = {"metric": "batched LP refinement throughput (pins processed per second, end to end)",
+            "value": (bp / args.steps) / t_batch, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_batch, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": f"{len(insts)} independent hypergraphs, {sum(h.n for h in hgs)} vertices, "
+                                   f"{pins_total} pins in total, k in {{2,4,8,16}}, 5 rounds",
+                       "subrounds": args.subrounds},
+            "device_resident": {"value": dev_pins / t_dev, "ms_per_step": 1e3 * t_dev},
+            "plain_loop": {"value": pp / t_plain, "ms_per_step": 1e3 * t_plain,
+                           "launch_mode": "direct" if flags else "graph"},
+            "speedup_vs_plain_loop": t_plain / t_batch, "km1_identical": same,
+            "km1_total": int(km_b.sum())}
+    print(json.dumps(line), flush=True)
+    return 0 if same else 1
+
+
+def served_arm(args):
+    """Refine requests arriving as a Poisson stream (vertex counts log-uniform in
+    [1,024, 2,097,152], Zipf nets, k in {2..64}, 8 rounds): the continuous-batching
+    server vs. the plain sequential loop on the same arrival times. Reports p50/p99
+    latency and throughput; every request's km1 must be identical."""
+    import lpgpu
+    from lpgpu import gen, serve
+    insts = gen.generate_many("served_request", args.seed, args.instances or 256)  # before any CUDA call
+    lpgpu.build()
+    arr = serve.poisson_arrivals(len(insts), args.rate, args.seed)
+
+    def requests():
+        return [serve.Request(i, x.hg, x.k, x.eps, x.part, x.rounds, float(arr[i])) for i, x in enumerate(insts)]
+
+    # warm-up: one small batch through a server and one plain call
+    warm = [serve.Request(0, insts[0].hg, insts[0].k, insts[0].eps, insts[0].part, insts[0].rounds, 0.0)]
+    serve.replay(serve.RefineServer(slots=args.slots), warm)
+    serve.plain_loop(warm)
+    rs = requests()
+    st_s = serve.replay(serve.RefineServer(slots=args.slots, subrounds=args.subrounds), rs)
+    rp = requests()
+    st_p = serve.plain_loop(rp, subrounds=args.subrounds)
+    same = all(a.km1 == b.km1 and np.array_equal(a.result, b.result) for a, b in zip(rs, rp))
+    ss, sp = st_s.summary(), st_p.summary()
+    line = {"metric": "served LP refinement p99 latency (Poisson arrivals)", "value": ss["p99_ms"], "unit": "ms",
+            "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": f"{len(insts)} requests at {args.rate:.0f} req/s, "
+                                   f"{sum(x.hg.num_pins for x in insts)} pins in total, 8 rounds each",
+                       "slots": args.slots, "budget_gb": 150, "subrounds": args.subrounds},
+            "server": ss, "plain_loop": sp, "identical_results": same}
+    print(json.dumps(line), flush=True)
+    return 0 if same else 1
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "batch":
+        return batch_arm(args)
+    if args.workload == "served":
+        return served_arm(args)
     return gpu_arm(args)
 
 

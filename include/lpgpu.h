@@ -67,9 +67,13 @@ typedef struct {
   int32_t subrounds;            /* sub-rounds per round (>= 1) */
   int32_t revert;               /* 1: undo moves whose reverse now strictly improves km1 */
   int32_t rollback;             /* 1: undo a sub-round whose summed delta is positive */
-  int32_t reserved0;
+  int32_t flags;                /* LPGPU_FLAG_* */
   int32_t reserved1;
 } lpgpu_config;
+
+/* lpgpu_config.flags: launch the refine directly instead of capturing it once
+ * as a CUDA graph and replaying it (useful when every call has new sizes). */
+#define LPGPU_FLAG_NO_GRAPH 1
 
 /* Result of one refine call. Mirrors the kahypar::Metrics update done in
  * LabelPropagationRefiner::refineImpl (label_propagation_refiner.cpp:48-67). */

@@ -303,7 +303,7 @@ void lpgpu_config_default(lpgpu_config* cfg) {
   cfg->subrounds = 16;
   cfg->revert = 1;
   cfg->rollback = 1;
-  cfg->reserved0 = 0;
+  cfg->flags = 0;
   cfg->reserved1 = 0;
 }
 
@@ -680,7 +680,7 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
     if (s->n > 0 && (e = cudaMemsetAsync(s->next_flag.p, 0, s->n, st)) != cudaSuccess) return e;
     return cudaSuccess;
   };
-  if (num_nodes > 0 || tm) {
+  if (num_nodes > 0 || tm || (cfg.flags & LPGPU_FLAG_NO_GRAPH)) {
     // direct launches: explicit node lists, and per-phase event timing
     if (tm) tm->reset();
     CK(enqueue());

@@ -21,13 +21,14 @@ U8P = ctypes.POINTER(ctypes.c_uint8)
 
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_ADMISSION, ERR_TIMEOUT, ERR_CUDA, ERR_NO_DEVICE, ERR_STATE = range(8)
 MAX_K = 1024
+FLAG_NO_GRAPH = 1
 
 
 class Config(ctypes.Structure):
     _fields_ = [("rounds", ctypes.c_int32), ("activation_threshold", ctypes.c_int32),
                 ("rebalancing", ctypes.c_int32), ("subrounds", ctypes.c_int32),
                 ("revert", ctypes.c_int32), ("rollback", ctypes.c_int32),
-                ("reserved0", ctypes.c_int32), ("reserved1", ctypes.c_int32)]
+                ("flags", ctypes.c_int32), ("reserved1", ctypes.c_int32)]
 
 
 class Result(ctypes.Structure):

@@ -243,7 +243,8 @@ def rownet(seed=0, n=4194304, k=128, eps=0.03, rounds=10, target_nnz=None) -> In
     return Instance("rownet", hg, k, eps, part, rounds)
 
 
-def batch_instance(seed, idx, lo=1024, hi=65536, ks=(2, 4, 8, 16), eps=0.03, rounds=5) -> Instance:
+def batch_instance(seed, idx, lo=1024, hi=65536, ks=(2, 4, 8, 16), eps=0.03, rounds=5,
+                   incidence=True) -> Instance:
     rng = np.random.default_rng([seed, 31, idx])
     n = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
     m = int(round(1.1 * n))
@@ -251,13 +252,15 @@ def batch_instance(seed, idx, lo=1024, hi=65536, ks=(2, 4, 8, 16), eps=0.03, rou
     sizes = _geom_sizes(rng, m, 4.0, 2, 256)
     anchors = rng.integers(0, n, size=m)
     net_off, pins = _build_csr(n, sizes, _window_pins(n, anchors, 512), rng, 2)
-    hg = Hypergraph(n, m, net_off, pins, np.ones(n, np.int32), np.ones(m, np.int32)).with_incidence()
+    hg = Hypergraph(n, m, net_off, pins, np.ones(n, np.int32), np.ones(m, np.int32))
+    if incidence:
+        hg.with_incidence()
     part = random_balanced_partition(n, k, rng)
     return Instance(f"batch[{idx}]", hg, k, eps, part, rounds)
 
 
 def served_request(seed, idx, lo=1024, hi=2097152, ks=(2, 4, 8, 16, 32, 64), eps=0.03,
-                   rounds=8) -> Instance:
+                   rounds=8, incidence=True) -> Instance:
     rng = np.random.default_rng([seed, 41, idx])
     n = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
     m = int(round(1.2 * n))
@@ -267,7 +270,9 @@ def served_request(seed, idx, lo=1024, hi=2097152, ks=(2, 4, 8, 16, 32, 64), eps
     net_off, pins = _build_csr(n, sizes, _window_pins(n, anchors, 4096, 0.2), rng, 2)
     w_v = rng.integers(1, 5, size=n).astype(np.int32)
     w_e = rng.integers(1, 9, size=m).astype(np.int32)
-    hg = Hypergraph(n, m, net_off, pins, w_v, w_e).with_incidence()
+    hg = Hypergraph(n, m, net_off, pins, w_v, w_e)
+    if incidence:
+        hg.with_incidence()
     part = random_balanced_partition(n, k, rng)
     return Instance(f"served[{idx}]", hg, k, eps, part, rounds)
 
@@ -282,6 +287,22 @@ def random_small(seed, n=200, m=240, k=4, max_size=8, weighted=True, eps=0.03, r
     hg = Hypergraph(n, m, net_off, pins, w_v, w_e).with_incidence()
     part = random_balanced_partition(n, k, rng)
     return Instance(f"random[{seed}]", hg, k, eps, part, rounds)
+
+
+def _one(name, seed, idx):
+    return globals()[name](seed, idx, incidence=False)
+
+
+def generate_many(name, seed, count, processes=None):
+    """Instances idx = 0..count-1 of `batch_instance` / `served_request`, built in a
+    spawn-context process pool (safe after a CUDA context exists)."""
+    import multiprocessing as mp
+    import os
+    procs = processes or min(count, os.cpu_count() or 1)
+    if procs <= 1:
+        return [_one(name, seed, i) for i in range(count)]
+    with mp.get_context("spawn").Pool(procs) as pool:
+        return pool.starmap(_one, [(name, seed, i) for i in range(count)], chunksize=max(1, count // (4 * procs)))
 
 
 WORKLOADS = {
