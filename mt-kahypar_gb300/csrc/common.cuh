@@ -55,6 +55,7 @@ enum Scalar : int {
   kEpoch = 8,      // activation stamp of the current round
   kDone = 9,       // arrival counter of the last-CTA pattern
   kOverCount = 10, // number of overflowing target blocks
+  kHeavyCount = 11, // vertices the sweep deferred to the heavy-vertex kernel
   kScalars = 16
 };
 
@@ -104,6 +105,7 @@ struct RoundCtx {
   // parameters
   int32_t zero_gain, revert, rollback;
   int32_t unit_nets;     // every net weight is 1
+  int32_t max_we;        // largest net weight (0 without nets)
   int64_t act_threshold;
   // batched sessions: many independent instances in one union hypergraph.
   // part[] holds global block ids (instance block offset + local id); Φ and
@@ -117,6 +119,7 @@ struct RoundCtx {
   const int32_t* inst_k;    // blocks of each instance
   int64_t* inst_delta;      // per-instance summed delta of the current sub-round
   int32_t* over_ids;        // target blocks that overflow (count in scal[kOverCount])
+  int32_t* heavy;           // list positions deferred by the sweep (count in scal[kHeavyCount])
 };
 
 // Global block offset of vertex v's instance.

@@ -472,9 +472,181 @@ __device__ __forceinline__ void decide(int k, int from, int wv, int internal, in
 }
 
 constexpr int kSweepThreads = 256;
+// Above this degree the tile windows of k_sweep (k > 128) defer a vertex to k_sweep_heavy.
+constexpr int kHeavyDegree = 1024;
 
 __device__ bool last_cta(int64_t* counter);
 __device__ void plan_to(const RoundCtx& c);
+
+// ---- lane-per-vertex sweep (k <= 128)
+//
+// A lane evaluates its own vertex: it walks the vertex's incident nets and adds
+// each net's Λ(e) bit vector (times w(e)) into bit-sliced counters, one
+// 32-block word t and plane p per register cnt[t][p], so that bit l of plane p
+// is bit p of the penalty of block 32 t + l. The best target then comes from a
+// bit-sliced maximum over the feasible blocks. Vertices whose summed incident
+// net weight stays below 2^PL take this path; the others take the
+// warp-cooperative windows below.
+constexpr int kLvWeights = 16;  // vertex weights 1..16 have precomputed feasibility masks
+
+// cnt += s0 + 2 s1 + 4 s2 (bit-sliced, ripple carry).
+template <int PL>
+__device__ __forceinline__ void lv_add3(uint32_t (&cnt)[PL], uint32_t s0, uint32_t s1, uint32_t s2) {
+  uint32_t cy = cnt[0] & s0;
+  cnt[0] ^= s0;
+  uint32_t t = cnt[1];
+  cnt[1] = t ^ s1 ^ cy;
+  cy = (t & s1) | (cy & (t ^ s1));
+  t = cnt[2];
+  cnt[2] = t ^ s2 ^ cy;
+  cy = (t & s2) | (cy & (t ^ s2));
+#pragma unroll
+  for (int p = 3; p < PL; ++p) {
+    const uint32_t c2 = cnt[p] & cy;
+    cnt[p] ^= cy;
+    cy = c2;
+  }
+}
+
+// cnt += w * x (bit-sliced; w < 2^PL).
+template <int PL>
+__device__ __forceinline__ void lv_add_weighted(uint32_t (&cnt)[PL], uint32_t x, int w) {
+  uint32_t cy = 0;
+#pragma unroll
+  for (int p = 0; p < PL; ++p) {
+    const uint32_t a = ((w >> p) & 1) ? x : 0u;
+    const uint32_t t = cnt[p];
+    cnt[p] = t ^ a ^ cy;
+    cy = (t & a) | (cy & (t ^ a));
+  }
+}
+
+// Best move of one vertex by its own lane: the same decision as `decide`
+// (Km1Policy::computeMaxGainMoveImpl with disable_randomization, plus the
+// zero-gain rebalancing rule of label_propagation_refiner.h:88-95). `from`,
+// `to` are local block ids; `bo` is the instance's first global block.
+template <int W, bool UNIT, int PL>
+__device__ __forceinline__ void lv_vertex(const RoundCtx& c, int64_t o0, int d, int from, int wv, int bo,
+                                          int inst, bool batched, int zero_gain,
+                                          const uint32_t* __restrict__ s_fmask, const int* __restrict__ s_slack,
+                                          const int64_t* __restrict__ s_bw, const int64_t* __restrict__ s_perf,
+                                          int& to, int& gain, bool& border) {
+  constexpr int U = 4;  // incidences whose loads are issued together
+  constexpr int W2 = 2 * W;
+  const int fw = from >> 5;
+  const uint32_t fbit = 1u << (from & 31);
+  uint32_t cnt[W][PL];
+#pragma unroll
+  for (int t = 0; t < W; ++t)
+#pragma unroll
+    for (int p = 0; p < PL; ++p) cnt[t][p] = 0;
+  int internal = 0;  // Σ w(e) over incident nets with Φ(e, from) > 1
+  for (int j = 0; j < d; j += U) {
+    int32_t ee[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) ee[u] = j + u < d ? __ldg(&c.inets[o0 + j + u]) : -1;
+    uint32_t wd[U][W], l1[U];
+    int we[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int t = 0; t < W; ++t) wd[u][t] = 0;
+      l1[u] = fbit;
+      we[u] = 0;
+      if (ee[u] >= 0) {
+        const uint32_t* rec = c.conn + (int64_t)ee[u] * W2;
+        load_words<W>(rec, wd[u]);
+        l1[u] = __ldg(rec + W + fw);
+        we[u] = UNIT ? 1 : __ldg(&c.w_e[ee[u]]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) internal += (l1[u] & fbit) ? 0 : we[u];
+    if constexpr (UNIT) {
+      // carry-save sum of the four vectors, then one 3-bit ripple add
+#pragma unroll
+      for (int t = 0; t < W; ++t) {
+        const uint32_t a = wd[0][t], b = wd[1][t], e = wd[2][t], f = wd[3][t];
+        const uint32_t s = a ^ b ^ e;
+        const uint32_t c1 = (a & b) | (e & (a ^ b));
+        const uint32_t c2 = s & f;
+        lv_add3<PL>(cnt[t], s ^ f, c1 ^ c2, c1 & c2);
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int t = 0; t < W; ++t) lv_add_weighted<PL>(cnt[t], wd[u][t], we[u]);
+    }
+  }
+  // feasible targets: c(V_b) + w(v) <= L_max(b)
+  uint32_t cand[W];
+  if (!batched && wv >= 1 && wv <= kLvWeights) {
+#pragma unroll
+    for (int t = 0; t < W; ++t) cand[t] = s_fmask[(wv - 1) * W + t];
+  } else {
+    const int kk = batched ? c.inst_k[inst] : c.k;
+#pragma unroll
+    for (int t = 0; t < W; ++t) {
+      uint32_t msk = 0;
+      for (int l = 0; l < 32; ++l) {
+        const int b = 32 * t + l;
+        if (b < kk) {
+          const int64_t sl = batched ? c.lmax[bo + b] - c.bw[bo + b] : (int64_t)s_slack[b];
+          if (sl >= wv) msk |= 1u << l;
+        }
+      }
+      cand[t] = msk;
+    }
+  }
+  // isBorderNode: some incident net holds a block other than `from`
+  uint32_t other = 0, anyc = 0;
+#pragma unroll
+  for (int t = 0; t < W; ++t) {
+    const uint32_t fm = t == fw ? ~fbit : ~0u;
+    uint32_t o = 0;
+#pragma unroll
+    for (int p = 0; p < PL; ++p) o |= cnt[t][p];
+    other |= o & fm;
+    cand[t] &= fm;
+    anyc |= cand[t];
+  }
+  if (!other) return;
+  border = true;
+  if (!anyc) return;
+  // maximum penalty over the candidates, plane by plane from the top
+  int val = 0;
+#pragma unroll
+  for (int p = PL - 1; p >= 0; --p) {
+    uint32_t tt[W], o = 0;
+#pragma unroll
+    for (int t = 0; t < W; ++t) {
+      tt[t] = cand[t] & cnt[t][p];
+      o |= tt[t];
+    }
+    if (o) {
+#pragma unroll
+      for (int t = 0; t < W; ++t) cand[t] = tt[t];
+      val |= 1 << p;
+    }
+  }
+  if (val < internal || (val == internal && !zero_gain)) return;
+  int b = 0;  // lowest block of maximum penalty
+#pragma unroll
+  for (int t = W - 1; t >= 0; --t)
+    if (cand[t]) b = 32 * t + __ffs(cand[t]) - 1;
+  if (val > internal) {
+    to = b;
+    gain = internal - val;
+    return;
+  }
+  const int64_t* bwp = batched ? c.bw + bo : s_bw;
+  const int64_t* pfp = batched ? c.perfect + bo : s_perf;
+  if (bwp[from] - 1 > bwp[b] + 1 && bwp[b] < pfp[b]) {
+    to = b;
+    gain = 0;
+  }
+}
 
 // Sweep: the best move of every active vertex (moveVertex's isBorderNode +
 // computeMaxGainMove, label_propagation_refiner.h:82-95) on the current state.
@@ -500,7 +672,7 @@ template <int W, bool UNIT>
 __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(RoundCtx c, int round, int sub,
                                                              int32_t* dbg_to, int32_t* dbg_gain,
                                                              uint8_t* dbg_border) {
-  constexpr int B = W <= 4 ? 4 : (W <= 8 ? 2 : 1);  // windows whose gathers are issued together
+  constexpr int B = W <= 8 ? 2 : 1;  // windows whose gathers are issued together (k > 128)
   extern __shared__ unsigned char smem_raw[];
   const bool batched = c.batched != 0;
   const int k = batched ? 0 : c.k;  // blocks kept in shared memory (none when batched)
@@ -511,7 +683,12 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(Round
   ull* s_out_w = s_in_w + k;
   int* s_slack = reinterpret_cast<int*>(s_out_w + k);
   unsigned* s_in_cnt = reinterpret_cast<unsigned*>(s_slack + k);
-  unsigned char* s_owner = reinterpret_cast<unsigned char*>(s_in_cnt + k) + (threadIdx.x >> 5) * 32;
+  // feasibility masks of the lane-per-vertex path: word t of weight w at (w - 1) W + t
+  constexpr bool kLv = W <= 4;
+  constexpr int PL = UNIT ? 6 : 8;  // lane-per-vertex counter planes
+  const int nfm = (kLv && !batched) ? kLvWeights * W : 0;
+  uint32_t* s_fmask = reinterpret_cast<uint32_t*>(s_in_cnt + k);
+  unsigned char* s_owner = reinterpret_cast<unsigned char*>(s_fmask + nfm) + (threadIdx.x >> 5) * 32;
   for (int b = threadIdx.x; b < k; b += blockDim.x) {
     const int64_t bw = c.bw[b];
     const int64_t sl = c.lmax[b] - bw;
@@ -523,6 +700,16 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(Round
     s_in_cnt[b] = 0;
   }
   __syncthreads();
+  for (int i = threadIdx.x; i < nfm; i += blockDim.x) {
+    const int w = i / W + 1, t = i % W;
+    uint32_t msk = 0;
+    for (int l = 0; l < 32; ++l) {
+      const int b = 32 * t + l;
+      if (b < k && s_slack[b] >= w) msk |= 1u << l;
+    }
+    s_fmask[i] = msk;
+  }
+  if (nfm) __syncthreads();
   const int lane = lane_id();
   int slack[W];
 #pragma unroll
@@ -553,167 +740,192 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(Round
       from = c.part[v] - bo;  // local block id
       wv = c.w_v[v];
     }
-    int incl = d;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(FULLMASK, incl, o);
-      if (lane >= o) incl += y;
-    }
-    const int excl = incl - d, eend = incl;
-    const int R = __shfl_sync(FULLMASK, incl, 31);  // incidences of the tile
-    const unsigned nz = __ballot_sync(FULLMASK, d > 0);
-    __syncwarp();
-    if (d > 0) s_owner[__popc(nz & lanemask_lt())] = (unsigned char)lane;
-    __syncwarp();
     int my_to = from, my_gain = 0;
     bool my_border = false;
-    // partial sums of the vertex that continues past the current window
-    int carry[W];
-#pragma unroll
-    for (int t = 0; t < W; ++t) carry[t] = 0;
-    int carry_int = 0;
-    bool carry_border = false;
-
-    // ---- the tile's incidences in windows of 32 (lane = incidence)
-    for (int wb0 = 0; wb0 < R; wb0 += 32 * B) {
-      uint32_t wd[B][W];
-      int icv[B], lamv[B], wev[B];
-#pragma unroll
-      for (int u = 0; u < B; ++u) {
-        const int wb = wb0 + 32 * u;
-        const int i = wb + lane;
-        const bool has = i < R;
-        const unsigned starts =
-            __reduce_or_sync(FULLMASK, (d > 0 && excl >= wb && excl < wb + 32) ? (1u << (excl - wb)) : 0u);
-        const int cb = __popc(__ballot_sync(FULLMASK, d > 0 && excl < wb));
-        const int ow = has ? s_owner[cb + __popc(starts & ((2u << lane) - 1u)) - 1] : 0;
-        const int64_t o_ow = __shfl_sync(FULLMASK, o0, ow);
-        const int ex_ow = __shfl_sync(FULLMASK, excl, ow);
-        const int f_ow = __shfl_sync(FULLMASK, from, ow);
-#pragma unroll
-        for (int t = 0; t < W; ++t) wd[u][t] = 0;
-        icv[u] = 0;
-        lamv[u] = 0;
-        wev[u] = 0;
-        if (has) {
-          const int64_t e = __ldcs(&c.inets[o_ow + i - ex_ow]);
-          const int we = UNIT ? 1 : __ldg(&c.w_e[e]);
-          const uint32_t* rec = c.conn + e * W2;
-          load_words<W>(rec, wd[u]);
-          const uint32_t l1 = __ldg(rec + W + (f_ow >> 5));
-          icv[u] = ((l1 >> (f_ow & 31)) & 1u) ? 0 : we;  // Φ(e, from) > 1
-          wev[u] = we;
-          int lam = 0;
-#pragma unroll
-          for (int t = 0; t < W; ++t) lam += __popc(wd[u][t]);
-          lamv[u] = lam;
-        }
+    // light vertices are evaluated here; heavy ones are deferred to k_sweep_heavy
+    bool defer = false;
+    if constexpr (kLv) {
+      if (d > 0) {
+        if ((int64_t)d * c.max_we < (1 << PL))
+          lv_vertex<W, UNIT, PL>(c, o0, d, from, wv, bo, inst, batched, zero_gain, s_fmask, s_slack, s_bw, s_perf,
+                                 my_to, my_gain, my_border);
+        else
+          defer = true;
+        d = 0;
       }
-#pragma unroll
-      for (int u = 0; u < B; ++u) {
-        const int wb = wb0 + 32 * u;
-        if (wb >= R) break;
-        uint32_t col[W];
-#pragma unroll
-        for (int t = 0; t < W; ++t) col[t] = transpose32(wd[u][t]);
-        const unsigned bm = __ballot_sync(FULLMASK, lamv[u] > 1);
-        const unsigned icb = __ballot_sync(FULLMASK, icv[u] != 0);
-        Planes wp, ip;
-        if constexpr (!UNIT) {
-          const int np = 32 - __clz(__reduce_or_sync(FULLMASK, (unsigned)wev[u]));
-          wp = make_planes(wev[u], np);
-          ip = make_planes(icv[u], np);
-        }
-        // vertices whose last incidence lies in this window
-        unsigned endm = __ballot_sync(FULLMASK, d > 0 && eend > wb && eend <= wb + 32);
-        while (endm) {
-          const int j = __ffs(endm) - 1;
-          endm &= endm - 1;
-          const int exj = __shfl_sync(FULLMASK, excl, j);
-          const int hi = __shfl_sync(FULLMASK, eend, j) - wb;
-          const int lo = exj > wb ? exj - wb : 0;
-          const unsigned mask = (hi == 32 ? FULLMASK : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
-          const bool cont = exj < wb;
-          if ((bm & mask) == 0 && !(cont && carry_border)) continue;  // not a border vertex
-          int internal;
-          int pen[W];
-          if constexpr (UNIT) {
-            internal = __popc(icb & mask);
-#pragma unroll
-            for (int t = 0; t < W; ++t) pen[t] = __popc(col[t] & mask);
-          } else {
-            internal = plane_sum(ip, mask, icv[u]);
-#pragma unroll
-            for (int t = 0; t < W; ++t) pen[t] = plane_sum(wp, col[t] & mask, wev[u]);
-          }
-          if (cont) {
-            internal += carry_int;
-#pragma unroll
-            for (int t = 0; t < W; ++t) pen[t] += carry[t];
-          }
-          const int fromj = __shfl_sync(FULLMASK, from, j);
-          const int wvj = __shfl_sync(FULLMASK, wv, j);
-          int to = fromj, gain = 0;
-          if (batched) {
-            const int ij = __shfl_sync(FULLMASK, inst, j);
-            const int boj = c.inst_boff[ij];
-            const int kj = c.inst_k[ij];
-            if (ij != slack_inst) {  // warp-uniform: reload the instance's block slack
-              slack_inst = ij;
-#pragma unroll
-              for (int t = 0; t < W; ++t) {
-                const int b = 32 * t + lane;
-                int sl = -1;
-                if (b < kj) {
-                  const int64_t x = c.lmax[boj + b] - c.bw[boj + b];
-                  sl = x < 0 ? -1 : (x > INT_MAX ? INT_MAX : (int)x);
-                }
-                slack[t] = sl;
-              }
-            }
-            decide<W, UNIT>(kj, fromj, wvj, internal, zero_gain, pen, slack, c.bw + boj, c.perfect + boj, to,
-                            gain);
-          } else {
-            decide<W, UNIT>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
-          }
-          if (lane == j) {
-            my_to = to;
-            my_gain = gain;
-            my_border = true;
+    } else if (d > kHeavyDegree) {
+      defer = true;
+      d = 0;
+    }
+    const unsigned dm = __ballot_sync(FULLMASK, defer);
+    if (dm) {
+      const int leader = __ffs(dm) - 1;
+      ull base = 0;
+      if (lane == leader) base = atomicAdd(reinterpret_cast<ull*>(&c.scal[kHeavyCount]), (ull)__popc(dm));
+      base = __shfl_sync(FULLMASK, base, leader);
+      if (defer) c.heavy[base + __popc(dm & lanemask_lt())] = (int32_t)pos;
+    }
+    if constexpr (!kLv) {  // k > 128: the tile's remaining vertices in warp windows
+      int incl = d;
+  #pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULLMASK, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int excl = incl - d, eend = incl;
+      const int R = __shfl_sync(FULLMASK, incl, 31);  // incidences of the tile
+      const unsigned nz = __ballot_sync(FULLMASK, d > 0);
+      __syncwarp();
+      if (d > 0) s_owner[__popc(nz & lanemask_lt())] = (unsigned char)lane;
+      __syncwarp();
+      // partial sums of the vertex that continues past the current window
+      int carry[W];
+  #pragma unroll
+      for (int t = 0; t < W; ++t) carry[t] = 0;
+      int carry_int = 0;
+      bool carry_border = false;
+
+      // ---- the tile's incidences in windows of 32 (lane = incidence)
+      for (int wb0 = 0; wb0 < R; wb0 += 32 * B) {
+        uint32_t wd[B][W];
+        int icv[B], lamv[B], wev[B];
+  #pragma unroll
+        for (int u = 0; u < B; ++u) {
+          const int wb = wb0 + 32 * u;
+          const int i = wb + lane;
+          const bool has = i < R;
+          const unsigned starts =
+              __reduce_or_sync(FULLMASK, (d > 0 && excl >= wb && excl < wb + 32) ? (1u << (excl - wb)) : 0u);
+          const int cb = __popc(__ballot_sync(FULLMASK, d > 0 && excl < wb));
+          const int ow = has ? s_owner[cb + __popc(starts & ((2u << lane) - 1u)) - 1] : 0;
+          const int64_t o_ow = __shfl_sync(FULLMASK, o0, ow);
+          const int ex_ow = __shfl_sync(FULLMASK, excl, ow);
+          const int f_ow = __shfl_sync(FULLMASK, from, ow);
+  #pragma unroll
+          for (int t = 0; t < W; ++t) wd[u][t] = 0;
+          icv[u] = 0;
+          lamv[u] = 0;
+          wev[u] = 0;
+          if (has) {
+            const int64_t e = __ldcs(&c.inets[o_ow + i - ex_ow]);
+            const int we = UNIT ? 1 : __ldg(&c.w_e[e]);
+            const uint32_t* rec = c.conn + e * W2;
+            load_words<W>(rec, wd[u]);
+            const uint32_t l1 = __ldg(rec + W + (f_ow >> 5));
+            icv[u] = ((l1 >> (f_ow & 31)) & 1u) ? 0 : we;  // Φ(e, from) > 1
+            wev[u] = we;
+            int lam = 0;
+  #pragma unroll
+            for (int t = 0; t < W; ++t) lam += __popc(wd[u][t]);
+            lamv[u] = lam;
           }
         }
-        // the vertex that continues into the next window (at most one)
-        const unsigned openm = __ballot_sync(FULLMASK, d > 0 && excl < wb + 32 && eend > wb + 32);
-        if (openm) {
-          const int j = __ffs(openm) - 1;
-          const int exj = __shfl_sync(FULLMASK, excl, j);
-          const int lo = exj > wb ? exj - wb : 0;
-          const unsigned mask = FULLMASK & ~((1u << lo) - 1u);
-          const bool cont = exj < wb;
-          int pint;
-          if constexpr (UNIT) {
-            pint = __popc(icb & mask);
-          } else {
-            pint = plane_sum(ip, mask, icv[u]);
+  #pragma unroll
+        for (int u = 0; u < B; ++u) {
+          const int wb = wb0 + 32 * u;
+          if (wb >= R) break;
+          uint32_t col[W];
+  #pragma unroll
+          for (int t = 0; t < W; ++t) col[t] = transpose32(wd[u][t]);
+          const unsigned bm = __ballot_sync(FULLMASK, lamv[u] > 1);
+          const unsigned icb = __ballot_sync(FULLMASK, icv[u] != 0);
+          Planes wp, ip;
+          if constexpr (!UNIT) {
+            const int np = 32 - __clz(__reduce_or_sync(FULLMASK, (unsigned)wev[u]));
+            wp = make_planes(wev[u], np);
+            ip = make_planes(icv[u], np);
           }
-          const bool pb = (bm & mask) != 0;
-#pragma unroll
-          for (int t = 0; t < W; ++t) {
-            int p;
+          // vertices whose last incidence lies in this window
+          unsigned endm = __ballot_sync(FULLMASK, d > 0 && eend > wb && eend <= wb + 32);
+          while (endm) {
+            const int j = __ffs(endm) - 1;
+            endm &= endm - 1;
+            const int exj = __shfl_sync(FULLMASK, excl, j);
+            const int hi = __shfl_sync(FULLMASK, eend, j) - wb;
+            const int lo = exj > wb ? exj - wb : 0;
+            const unsigned mask = (hi == 32 ? FULLMASK : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+            const bool cont = exj < wb;
+            if ((bm & mask) == 0 && !(cont && carry_border)) continue;  // not a border vertex
+            int internal;
+            int pen[W];
             if constexpr (UNIT) {
-              p = __popc(col[t] & mask);
+              internal = __popc(icb & mask);
+  #pragma unroll
+              for (int t = 0; t < W; ++t) pen[t] = __popc(col[t] & mask);
             } else {
-              p = plane_sum(wp, col[t] & mask, wev[u]);
+              internal = plane_sum(ip, mask, icv[u]);
+  #pragma unroll
+              for (int t = 0; t < W; ++t) pen[t] = plane_sum(wp, col[t] & mask, wev[u]);
             }
-            carry[t] = cont ? carry[t] + p : p;
+            if (cont) {
+              internal += carry_int;
+  #pragma unroll
+              for (int t = 0; t < W; ++t) pen[t] += carry[t];
+            }
+            const int fromj = __shfl_sync(FULLMASK, from, j);
+            const int wvj = __shfl_sync(FULLMASK, wv, j);
+            int to = fromj, gain = 0;
+            if (batched) {
+              const int ij = __shfl_sync(FULLMASK, inst, j);
+              const int boj = c.inst_boff[ij];
+              const int kj = c.inst_k[ij];
+              if (ij != slack_inst) {  // warp-uniform: reload the instance's block slack
+                slack_inst = ij;
+  #pragma unroll
+                for (int t = 0; t < W; ++t) {
+                  const int b = 32 * t + lane;
+                  int sl = -1;
+                  if (b < kj) {
+                    const int64_t x = c.lmax[boj + b] - c.bw[boj + b];
+                    sl = x < 0 ? -1 : (x > INT_MAX ? INT_MAX : (int)x);
+                  }
+                  slack[t] = sl;
+                }
+              }
+              decide<W, UNIT>(kj, fromj, wvj, internal, zero_gain, pen, slack, c.bw + boj, c.perfect + boj, to,
+                              gain);
+            } else {
+              decide<W, UNIT>(k, fromj, wvj, internal, zero_gain, pen, slack, s_bw, s_perf, to, gain);
+            }
+            if (lane == j) {
+              my_to = to;
+              my_gain = gain;
+              my_border = true;
+            }
           }
-          carry_int = cont ? carry_int + pint : pint;
-          carry_border = cont ? (carry_border || pb) : pb;
+          // the vertex that continues into the next window (at most one)
+          const unsigned openm = __ballot_sync(FULLMASK, d > 0 && excl < wb + 32 && eend > wb + 32);
+          if (openm) {
+            const int j = __ffs(openm) - 1;
+            const int exj = __shfl_sync(FULLMASK, excl, j);
+            const int lo = exj > wb ? exj - wb : 0;
+            const unsigned mask = FULLMASK & ~((1u << lo) - 1u);
+            const bool cont = exj < wb;
+            int pint;
+            if constexpr (UNIT) {
+              pint = __popc(icb & mask);
+            } else {
+              pint = plane_sum(ip, mask, icv[u]);
+            }
+            const bool pb = (bm & mask) != 0;
+  #pragma unroll
+            for (int t = 0; t < W; ++t) {
+              int p;
+              if constexpr (UNIT) {
+                p = __popc(col[t] & mask);
+              } else {
+                p = plane_sum(wp, col[t] & mask, wev[u]);
+              }
+              carry[t] = cont ? carry[t] + p : p;
+            }
+            carry_int = cont ? carry_int + pint : pint;
+            carry_border = cont ? (carry_border || pb) : pb;
+          }
         }
       }
     }
 
-    if (valid) {
+    if (valid && !defer) {
       if (query) {
         dbg_to[v] = my_to;
         if (dbg_gain) dbg_gain[v] = my_gain;
@@ -754,7 +966,140 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(Round
     }
     if (s_out_w[b]) atomicAdd(reinterpret_cast<ull*>(&c.cand_out[b]), s_out_w[b]);
   }
-  if (last_cta(&c.scal[kDone])) plan_to(c);
+  // the plan needs every candidate: with deferred vertices k_sweep_heavy makes it
+  if (last_cta(&c.scal[kDone]) && *(volatile int64_t*)&c.scal[kHeavyCount] == 0) plan_to(c);
+}
+
+// Heavy vertices deferred by k_sweep (summed net weight too large for the
+// lane counters, or more than kHeavyDegree incidences): one CTA per vertex,
+// whose warps split the incidence windows (lane = incidence, Λ words
+// transposed so that lane l counts block l + 32 t), sum their per-block
+// penalties in shared memory, and warp 0 decides. Its last CTA plans the
+// selection and clears the deferred count.
+template <int W, bool UNIT>
+__global__ void __launch_bounds__(kSweepThreads) k_sweep_heavy(RoundCtx c, int round, int32_t* dbg_to,
+                                                               int32_t* dbg_gain, uint8_t* dbg_border) {
+  const int64_t nh = *(volatile int64_t*)&c.scal[kHeavyCount];
+  if (nh == 0) return;  // the sweep planned already
+  constexpr int B = W <= 4 ? 4 : (W <= 8 ? 2 : 1);  // windows per warp whose gathers are issued together
+  constexpr int W2 = 2 * W;
+  __shared__ int s_pen[32 * W];
+  __shared__ ull s_int;
+  __shared__ int s_border;
+  const bool query = dbg_to != nullptr;
+  const bool batched = c.batched != 0;
+  const int lane = lane_id(), wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int zero_gain = query ? 0 : c.zero_gain;
+  int64_t cands = 0;
+  for (int64_t i = blockIdx.x; i < nh; i += gridDim.x) {
+    const int32_t pos = c.heavy[i];
+    const int64_t v = query ? pos : c.list[pos];
+    const int64_t o0 = c.vtx_off[v];
+    const int d = (int)(c.vtx_off[v + 1] - o0);  // 0 < d <= kHighDegree for deferred vertices
+    const int inst = batched ? c.vinst[v] : 0;
+    const int bo = batched ? c.inst_boff[inst] : 0;
+    const int kk = batched ? c.inst_k[inst] : c.k;
+    const int from = c.part[v] - bo;
+    const int wv = c.w_v[v];
+    for (int b = threadIdx.x; b < 32 * W; b += blockDim.x) s_pen[b] = 0;
+    if (threadIdx.x == 0) {
+      s_int = 0;
+      s_border = 0;
+    }
+    __syncthreads();
+    int pen[W];
+#pragma unroll
+    for (int t = 0; t < W; ++t) pen[t] = 0;
+    long long internal = 0;
+    bool border = false;
+    for (int wb0 = 32 * B * wid; wb0 < d; wb0 += 32 * B * nw) {
+      uint32_t wd[B][W];
+      int we[B], lam[B];
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        const int j = wb0 + 32 * u + lane;
+#pragma unroll
+        for (int t = 0; t < W; ++t) wd[u][t] = 0;
+        we[u] = 0;
+        lam[u] = 0;
+        if (j < d) {
+          const int64_t e = c.inets[o0 + j];
+          const int w = UNIT ? 1 : __ldg(&c.w_e[e]);
+          const uint32_t* rec = c.conn + e * W2;
+          load_words<W>(rec, wd[u]);
+          const uint32_t l1 = __ldg(rec + W + (from >> 5));
+          internal += ((l1 >> (from & 31)) & 1u) ? 0 : w;  // Φ(e, from) > 1
+          we[u] = w;
+#pragma unroll
+          for (int t = 0; t < W; ++t) lam[u] += __popc(wd[u][t]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        if (wb0 + 32 * u >= d) break;  // warp-uniform
+        border = border || __ballot_sync(FULLMASK, lam[u] > 1) != 0;
+        if constexpr (UNIT) {
+#pragma unroll
+          for (int t = 0; t < W; ++t) pen[t] += __popc(transpose32(wd[u][t]));
+        } else {
+          const int np = 32 - __clz(__reduce_or_sync(FULLMASK, (unsigned)we[u]));
+          const Planes wp = make_planes(we[u], np);
+#pragma unroll
+          for (int t = 0; t < W; ++t) pen[t] += plane_sum(wp, transpose32(wd[u][t]), we[u]);
+        }
+      }
+    }
+    internal = warp_sum(internal);
+    if (lane == 0 && internal) atomicAdd(&s_int, (ull)internal);
+    if (lane == 0 && border) s_border = 1;
+#pragma unroll
+    for (int t = 0; t < W; ++t)
+      if (pen[t]) atomicAdd(&s_pen[32 * t + lane], pen[t]);
+    __syncthreads();
+    if (wid == 0) {
+      int to = from, gain = 0;
+      const bool bd = s_border != 0;
+      if (bd) {
+        int p[W], slack[W];
+#pragma unroll
+        for (int t = 0; t < W; ++t) {
+          const int b = 32 * t + lane;
+          p[t] = s_pen[b];
+          int sl = -1;
+          if (b < kk) {
+            const int64_t x = c.lmax[bo + b] - c.bw[bo + b];
+            sl = x < 0 ? -1 : (x > INT_MAX ? INT_MAX : (int)x);
+          }
+          slack[t] = sl;
+        }
+        decide<W, UNIT>(kk, from, wv, (int)s_int, zero_gain, p, slack, c.bw + bo, c.perfect + bo, to, gain);
+      }
+      if (lane == 0) {
+        if (query) {
+          dbg_to[v] = to;
+          if (dbg_gain) dbg_gain[v] = gain;
+          if (dbg_border) dbg_border[v] = bd;
+        } else {
+          int2 r = make_int2(-1, 0);
+          if (to != from) {
+            r = make_int2(to + bo, gain);
+            atomicAdd(reinterpret_cast<ull*>(&c.in_w[to + bo]), (ull)(int64_t)wv);
+            atomicAdd(reinterpret_cast<ull*>(&c.in_cnt[to + bo]), 1ull);
+            atomicAdd(reinterpret_cast<ull*>(&c.cand_out[from + bo]), (ull)(int64_t)wv);
+            ++cands;
+          }
+          c.rec[pos] = r;
+        }
+      }
+    }
+    __syncthreads();  // s_pen is cleared for the next vertex
+  }
+  if (!query && threadIdx.x == 0 && cands)
+    atomicAdd(reinterpret_cast<ull*>(&c.stats[(int64_t)round * kStats + kStCands]), (ull)cands);
+  if (last_cta(&c.scal[kDone])) {
+    if (threadIdx.x == 0) c.scal[kHeavyCount] = 0;
+    if (!query) plan_to(c);
+  }
 }
 
 #define LPGPU_DISPATCH_W(W, ...)          \
@@ -783,20 +1128,24 @@ static int occupancy(const void* kern, int threads, size_t smem) {
   return blocks;
 }
 
-static size_t sweep_smem(int k) {
-  return sizeof(int64_t) * 4 * k + sizeof(int) * k + sizeof(unsigned) * k + 32 * (kSweepThreads / 32);
+static size_t sweep_smem(int k, int W, bool batched) {
+  const size_t fm = (W <= 4 && !batched) ? sizeof(uint32_t) * kLvWeights * W : 0;
+  return sizeof(int64_t) * 4 * k + sizeof(int) * k + sizeof(unsigned) * k + fm + 32 * (kSweepThreads / 32);
 }
 
 static cudaError_t launch_sweep(const Launch& L, const RoundCtx& c, int round, int sub,
                                 int32_t* to, int32_t* gain, uint8_t* border) {
   if (word_class(c.W) != c.W) return cudaErrorInvalidValue;
-  const size_t smem = sweep_smem(c.batched ? 0 : c.k);
+  const size_t smem = sweep_smem(c.batched ? 0 : c.k, c.W, c.batched != 0);
   LPGPU_DISPATCH_W(c.W, {
     auto kern = c.unit_nets ? k_sweep<kW, true> : k_sweep<kW, false>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int per_sm = occupancy((const void*)kern, kSweepThreads, smem);
     kern<<<grid_for(L, c.n * 4, kSweepThreads, per_sm), kSweepThreads, smem, L.st>>>(c, round, sub, to, gain, border);
     LAUNCHED("k_sweep");
+    auto heavy = c.unit_nets ? k_sweep_heavy<kW, true> : k_sweep_heavy<kW, false>;
+    heavy<<<grid_for(L, c.n, kSweepThreads, 2), kSweepThreads, 0, L.st>>>(c, round, to, gain, border);
+    LAUNCHED("k_sweep_heavy");
   });
   return cudaSuccess;
 }
@@ -804,6 +1153,8 @@ static cudaError_t launch_sweep(const Launch& L, const RoundCtx& c, int round, i
 cudaError_t launch_best_moves(const Launch& L, const RoundCtx& c, int32_t* to, int32_t* gain,
                               uint8_t* border) {
   if (c.n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(c.scal + kHeavyCount, 0, sizeof(int64_t), L.st);
+  if (e != cudaSuccess) return e;
   return launch_sweep(L, c, 0, 0, to, gain, border);
 }
 

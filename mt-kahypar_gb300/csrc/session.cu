@@ -85,6 +85,7 @@ struct lpgpu_session_s {
   int64_t n = 0, m = 0, P = 0;
   int64_t total_vw = 0;
   bool unit_nets = true;
+  int32_t max_we = 0;
   DevBuf<int64_t> net_off, vtx_off;
   DevBuf<int32_t> pins, inets, w_v, w_e;
   // partition
@@ -95,7 +96,7 @@ struct lpgpu_session_s {
   DevBuf<int64_t> bw, lmax, perfect;
   std::vector<int64_t> h_perfect;
   // refine scratch
-  DevBuf<int32_t> list, net_epoch, seg_w;
+  DevBuf<int32_t> list, net_epoch, seg_w, heavy;
   DevBuf<int64_t> sub_off, blk64, scal, stats, tile_cnt, tile_off, scan_tmp;
   DevBuf<uint8_t> next_flag, status, over;
   DevBuf<int2> rec;
@@ -137,6 +138,7 @@ struct lpgpu_session_s {
     c.w_v = w_v.p;
     c.w_e = w_e.p;
     c.unit_nets = unit_nets ? 1 : 0;
+    c.max_we = max_we;
     c.part = part.p;
     c.phi = phi.p;
     c.conn = conn.p;
@@ -178,6 +180,7 @@ struct lpgpu_session_s {
     }
     c.seg_key = seg_key.p;
     c.seg_w = seg_w.p;
+    c.heavy = heavy.p;
     c.scal = scal.p;
     c.stats = stats.p;
     if (cfg) {
@@ -209,7 +212,7 @@ struct lpgpu_session_s {
     release_partition();
     DevBuf<int64_t>* b64[] = {&net_off, &vtx_off, &sub_off, &stats, &tile_cnt, &tile_off, &scan_tmp};
     for (auto* b : b64) b->release(&footprint);
-    DevBuf<int32_t>* b32[] = {&pins, &inets, &w_v, &w_e, &list, &net_epoch, &seg_w};
+    DevBuf<int32_t>* b32[] = {&pins, &inets, &w_v, &w_e, &list, &net_epoch, &seg_w, &heavy};
     for (auto* b : b32) b->release(&footprint);
     next_flag.release(&footprint);
     saved_part.release(&footprint);
@@ -346,7 +349,9 @@ lpgpu_status lpgpu_session_create(int32_t device, lpgpu_session** out) {
     return cuda_fail(e, "cudaStreamCreate");
   }
   s->timer.st = s->st;
-  if ((e = s->scal.alloc(kScalars, &s->footprint)) != cudaSuccess) {
+  if ((e = s->scal.alloc(kScalars, &s->footprint)) != cudaSuccess ||
+      (e = cudaMemset(s->scal.p, 0, sizeof(int64_t) * kScalars)) != cudaSuccess) {
+    s->scal.release(&s->footprint);
     cudaStreamDestroy(s->st);
     delete s;
     return cuda_fail(e, "alloc scalars");
@@ -388,8 +393,14 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const in
   s->P = net_off[m];
   s->total_vw = total;
   s->unit_nets = true;
-  if (w_e)
-    for (int64_t e = 0; e < m && s->unit_nets; ++e) s->unit_nets = w_e[e] == 1;
+  s->max_we = m > 0 ? 1 : 0;
+  if (w_e) {
+    s->max_we = 0;
+    for (int64_t e = 0; e < m; ++e) {
+      s->unit_nets = s->unit_nets && w_e[e] == 1;
+      s->max_we = std::max(s->max_we, w_e[e]);
+    }
+  }
   int64_t* fp = &s->footprint;
   const int64_t P = s->P;
   CK(s->net_off.alloc(m + 1, fp));
@@ -405,6 +416,7 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const in
   CK(s->rec.alloc(n, fp));
   CK(s->seg_key.alloc(n, fp));
   CK(s->seg_w.alloc(n, fp));
+  CK(s->heavy.alloc(n, fp));
   CK(s->sub_off.alloc(kMaxSubrounds + 1, fp));
   const int64_t tiles = tiles_for(n);
   CK(s->tile_cnt.alloc(kMaxSubrounds * tiles, fp));
@@ -989,7 +1001,7 @@ int64_t lpgpu_estimate_footprint(int64_t n, int64_t m, int64_t P, int32_t k, int
   const int64_t tiles = tiles_for(n);
   int64_t b = 0;
   b += 8 * (m + 1) + 8 * (n + 1) + 4 * P * 2 + 4 * n + 4 * m;          // CSR + weights
-  b += 4 * m + 4 * n + n + n + 8 * n + 8 * n + 4 * n;                  // epoch, list, flags, status, rec, seg
+  b += 4 * m + 4 * n + n + n + 8 * n + 8 * n + 4 * n + 4 * n;          // epoch, list, flags, status, rec, seg, heavy
   b += 8 * (kMaxSubrounds + 1) + 2 * 8 * kMaxSubrounds * tiles;        // sub-round bins
   b += 8 * (scan_tmp_elems(std::max(n + 1, kMaxSubrounds * tiles)) + 1);
   b += 4 * n + 4 * m * (int64_t)k + 8 * m * W;                         // part, Φ, Λ + Λ1

@@ -277,12 +277,25 @@ def served_request(seed, idx, lo=1024, hi=2097152, ks=(2, 4, 8, 16, 32, 64), eps
     return Instance(f"served[{idx}]", hg, k, eps, part, rounds)
 
 
-def random_small(seed, n=200, m=240, k=4, max_size=8, weighted=True, eps=0.03, rounds=5) -> Instance:
-    """Small random hypergraph for property tests (includes degree-0 vertices)."""
+def random_small(seed, n=200, m=240, k=4, max_size=8, weighted=True, eps=0.03, rounds=5, hubs=0,
+                 hub_frac=0.2, vw_hi=5) -> Instance:
+    """Small random hypergraph for property tests (includes degree-0 vertices).
+
+    `hubs` > 0 sends a fraction `hub_frac` of the pins to `hubs` high-degree
+    vertices (ids spaced n / hubs apart); vertex weights are drawn from
+    [1, vw_hi)."""
     rng = np.random.default_rng([seed, 51])
     sizes = rng.integers(2, max_size + 1, size=m)
-    net_off, pins = _build_csr(n, sizes, lambda ids, r: r.integers(0, n, size=len(ids)), rng, 2)
-    w_v = rng.integers(1, 5, size=n).astype(np.int32) if weighted else np.ones(n, np.int32)
+
+    def pick(ids, r):
+        x = r.integers(0, n, size=len(ids))
+        if hubs:
+            h = r.random(len(ids)) < hub_frac
+            x[h] = r.integers(0, hubs, size=int(h.sum())) * (n // hubs)
+        return x
+
+    net_off, pins = _build_csr(n, sizes, pick, rng, 2)
+    w_v = rng.integers(1, vw_hi, size=n).astype(np.int32) if weighted else np.ones(n, np.int32)
     w_e = rng.integers(1, 9, size=m).astype(np.int32) if weighted else np.ones(m, np.int32)
     hg = Hypergraph(n, m, net_off, pins, w_v, w_e).with_incidence()
     part = random_balanced_partition(n, k, rng)

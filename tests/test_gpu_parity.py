@@ -150,6 +150,29 @@ def test_random_state_and_best_moves(lp, orc, seed, k):
     s.close()
 
 
+@pytest.mark.parametrize("seed", range(3))
+@pytest.mark.parametrize("k", [2, 5, 32, 64, 100, 128, 129])
+@pytest.mark.parametrize("weighted", [False, True])
+def test_hub_vertices_and_heavy_weights(lp, orc, seed, k, weighted):
+    """Tiles that mix light vertices (lane-per-vertex counters) with hub vertices
+    of degree > 100 (warp windows), and vertex weights above 16 (feasibility
+    computed per lane instead of from the precomputed masks)."""
+    from lpgpu import gen
+    inst = gen.random_small(seed, n=500, m=600, k=k, max_size=10, weighted=weighted, hubs=5, vw_hi=40)
+    hg, part = inst.hg, inst.part
+    deg = np.diff(hg.vtx_off)
+    assert deg.max() > 100
+    s = session(lp, hg, k, part, lmax=inst.lmax, perfect=inst.perfect)
+    to, gain, border = s.best_moves()
+    eto, egain, eborder = orc.best_moves(hg, k, part, inst.lmax)
+    assert np.array_equal(to, eto) and np.array_equal(gain, egain) and np.array_equal(border, eborder)
+    s.close()
+    for mode in (LP_MODES[1], LP_MODES[3]):
+        out = run_both(lp, orc, inst, 4, mode)
+        assert_same_run(*out, orc, inst)
+        out[0].close()
+
+
 LP_MODES = [
     dict(subrounds=1, revert=0, rollback=0, rebalancing=1),
     dict(subrounds=1, revert=1, rollback=1, rebalancing=1),
