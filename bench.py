@@ -56,7 +56,7 @@ def parse_args():
     ap.add_argument("--rate", type=float, default=2000.0, help="served: Poisson arrival rate (req/s)")
     ap.add_argument("--slots", type=int, default=2, help="served: concurrent batched sessions")
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--subrounds", type=int, default=16)
+    ap.add_argument("--subrounds", type=int, default=8)
     ap.add_argument("--no-baseline", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     return ap.parse_args()

@@ -59,6 +59,21 @@ enum Scalar : int {
   kScalars = 16
 };
 
+using ull = unsigned long long;
+
+// Result words of the device-side input checks (validate.cu): the first
+// failure code, the largest net weight, whether some net weight is not 1,
+// then I per-instance sums of |e|·w(e) and I per-instance vertex weights.
+enum ValidateWord : int { kVErr = 0, kVMaxWe = 1, kVNonUnit = 2, kVSums = 4 };
+enum ValidateCode : int {
+  kVOk = 0,
+  kVBadOffsets = 1,
+  kVNegNetWeight = 2,
+  kVPinRange = 3,
+  kVNegVertexWeight = 4,
+  kVBlockRange = 5
+};
+
 // Per-round statistics slots (lpgpu_round_stats order).
 enum Stat : int { kStActive = 0, kStPins, kStCands, kStMoved, kStReverted, kStDelta, kStats = 8 };
 
@@ -155,6 +170,17 @@ cudaError_t launch_gain_cache(const Launch& L, const RoundCtx& c, int32_t* benef
                               int32_t* penalty);
 cudaError_t launch_apply_moves(const Launch& L, const RoundCtx& c, int64_t count,
                                const int32_t* v, const int32_t* from, const int32_t* to);
+
+// Device-side input checks (validate.cu). `out` holds kVSums + 2 I words;
+// `inst_voff`, `inst_noff`, `vinst` are used (and vinst written) when I > 1.
+cudaError_t launch_validate_csr(const Launch& L, int64_t n, int64_t m, int64_t P, const int64_t* net_off,
+                                const int32_t* pins, const int32_t* w_v, const int32_t* w_e, int I,
+                                const int64_t* inst_voff, const int64_t* inst_noff, int32_t* vinst,
+                                int64_t* out);
+// Checks the partition ids in `part` (device) against k, or per instance when
+// `vinst` is given, and turns local ids into global ones.
+cudaError_t launch_check_partition(const Launch& L, int64_t n, int32_t* part, int k, const int32_t* vinst,
+                                   const int32_t* inst_boff, const int32_t* inst_k, int64_t* out);
 
 // Round phases (the sub-round pipeline). `timer` may be null.
 struct PhaseTimer;

@@ -12,7 +12,6 @@ namespace lpgpu {
 
 #define FULLMASK 0xffffffffu
 
-using ull = unsigned long long;
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }

@@ -110,7 +110,8 @@ struct lpgpu_session_s {
   std::vector<int64_t> h_inst_voff, h_inst_noff, h_inst_weight;
   std::vector<int32_t> h_inst_boff, h_inst_k;
   DevBuf<int32_t> vinst, inst_boff, inst_k, over_ids;
-  DevBuf<int64_t> inst_voff, inst_delta;
+  DevBuf<int64_t> inst_voff, inst_noff, inst_delta;
+  DevBuf<int64_t> vout;  // verdict words of the device-side input checks
   // results of the last refine
   std::vector<lpgpu_round_stats> last_stats;
   // timing
@@ -218,6 +219,8 @@ struct lpgpu_session_s {
     saved_part.release(&footprint);
     vinst.release(&footprint);
     inst_voff.release(&footprint);
+    inst_noff.release(&footprint);
+    vout.release(&footprint);
     status.release(&footprint);
     rec.release(&footprint);
     seg_key.release(&footprint);
@@ -244,53 +247,25 @@ struct DeviceGuard {
 
 int64_t tiles_for(int64_t n) { return std::max<int64_t>(1, (n + 1023) / 1024); }
 
-// Checks the CSR before upload. With instance ranges (batched sessions), every
-// net's pins must lie in its instance's vertex range, and the int32 bounds of
-// the reference's Gain / HypernodeWeight types apply per instance.
-lpgpu_status validate_csr(int64_t n, int64_t m, const int64_t* net_off, const int32_t* pins,
-                          const int32_t* w_v, const int32_t* w_e, int64_t* total_vw,
-                          int32_t num_inst = 1, const int64_t* inst_voff = nullptr,
-                          const int64_t* inst_noff = nullptr) {
+// Structural checks of the upload arguments on the host (O(instances)); the
+// per-net, per-pin and per-vertex checks run on the device after the copy
+// (launch_validate_csr) and are reported by upload_impl.
+lpgpu_status check_shape(int64_t n, int64_t m, const int64_t* net_off, const int32_t* pins, int32_t num_inst,
+                         const int64_t* inst_voff, const int64_t* inst_noff) {
   if (n < 0 || m < 0) return invalid("negative vertex or net count");
   if (n > INT32_MAX || m > INT32_MAX) return invalid("vertex and net ids must fit int32");
   if (!net_off || (m > 0 && net_off[m] > 0 && !pins)) return invalid("null CSR pointer");
   if (net_off[0] != 0) return invalid("net_offsets[0] must be 0");
-  const int64_t one_v[2] = {0, n}, one_n[2] = {0, m};
-  if (!inst_voff) {
-    inst_voff = one_v;
-    inst_noff = one_n;
-    num_inst = 1;
-  }
-  int64_t tw_all = 0;
-  for (int32_t i = 0; i < num_inst; ++i) {
-    const int64_t v0 = inst_voff[i], v1 = inst_voff[i + 1], e0 = inst_noff[i], e1 = inst_noff[i + 1];
-    if (v0 < 0 || v1 < v0 || v1 > n || e0 < 0 || e1 < e0 || e1 > m)
-      return invalid("instance offsets must be non-decreasing and within the union");
-    int64_t gain_bound = 0;
-    for (int64_t e = e0; e < e1; ++e) {
-      const int64_t sz = net_off[e + 1] - net_off[e];
-      if (sz < 0) return invalid("net_offsets must be non-decreasing");
-      if (w_e && w_e[e] < 0) return invalid("net weights must be >= 0");
-      gain_bound += sz * (w_e ? (int64_t)w_e[e] : 1);
-      for (int64_t q = net_off[e]; q < net_off[e + 1]; ++q)
-        if (pins[q] < v0 || pins[q] >= v1)
-          return invalid(num_inst > 1 ? "pin id outside its instance's vertex range" : "pin id out of range");
+  if (net_off[m] < 0) return invalid("net_offsets must be non-decreasing");
+  if (inst_voff) {
+    for (int32_t i = 0; i < num_inst; ++i) {
+      const int64_t v0 = inst_voff[i], v1 = inst_voff[i + 1], e0 = inst_noff[i], e1 = inst_noff[i + 1];
+      if (v0 < 0 || v1 < v0 || v1 > n || e0 < 0 || e1 < e0 || e1 > m)
+        return invalid("instance offsets must be non-decreasing and within the union");
     }
-    if (gain_bound > INT32_MAX)
-      return invalid("sum of |e| * w(e) exceeds int32: gains would overflow the reference's Gain type");
-    int64_t tw = 0;
-    for (int64_t v = v0; v < v1; ++v) {
-      const int64_t w = w_v ? w_v[v] : 1;
-      if (w < 0) return invalid("vertex weights must be >= 0");
-      tw += w;
-    }
-    if (tw > INT32_MAX)
-      return invalid("total vertex weight exceeds int32 (the reference's HypernodeWeight)");
-    tw_all += tw;
+    if (inst_voff[0] != 0 || inst_voff[num_inst] != n || inst_noff[0] != 0 || inst_noff[num_inst] != m)
+      return invalid("instance offsets must cover the union exactly");
   }
-  if (inst_voff[0] != 0 || inst_voff[num_inst] != n || inst_noff[0] != 0 || inst_noff[num_inst] != m)
-    return invalid("instance offsets must cover the union exactly");
-  *total_vw = tw_all;
   return LPGPU_OK;
 }
 
@@ -380,8 +355,7 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const in
                                 const int32_t* pins, const int32_t* w_v, const int32_t* w_e,
                                 int32_t num_inst, const int64_t* inst_voff, const int64_t* inst_noff) {
   if (!s) return invalid("null session");
-  int64_t total = 0;
-  lpgpu_status vs = validate_csr(n, m, net_off, pins, w_v, w_e, &total, num_inst, inst_voff, inst_noff);
+  lpgpu_status vs = check_shape(n, m, net_off, pins, num_inst, inst_voff, inst_noff);
   if (vs != LPGPU_OK) return vs;
   DeviceGuard g(s->device);
   CK(cudaStreamSynchronize(s->st));
@@ -391,16 +365,7 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const in
   s->n = n;
   s->m = m;
   s->P = net_off[m];
-  s->total_vw = total;
-  s->unit_nets = true;
-  s->max_we = m > 0 ? 1 : 0;
-  if (w_e) {
-    s->max_we = 0;
-    for (int64_t e = 0; e < m; ++e) {
-      s->unit_nets = s->unit_nets && w_e[e] == 1;
-      s->max_we = std::max(s->max_we, w_e[e]);
-    }
-  }
+  const int32_t I = inst_voff ? num_inst : 1;
   int64_t* fp = &s->footprint;
   const int64_t P = s->P;
   CK(s->net_off.alloc(m + 1, fp));
@@ -417,6 +382,7 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const in
   CK(s->seg_key.alloc(n, fp));
   CK(s->seg_w.alloc(n, fp));
   CK(s->heavy.alloc(n, fp));
+  CK(s->vout.alloc(kVSums + 2 * (int64_t)I, fp));
   CK(s->sub_off.alloc(kMaxSubrounds + 1, fp));
   const int64_t tiles = tiles_for(n);
   CK(s->tile_cnt.alloc(kMaxSubrounds * tiles, fp));
@@ -448,30 +414,52 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const in
   }
   // instance ranges of a batched session
   s->batched = inst_voff != nullptr;
-  s->num_inst = s->batched ? num_inst : 1;
+  s->num_inst = I;
   s->h_inst_voff.assign(2, 0);
   s->h_inst_noff.assign(2, 0);
   s->h_inst_voff[1] = n;
   s->h_inst_noff[1] = m;
-  s->h_inst_weight.assign(1, total);
   if (s->batched) {
-    s->h_inst_voff.assign(inst_voff, inst_voff + num_inst + 1);
-    s->h_inst_noff.assign(inst_noff, inst_noff + num_inst + 1);
-    s->h_inst_weight.assign(num_inst, 0);
-    for (int32_t i = 0; i < num_inst; ++i)
-      for (int64_t v = inst_voff[i]; v < inst_voff[i + 1]; ++v) s->h_inst_weight[i] += w_v ? w_v[v] : 1;
-    std::vector<int32_t> vi(n);
-    for (int32_t i = 0; i < num_inst; ++i)
-      for (int64_t v = inst_voff[i]; v < inst_voff[i + 1]; ++v) vi[v] = i;
+    s->h_inst_voff.assign(inst_voff, inst_voff + I + 1);
+    s->h_inst_noff.assign(inst_noff, inst_noff + I + 1);
     CK(s->vinst.alloc(n, fp));
-    CK(s->inst_voff.alloc(num_inst + 1, fp));
-    if (n > 0) CK(cudaMemcpyAsync(s->vinst.p, vi.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(s->inst_voff.p, inst_voff, sizeof(int64_t) * (num_inst + 1), cudaMemcpyHostToDevice, st));
-    CK(cudaStreamSynchronize(st));
+    CK(s->inst_voff.alloc(I + 1, fp));
+    CK(s->inst_noff.alloc(I + 1, fp));
+    CK(cudaMemcpyAsync(s->inst_voff.p, inst_voff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->inst_noff.p, inst_noff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
   } else {
     s->vinst.release(fp);
     s->inst_voff.release(fp);
+    s->inst_noff.release(fp);
   }
+  // device-side checks; one copy back of the verdict and the per-instance sums
+  CK(launch_validate_csr(s->launch(), n, m, P, s->net_off.p, s->pins.p, s->w_v.p, s->w_e.p, I,
+                         s->inst_voff.p, s->inst_noff.p, s->vinst.p, s->vout.p));
+  std::vector<int64_t> h(kVSums + 2 * (size_t)I);
+  CK(cudaMemcpyAsync(h.data(), s->vout.p, sizeof(int64_t) * h.size(), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  switch (h[kVErr]) {
+    case kVOk: break;
+    case kVBadOffsets: return invalid("net_offsets must be non-decreasing and within the pin array");
+    case kVNegNetWeight: return invalid("net weights must be >= 0");
+    case kVPinRange:
+      return invalid(I > 1 ? "pin id outside its instance's vertex range" : "pin id out of range");
+    case kVNegVertexWeight: return invalid("vertex weights must be >= 0");
+    default: return invalid("invalid hypergraph");
+  }
+  s->h_inst_weight.assign(I, 0);
+  int64_t total = 0;
+  for (int32_t i = 0; i < I; ++i) {
+    if (h[kVSums + i] > INT32_MAX)
+      return invalid("sum of |e| * w(e) exceeds int32: gains would overflow the reference's Gain type");
+    const int64_t tw = h[kVSums + I + i];
+    if (tw > INT32_MAX) return invalid("total vertex weight exceeds int32 (the reference's HypernodeWeight)");
+    s->h_inst_weight[i] = tw;
+    total += tw;
+  }
+  s->total_vw = total;
+  s->max_we = (int32_t)h[kVMaxWe];
+  s->unit_nets = h[kVNonUnit] == 0;
   CK(launch_build_incidence(s->launch(), n, m, s->net_off.p, s->pins.p, s->vtx_off.p, s->inets.p,
                             reinterpret_cast<int64_t*>(s->seg_key.p), s->scan_tmp.p, s->scan_tmp_n));
   CK(cudaStreamSynchronize(st));
@@ -496,16 +484,18 @@ lpgpu_status lpgpu_session_upload_batch(lpgpu_session* s, int32_t num_instances,
 }
 
 // Allocates the partition state for K global blocks (Φ rows of kmax entries)
-// and builds it from `gpart` (global block ids).
-static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax, const int32_t* gpart,
+// and builds it from `part` (host): block ids in [0, K) for one instance, or
+// local ids per instance for a batch (turned into global ids on the device).
+static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax, const int32_t* part,
                                        const std::vector<int64_t>& hl, const std::vector<int64_t>& hp) {
   DeviceGuard g(s->device);
   CK(cudaStreamSynchronize(s->st));
-  s->release_partition();
+  s->has_part = false;
   s->k = K;
   s->kmax = kmax;
   s->W = word_class_of(kmax);
   int64_t* fp = &s->footprint;
+  // same-size buffers are kept from the previous partition
   CK(s->part.alloc(s->n, fp));
   CK(s->phi.alloc((size_t)s->m * kmax, fp));
   CK(s->conn.alloc((size_t)s->m * 2 * s->W, fp));
@@ -525,9 +515,15 @@ static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax
     CK(cudaMemcpyAsync(s->inst_k.p, s->h_inst_k.data(), sizeof(int32_t) * s->num_inst, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(s->inst_delta.p, 0, sizeof(int64_t) * s->num_inst, st));
   }
-  if (s->n > 0) CK(cudaMemcpyAsync(s->part.p, gpart, sizeof(int32_t) * s->n, cudaMemcpyHostToDevice, st));
+  if (s->n > 0) CK(cudaMemcpyAsync(s->part.p, part, sizeof(int32_t) * s->n, cudaMemcpyHostToDevice, st));
+  CK(launch_check_partition(s->launch(), s->n, s->part.p, K, s->batched ? s->vinst.p : nullptr,
+                            s->inst_boff.p, s->inst_k.p, s->vout.p));
+  int64_t verdict = 0;
+  CK(cudaMemcpyAsync(&verdict, s->vout.p + kVErr, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(s->lmax.p, hl.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(s->perfect.p, hp.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));
+  if (verdict != kVOk) return invalid("block id out of range");
   CK(cudaMemsetAsync(s->blk64.p, 0, sizeof(int64_t) * (7 * (size_t)K + 1), st));
   RoundCtx c = s->ctx();
   CK(launch_init_partition(s->launch(), c));
@@ -556,16 +552,10 @@ lpgpu_status lpgpu_session_set_partition_batch(lpgpu_session* s, const int32_t* 
     kmax = std::max(kmax, instance_k[i]);
   }
   if (K > INT32_MAX / 8) return invalid("too many blocks in one batch");
-  std::vector<int32_t> gpart(s->n);
   std::vector<int64_t> hl(K), hp(K);
   for (int32_t i = 0; i < I; ++i) {
-    int64_t tw = 0;
-    for (int64_t v = s->h_inst_voff[i]; v < s->h_inst_voff[i + 1]; ++v) {
-      if (partition[v] < 0 || partition[v] >= instance_k[i]) return invalid("block id out of range");
-      gpart[v] = partition[v] + boff[i];
-    }
     // total weight of the instance for Context::setupPartWeights (context.cpp:237-250)
-    tw = s->h_inst_weight[i];
+    const int64_t tw = s->h_inst_weight[i];
     const int64_t perfect = std::max<int64_t>(1, (int64_t)std::ceil((double)tw / (double)instance_k[i]));
     const int64_t lmax = (int64_t)((1.0 + instance_eps[i]) * (double)perfect);
     for (int32_t b = 0; b < instance_k[i]; ++b) {
@@ -575,7 +565,7 @@ lpgpu_status lpgpu_session_set_partition_batch(lpgpu_session* s, const int32_t* 
   }
   s->h_inst_boff = boff;
   s->h_inst_k.assign(instance_k, instance_k + I);
-  return set_partition_impl(s, (int32_t)K, kmax, gpart.data(), hl, hp);
+  return set_partition_impl(s, (int32_t)K, kmax, partition, hl, hp);
 }
 
 lpgpu_status lpgpu_session_set_partition(lpgpu_session* s, int32_t k, double eps,
@@ -592,8 +582,6 @@ lpgpu_status lpgpu_session_set_partition(lpgpu_session* s, int32_t k, double eps
   }
   if (k < 1 || k > LPGPU_MAX_K) return invalid("k must be in [1, 1024]");
   if (s->n > 0 && !partition) return invalid("null partition");
-  for (int64_t v = 0; v < s->n; ++v)
-    if (partition[v] < 0 || partition[v] >= k) return invalid("block id out of range");
   std::vector<int64_t> hp(k), hl(k);
   // Context::setupPartWeights (context.cpp:237-250)
   const int64_t perfect = (int64_t)std::ceil((double)s->total_vw / (double)k);

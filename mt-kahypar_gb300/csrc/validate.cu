@@ -1,0 +1,175 @@
+// Input checks of lpgpu_session_upload / _upload_batch and
+// lpgpu_session_set_partition(_batch), run on the device over the copied
+// buffers so that the host does no per-pin or per-vertex work.
+//
+// Every check sets the first failure code in out[kVErr]; the per-instance
+// sums the int32 bounds need (Σ_e |e|·w(e), the Gain bound, and Σ_v w(v),
+// the HypernodeWeight bound) are accumulated in out[kVSums + ...] and checked
+// by the host after one copy back.
+#include "common.cuh"
+
+namespace lpgpu {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ void fail(int64_t* out, int code) {
+  atomicCAS(reinterpret_cast<ull*>(&out[kVErr]), 0ull, (ull)code);
+}
+
+// Instance of element x given the instance start offsets off[0..I].
+__device__ __forceinline__ int find_instance(const int64_t* __restrict__ off, int I, int64_t x) {
+  int lo = 0, hi = I - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Warp per net: offsets inside [0, P] and non-decreasing, w(e) >= 0, every
+// pin inside its instance's vertex range; Σ |e|·w(e) per instance, the
+// largest net weight and whether some weight differs from 1.
+__global__ void k_check_nets(int64_t m, int64_t P, const int64_t* __restrict__ net_off,
+                             const int32_t* __restrict__ pins, const int32_t* __restrict__ w_e, int I,
+                             const int64_t* __restrict__ inst_voff, const int64_t* __restrict__ inst_noff,
+                             int64_t n, int64_t* out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int64_t gsum = 0;
+  int cur = -1;  // instance whose sum is held in gsum
+  int maxw = 0, nonunit = 0;
+  for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < m; e += warps) {
+    const int64_t a = net_off[e], b = net_off[e + 1];
+    if (a < 0 || b < a || b > P) {
+      if (lane == 0) fail(out, kVBadOffsets);
+      continue;
+    }
+    const int we = w_e ? w_e[e] : 1;
+    if (we < 0) {
+      if (lane == 0) fail(out, kVNegNetWeight);
+      continue;
+    }
+    maxw = max(maxw, we);
+    nonunit |= we != 1;
+    int inst = 0;
+    int64_t v0 = 0, v1 = n;
+    if (I > 1) {
+      inst = find_instance(inst_noff, I, e);
+      v0 = inst_voff[inst];
+      v1 = inst_voff[inst + 1];
+    }
+    bool bad = false;
+    for (int64_t q = a + lane; q < b; q += 32) {
+      const int32_t p = pins[q];
+      bad |= p < v0 || p >= v1;
+    }
+    if (__any_sync(FULL, bad) && lane == 0) fail(out, kVPinRange);
+    if (lane == 0) {
+      if (inst != cur) {
+        if (cur >= 0 && gsum) atomicAdd(reinterpret_cast<ull*>(&out[kVSums + cur]), (ull)gsum);
+        cur = inst;
+        gsum = 0;
+      }
+      gsum += (b - a) * (int64_t)we;
+    }
+  }
+  if (lane == 0 && cur >= 0 && gsum) atomicAdd(reinterpret_cast<ull*>(&out[kVSums + cur]), (ull)gsum);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    maxw = max(maxw, __shfl_xor_sync(FULL, maxw, o));
+    nonunit |= __shfl_xor_sync(FULL, nonunit, o);
+  }
+  if (lane == 0) {
+    if (maxw) atomicMax(reinterpret_cast<unsigned long long*>(&out[kVMaxWe]), (ull)maxw);
+    if (nonunit) atomicOr(reinterpret_cast<ull*>(&out[kVNonUnit]), 1ull);
+  }
+}
+
+// Thread per vertex: w(v) >= 0, the vertex's instance (batched), Σ w(v) per
+// instance (warp sums when the warp's vertices share an instance).
+__global__ void k_check_vertices(int64_t n, const int32_t* __restrict__ w_v, int I,
+                                 const int64_t* __restrict__ inst_voff, int32_t* __restrict__ vinst,
+                                 int64_t* out) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < n;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t v = base + lane;
+    const bool ok = v < n;
+    int64_t w = 0;
+    int inst = 0;
+    if (ok) {
+      w = w_v ? w_v[v] : 1;
+      if (w < 0) fail(out, kVNegVertexWeight);
+      if (I > 1) {
+        inst = find_instance(inst_voff, I, v);
+        vinst[v] = inst;
+      }
+    }
+    const int i0 = __shfl_sync(FULL, inst, 0);
+    if (__all_sync(FULL, !ok || inst == i0)) {
+      int64_t s = w;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+      if (lane == 0 && s) atomicAdd(reinterpret_cast<ull*>(&out[kVSums + I + i0]), (ull)s);
+    } else if (ok && w) {
+      atomicAdd(reinterpret_cast<ull*>(&out[kVSums + I + inst]), (ull)w);
+    }
+  }
+}
+
+// Partition ids: local id p of vertex v must lie in [0, k of v's instance);
+// the stored id is the global block boff(instance) + p.
+__global__ void k_check_partition(int64_t n, int32_t* __restrict__ part, int k, const int32_t* __restrict__ vinst,
+                                  const int32_t* __restrict__ inst_boff, const int32_t* __restrict__ inst_k,
+                                  int64_t* out) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t p = part[v];
+    if (vinst) {
+      const int i = vinst[v];
+      if (p < 0 || p >= inst_k[i]) {
+        fail(out, kVBlockRange);
+        part[v] = 0;  // keeps later indexing in range; the call fails anyway
+      } else {
+        part[v] = p + inst_boff[i];
+      }
+    } else if (p < 0 || p >= k) {
+      fail(out, kVBlockRange);
+      part[v] = 0;
+    }
+  }
+}
+
+int grid(const Launch& L, int64_t items, int threads) {
+  const int64_t need = (items + threads - 1) / threads;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)L.num_sms * 8));
+}
+
+}  // namespace
+
+cudaError_t launch_validate_csr(const Launch& L, int64_t n, int64_t m, int64_t P, const int64_t* net_off,
+                                const int32_t* pins, const int32_t* w_v, const int32_t* w_e, int I,
+                                const int64_t* inst_voff, const int64_t* inst_noff, int32_t* vinst,
+                                int64_t* out) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(int64_t) * (kVSums + 2 * (int64_t)I), L.st);
+  if (e != cudaSuccess) return e;
+  if (m > 0) k_check_nets<<<grid(L, m * 32, 256), 256, 0, L.st>>>(m, P, net_off, pins, w_e, I, inst_voff,
+                                                                    inst_noff, n, out);
+  if (n > 0) k_check_vertices<<<grid(L, n, 256), 256, 0, L.st>>>(n, w_v, I, inst_voff, vinst, out);
+  add_kernel_launches((m > 0) + (n > 0));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_check_partition(const Launch& L, int64_t n, int32_t* part, int k, const int32_t* vinst,
+                                   const int32_t* inst_boff, const int32_t* inst_k, int64_t* out) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(int64_t) * kVSums, L.st);
+  if (e != cudaSuccess) return e;
+  if (n > 0) {
+    k_check_partition<<<grid(L, n, 256), 256, 0, L.st>>>(n, part, k, vinst, inst_boff, inst_k, out);
+    add_kernel_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace lpgpu

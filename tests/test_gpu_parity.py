@@ -283,6 +283,54 @@ def test_invalid_arguments_are_rejected(lp):
     s.close()
 
 
+def test_device_side_input_checks(lp, orc):
+    """Per-pin / per-net / per-vertex checks run on the device after the copy;
+    each failure is reported as INVALID_ARG and leaves the session usable."""
+    from lpgpu import gen
+    H = gen.Hypergraph
+    ones = lambda k: np.ones(k, np.int32)  # noqa: E731
+    cases = [
+        ("offsets", H(4, 2, np.array([0, 3, 2], np.int64), np.array([0, 1, 2], np.int32), ones(4), ones(2))),
+        ("net weight", H(4, 1, np.array([0, 2], np.int64), np.array([0, 1], np.int32), ones(4),
+                         np.array([-1], np.int32))),
+        ("vertex weight", H(4, 1, np.array([0, 2], np.int64), np.array([0, 1], np.int32),
+                            np.array([1, -2, 1, 1], np.int32), ones(1))),
+        ("pin", H(4, 1, np.array([0, 2], np.int64), np.array([0, -1], np.int32), ones(4), ones(1))),
+        ("gain bound", H(4, 1, np.array([0, 3], np.int64), np.array([0, 1, 2], np.int32), ones(4),
+                         np.array([10 ** 9], np.int32))),
+        ("total weight", H(3, 1, np.array([0, 2], np.int64), np.array([0, 1], np.int32),
+                           np.array([1_500_000_000, 1_500_000_000, 1], np.int32), ones(1))),
+    ]
+    ok = gen.random_small(3, n=300, m=360, k=4)
+    with lp.Session(0) as s:
+        for name, hg in cases:
+            with pytest.raises(lp.LpgpuError) as e:
+                s.upload(hg)
+            assert e.value.status == lp.ERR_INVALID_ARG, name
+            with pytest.raises(lp.LpgpuError) as e:
+                s.set_partition(2, np.zeros(hg.n, np.int32))
+            assert e.value.status == lp.ERR_STATE, name
+        s.upload(ok.hg)
+        bad = ok.part.copy()
+        bad[123] = 4
+        with pytest.raises(lp.LpgpuError) as e:
+            s.set_partition(4, bad)
+        assert e.value.status == lp.ERR_INVALID_ARG
+        s.set_partition(4, ok.part, lmax=ok.lmax, perfect=ok.perfect)
+        check_state(orc, s, ok.hg, 4, ok.part)
+    # batch: a local block id above its instance's k
+    insts = [gen.random_small(10 + i, n=100, m=120, k=3) for i in range(3)]
+    with lp.Session(0) as s:
+        s.upload_batch([x.hg for x in insts])
+        parts = [x.part.copy() for x in insts]
+        parts[1][7] = 3
+        with pytest.raises(lp.LpgpuError) as e:
+            s.set_partition_batch([3, 3, 3], parts)
+        assert e.value.status == lp.ERR_INVALID_ARG
+        s.set_partition_batch([3, 3, 3], [x.part for x in insts])
+        assert s.instance_km1().shape == (3,)
+
+
 def test_one_shot_entry_point(lp, orc):
     from lpgpu import gen
     inst = gen.plain_small(seed=2)
