@@ -56,6 +56,7 @@ enum Scalar : int {
   kDone = 9,       // arrival counter of the last-CTA pattern
   kOverCount = 10, // number of overflowing target blocks
   kHeavyCount = 11, // vertices the sweep deferred to the heavy-vertex kernel
+  kRevCount = 12,  // moves marked for revert in the current sub-round
   kScalars = 16
 };
 
@@ -135,6 +136,7 @@ struct RoundCtx {
   int64_t* inst_delta;      // per-instance summed delta of the current sub-round
   int32_t* over_ids;        // target blocks that overflow (count in scal[kOverCount])
   int32_t* heavy;           // list positions deferred by the sweep (count in scal[kHeavyCount])
+  int32_t* revl;            // list positions of moves marked for revert (count in scal[kRevCount])
 };
 
 // Global block offset of vertex v's instance.
@@ -191,7 +193,10 @@ cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int
                               int64_t* tile_cnt, int64_t* tile_off, int64_t* scan_tmp,
                               int64_t scan_tmp_elems, PhaseTimer* timer);
 cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int sub, PhaseTimer* timer);
-cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, PhaseTimer* timer);
+// End of a round that has a successor: activation of the kept moves
+// (moveVertex, label_propagation_refiner.h:112-128) and expansion of the
+// stamped nets into the next round's active set.
+cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, int S, PhaseTimer* timer);
 
 // Optional per-phase CUDA-event timing.
 struct PhaseTimer {

@@ -1555,6 +1555,7 @@ __device__ void plan_to(const RoundCtx& c) {
     c.scal[kAnyOverFrom] = s_any_from;
     c.scal[kDeltaSub] = 0;
     c.scal[kDeltaRb] = 0;
+    c.scal[kRevCount] = 0;
   }
 }
 
@@ -1594,55 +1595,70 @@ __global__ void k_bin_moves(RoundCtx c, int sub) {
 }
 
 // Gain-sorted prefix without sorting, by one CTA: radix selection (8 bits per
-// pass, most significant differing byte first) of the first key whose
-// inclusive weighted prefix exceeds `budget`; keys below it are accepted.
-// Bytes shared by all keys are skipped, each warp keeps a private 256-bin
-// histogram (32-bit: vertex weights total at most INT32_MAX), and one warp
-// scans the bins. Returns the threshold to every thread.
+// pass, most significant byte first) of the first key whose inclusive
+// weighted prefix exceeds `budget`; keys below it are accepted. Bytes equal in
+// all keys need no pass (bitwise AND == OR). Segments of up to kSelStage keys
+// are staged in shared memory once; each warp keeps a private 256-bin
+// histogram (32-bit: vertex weights total at most INT32_MAX) and the whole CTA
+// folds them before one warp scans the bins. Returns the threshold to every
+// thread.
 constexpr int kSelThreads = 512;
+constexpr int kSelStage = 12288;  // keys (8 B) + weights (4 B) staged in shared memory
+constexpr size_t kSelSmem = (size_t)kSelStage * 12;
 
-__device__ uint64_t cta_radix_select(const uint64_t* __restrict__ keys, const int32_t* __restrict__ ws,
+__device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const int32_t* __restrict__ gws,
                                      int64_t cnt, int64_t budget0) {
   constexpr int NW = kSelThreads / 32;
+  extern __shared__ __align__(16) unsigned char sel_smem[];
   __shared__ unsigned hist[NW][256];
-  __shared__ uint64_t s_min[NW], s_max[NW];
+  __shared__ unsigned tot[256];
+  __shared__ uint64_t s_and[NW], s_or[NW];
   __shared__ int64_t s_budget;
   __shared__ int s_sel;
-  __shared__ int64_t s_below;
   const int lane = lane_id(), wid = threadIdx.x >> 5;
-  uint64_t mn = ~0ull, mx = 0;
+  const bool staged = cnt <= kSelStage;
+  uint64_t* skeys = reinterpret_cast<uint64_t*>(sel_smem);
+  int32_t* sws = reinterpret_cast<int32_t*>(skeys + kSelStage);
+  uint64_t ka = ~0ull, ko = 0;
   for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
-    const uint64_t key = keys[i];
-    mn = key < mn ? key : mn;
-    mx = key > mx ? key : mx;
+    const uint64_t key = gkeys[i];
+    if (staged) {
+      skeys[i] = key;
+      sws[i] = gws[i];
+    }
+    ka &= key;
+    ko |= key;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    const uint64_t a = __shfl_xor_sync(FULLMASK, mn, o), z = __shfl_xor_sync(FULLMASK, mx, o);
-    mn = a < mn ? a : mn;
-    mx = z > mx ? z : mx;
+    ka &= __shfl_xor_sync(FULLMASK, ka, o);
+    ko |= __shfl_xor_sync(FULLMASK, ko, o);
   }
   __syncthreads();
-  if (lane == 0) { s_min[wid] = mn; s_max[wid] = mx; }
+  if (lane == 0) { s_and[wid] = ka; s_or[wid] = ko; }
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int w = 1; w < NW; ++w) {
-      mn = s_min[w] < mn ? s_min[w] : mn;
-      mx = s_max[w] > mx ? s_max[w] : mx;
+      ka &= s_and[w];
+      ko |= s_or[w];
     }
-    s_min[0] = mn;
-    s_max[0] = mx;
+    s_and[0] = ka;
+    s_or[0] = ko;
     s_budget = budget0;
   }
   __syncthreads();
-  mn = s_min[0];
-  mx = s_max[0];
-  const uint64_t diff = mn ^ mx;
-  const int top = diff ? (63 - __clzll((long long)diff)) >> 3 : 0;  // highest differing byte
-  uint64_t mask = top == 7 ? 0ull : ~((1ull << (8 * (top + 1))) - 1);
-  uint64_t prefix = mn & mask;
-  for (int byte = top; byte >= 0; --byte) {
+  ka = s_and[0];
+  ko = s_or[0];
+  const uint64_t* keys = staged ? skeys : gkeys;
+  const int32_t* ws = staged ? sws : gws;
+  uint64_t prefix = 0, mask = 0;
+  for (int byte = 7; byte >= 0; --byte) {
     const int shift = 8 * byte;
+    if ((((ka ^ ko) >> shift) & 255) == 0) {  // every key has this byte
+      prefix |= ka & (255ull << shift);
+      mask |= 255ull << shift;
+      continue;
+    }
     for (int i = threadIdx.x; i < NW * 256; i += blockDim.x) (&hist[0][0])[i] = 0;
     __syncthreads();
     for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
@@ -1650,15 +1666,20 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ keys, const in
       if ((key & mask) == prefix) atomicAdd(&hist[wid][(key >> shift) & 255], (unsigned)ws[i]);
     }
     __syncthreads();
+    for (int bin = threadIdx.x; bin < 256; bin += blockDim.x) {
+      unsigned t = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) t += hist[w][bin];
+      tot[bin] = t;
+    }
+    __syncthreads();
     if (wid == 0) {
       // lane l owns bins 8l .. 8l+7: first bin whose running sum exceeds the budget
       int64_t h[8], sum = 0;
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        int64_t t = 0;
-        for (int w = 0; w < NW; ++w) t += hist[w][8 * lane + j];
-        h[j] = t;
-        sum += t;
+        h[j] = tot[8 * lane + j];
+        sum += h[j];
       }
       int64_t run = sum;
 #pragma unroll
@@ -1678,15 +1699,12 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ keys, const in
       const int first = found ? __ffs(found) - 1 : 31;
       if (lane == first) {
         s_sel = found ? sel : 255;
-        s_below = found ? below : acc;
+        s_budget = budget - (found ? below : acc);
       }
     }
     __syncthreads();
     prefix |= (uint64_t)s_sel << shift;
     mask |= 255ull << shift;
-    __syncthreads();
-    if (threadIdx.x == 0) s_budget -= s_below;
-    __syncthreads();
   }
   return prefix;
 }
@@ -1893,8 +1911,8 @@ constexpr int kPackThreads = 256;
 // per-move weight check: the selection already guarantees both bounds).
 // Marks status[pos] = 1 for committed moves and overwrites rec[pos].y with
 // the source block (the gain is no longer needed). With `last`, the moves
-// are final: they are activated (moveVertex, label_propagation_refiner.h:112-128)
-// and the sub-round is closed.
+// are final and the sub-round is closed; kept moves are activated at the end
+// of the round (k_activate_round).
 __global__ void __launch_bounds__(kPackThreads, 4) k_commit(RoundCtx c, int round, int sub, int last) {
   extern __shared__ ull s_dw[];
   __shared__ unsigned char s_own[kPackThreads];
@@ -1905,7 +1923,6 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_commit(RoundCtx c, int roun
   __syncthreads();
   const int lane = lane_id();
   unsigned char* own = s_own + (threadIdx.x & ~31);
-  const int epoch = (int)c.scal[kEpoch];
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
   int64_t att = 0, moved = 0;
   const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
@@ -1937,19 +1954,12 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_commit(RoundCtx c, int roun
       const int bow = __shfl_sync(FULLMASK, bo, ow);
       const int fo = __shfl_sync(FULLMASK, f, ow) - bow;   // local blocks
       const int to = __shfl_sync(FULLMASK, r.x, ow) - bow;
-      int a = 0;
-      if (has) {
-        const int64_t e = c.inets[j];
-        a = commit_incidence(c, e, fo, to);
-        if (last) activate_incidence(c, e, epoch);
-      }
-      return a;
+      return has ? commit_incidence(c, c.inets[j], fo, to) : 0;
     });
     if (acc) {
       att += tot;
       if (c.batched) atomicAdd(reinterpret_cast<ull*>(&c.inst_delta[c.vinst[v]]), (ull)(int64_t)tot);
       c.part[v] = r.x;
-      if (last) c.next_flag[v] = 1;
       const int64_t wv = c.w_v[v];
       atomicAdd(&dw[r.x], (ull)wv);
       atomicAdd(&dw[f], (ull)(-wv));
@@ -2009,18 +2019,64 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_revert_eval(RoundCtx c, int
       }
       return x;
     });
-    if (moved && score < 0) c.status[pos] = 2;
+    const bool rev = moved && score < 0;
+    if (rev) c.status[pos] = 2;
+    const unsigned rm = __ballot_sync(FULLMASK, rev);
+    if (rm) {
+      const int leader = __ffs(rm) - 1;
+      ull base = 0;
+      if (lane == leader) base = atomicAdd(reinterpret_cast<ull*>(&c.scal[kRevCount]), (ull)__popc(rm));
+      base = __shfl_sync(FULLMASK, base, leader);
+      if (rev) c.revl[base + __popc(rm & lanemask_lt())] = (int32_t)pos;
+    }
   }
 }
 
-// mode 0: undo of the moves marked 2 by the hindsight check; mode 1
-// (rollback): when the sub-round's delta is positive, undo of all moves still
-// marked 1 (status 3). With `last`, the moves that stay are activated and the
-// sub-round is closed.
-__global__ void __launch_bounds__(kPackThreads, 4) k_undo(RoundCtx c, int round, int sub, int rollback, int last) {
-  // rollback: the sub-round's delta decides (per instance when batched);
-  // kDeltaSub and inst_delta are not written in rollback mode
-  const bool roll = rollback && (c.batched || c.scal[kDeltaSub] > 0);
+// Undo of one tile of moves (lane = move): Φ / Λ / Λ1 back from t to f,
+// part and block weights restored. Returns the summed attributed delta.
+__device__ __forceinline__ int64_t undo_tile(const RoundCtx& c, bool sel, int64_t v, int2 r, int bo,
+                                             unsigned char* own, ull* dw, bool inst_delta) {
+  int64_t o0 = 0;
+  int deg = 0;
+  if (sel) {
+    o0 = c.vtx_off[v];
+    deg = (int)(c.vtx_off[v + 1] - o0);
+  }
+  const int tot = packed_incidences(sel, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
+    const int bow = __shfl_sync(FULLMASK, bo, ow);
+    const int t = __shfl_sync(FULLMASK, r.x, ow) - bow;
+    const int f = __shfl_sync(FULLMASK, r.y, ow) - bow;
+    return has ? commit_incidence(c, c.inets[j], t, f) : 0;
+  });
+  if (!sel) return 0;
+  if (inst_delta) atomicAdd(reinterpret_cast<ull*>(&c.inst_delta[c.vinst[v]]), (ull)(int64_t)tot);
+  c.part[v] = r.y;
+  const int64_t wv = c.w_v[v];
+  atomicAdd(&dw[r.y], (ull)wv);
+  atomicAdd(&dw[r.x], (ull)(-wv));
+  return tot;
+}
+
+// Books undone moves into the sub-round's delta and statistics and flushes
+// the CTA's block-weight deltas.
+__device__ __forceinline__ void undo_epilogue(const RoundCtx& c, int round, int64_t att, int64_t undone,
+                                              int slot, ull* s_dw, int kdw) {
+  att = block_sum_i64(att);
+  undone = block_sum_i64(undone);
+  if (threadIdx.x == 0 && undone) {
+    atomicAdd(reinterpret_cast<ull*>(&c.scal[slot]), (ull)att);
+    int64_t* stt = c.stats + (int64_t)round * kStats;
+    atomicAdd(reinterpret_cast<ull*>(&stt[kStMoved]), (ull)(-undone));
+    atomicAdd(reinterpret_cast<ull*>(&stt[kStReverted]), (ull)undone);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < kdw; b += blockDim.x)
+    if (s_dw[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_dw[b]);
+}
+
+// Undo of the moves the hindsight check marked (status 2), from the compact
+// list k_revert_eval wrote. With `last` the sub-round is closed.
+__global__ void __launch_bounds__(kPackThreads, 4) k_undo_reverts(RoundCtx c, int round, int last) {
   extern __shared__ ull s_dw[];
   __shared__ unsigned char s_own[kPackThreads];
   ull* dw = c.batched ? reinterpret_cast<ull*>(c.bw) : s_dw;
@@ -2029,74 +2085,102 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_undo(RoundCtx c, int round,
   __syncthreads();
   const int lane = lane_id();
   unsigned char* own = s_own + (threadIdx.x & ~31);
-  const int epoch = (int)c.scal[kEpoch];
-  const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
-  const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
+  const int64_t cnt = c.scal[kRevCount];
+  // spread the moves over all warps (few per warp): their incidence chains
+  // then run side by side instead of one after another inside a warp
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t want = (cnt + nwarps - 1) / nwarps;
+  const int per = want < 1 ? 1 : (want > 32 ? 32 : (int)want);
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int64_t att = 0, undone = 0;
-  if (!rollback || roll || last) {
-    for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
-         base += stride) {
-      const int64_t pos = base + lane;
-      const uint8_t st = pos < end ? c.status[pos] : 0;
-      int64_t v = 0;
-      int bo = 0;
-      bool inst_roll = roll;
-      if (st == 1 || st == 2) {
-        v = c.list[pos];
-        if (c.batched) {
-          const int i = c.vinst[v];
-          bo = c.inst_boff[i];
-          inst_roll = rollback && c.inst_delta[i] > 0;  // rollback is decided per instance
-        }
-      }
-      const bool sel = rollback ? (inst_roll && st == 1) : st == 2;
-      const bool keep = last && st == 1 && !sel;
-      int2 r = make_int2(0, 0);  // (to, from), global blocks
-      int64_t o0 = 0;
-      int deg = 0;
-      if (sel || keep) {
-        r = c.rec[pos];
-        o0 = c.vtx_off[v];
-        deg = (int)(c.vtx_off[v + 1] - o0);
-      }
-      const int tot = packed_incidences(sel, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
-        const int bow = __shfl_sync(FULLMASK, bo, ow);
-        const int t = __shfl_sync(FULLMASK, r.x, ow) - bow;
-        const int f = __shfl_sync(FULLMASK, r.y, ow) - bow;
-        return has ? commit_incidence(c, c.inets[j], t, f) : 0;
-      });
-      if (sel) {
-        att += tot;
-        if (c.batched && !rollback)
-          atomicAdd(reinterpret_cast<ull*>(&c.inst_delta[c.vinst[v]]), (ull)(int64_t)tot);
-        c.part[v] = r.y;
-        const int64_t wv = c.w_v[v];
-        atomicAdd(&dw[r.y], (ull)wv);
-        atomicAdd(&dw[r.x], (ull)(-wv));
-        if (rollback) c.status[pos] = 3;
-        ++undone;
-      }
-      if (last) {
-        packed_incidences(keep, o0, deg, own, [&](bool has, int, int64_t j) -> int {
-          if (has) activate_incidence(c, c.inets[j], epoch);
-          return 0;
-        });
-        if (keep) c.next_flag[v] = 1;
+  for (int64_t base = gw * per; base < cnt; base += nwarps * per) {
+    const int64_t i = base + lane;
+    const bool sel = lane < per && i < cnt;
+    int64_t v = 0;
+    int2 r = make_int2(0, 0);  // (to, from), global blocks
+    int bo = 0;
+    if (sel) {
+      const int32_t pos = c.revl[i];
+      v = c.list[pos];
+      r = c.rec[pos];
+      bo = block_offset(c, v);
+    }
+    att += undo_tile(c, sel, v, r, bo, own, dw, c.batched != 0);
+    undone += sel ? 1 : 0;
+  }
+  undo_epilogue(c, round, att, undone, kDeltaSub, s_dw, kdw);
+  if (last && last_cta(&c.scal[kDone])) close_subround(c, round);
+}
+
+// Rollback: when the sub-round's delta is positive, undo of every move still
+// marked 1 (status 3); decided per instance when batched (kDeltaSub and
+// inst_delta are not written here). Closes the sub-round.
+__global__ void __launch_bounds__(kPackThreads, 4) k_rollback(RoundCtx c, int round, int sub) {
+  const bool roll = c.batched || c.scal[kDeltaSub] > 0;
+  extern __shared__ ull s_dw[];
+  __shared__ unsigned char s_own[kPackThreads];
+  ull* dw = c.batched ? reinterpret_cast<ull*>(c.bw) : s_dw;
+  const int kdw = c.batched ? 0 : c.k;
+  for (int b = threadIdx.x; b < kdw; b += blockDim.x) s_dw[b] = 0;
+  __syncthreads();
+  const int lane = lane_id();
+  unsigned char* own = s_own + (threadIdx.x & ~31);
+  const int64_t beg = c.sub_off[sub], end = roll ? c.sub_off[sub + 1] : beg;
+  int64_t att = 0, undone = 0;
+  for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pos = base + lane;
+    const uint8_t st = pos < end ? c.status[pos] : 0;
+    int64_t v = 0;
+    int bo = 0;
+    bool sel = false;
+    if (st == 1) {
+      v = c.list[pos];
+      sel = true;
+      if (c.batched) {
+        const int i = c.vinst[v];
+        bo = c.inst_boff[i];
+        sel = c.inst_delta[i] > 0;  // rollback is decided per instance
       }
     }
+    const int2 r = sel ? c.rec[pos] : make_int2(0, 0);
+    att += undo_tile(c, sel, v, r, bo, own, dw, false);
+    if (sel) {
+      c.status[pos] = 3;
+      ++undone;
+    }
   }
-  att = block_sum_i64(att);
-  undone = block_sum_i64(undone);
-  if (threadIdx.x == 0 && undone) {
-    atomicAdd(reinterpret_cast<ull*>(&c.scal[rollback ? kDeltaRb : kDeltaSub]), (ull)att);
-    int64_t* stt = c.stats + (int64_t)round * kStats;
-    atomicAdd(reinterpret_cast<ull*>(&stt[kStMoved]), (ull)(-undone));
-    atomicAdd(reinterpret_cast<ull*>(&stt[kStReverted]), (ull)undone);
+  undo_epilogue(c, round, att, undone, kDeltaRb, s_dw, kdw);
+  if (last_cta(&c.scal[kDone])) close_subround(c, round);
+}
+
+// Activation of the round's kept moves (status 1): the moved vertex and the
+// pins of its incident nets with |e| <= activation threshold become active in
+// the next round (moveVertex, label_propagation_refiner.h:112-128). Nets are
+// stamped with the round's epoch and expanded by k_expand_nets.
+__global__ void __launch_bounds__(kPackThreads, 4) k_activate_round(RoundCtx c, int S) {
+  __shared__ unsigned char s_own[kPackThreads];
+  const int lane = lane_id();
+  unsigned char* own = s_own + (threadIdx.x & ~31);
+  const int epoch = (int)c.scal[kEpoch];
+  const int64_t end = c.sub_off[S];
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pos = base + lane;
+    const bool keep = pos < end && c.status[pos] == 1;
+    int64_t v = 0, o0 = 0;
+    int deg = 0;
+    if (keep) {
+      v = c.list[pos];
+      o0 = c.vtx_off[v];
+      deg = (int)(c.vtx_off[v + 1] - o0);
+      c.next_flag[v] = 1;
+    }
+    packed_incidences(keep, o0, deg, own, [&](bool has, int, int64_t j) -> int {
+      if (has) activate_incidence(c, c.inets[j], epoch);
+      return 0;
+    });
   }
-  __syncthreads();
-  for (int b = threadIdx.x; b < kdw; b += blockDim.x)
-    if (s_dw[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_dw[b]);
-  if (last && last_cta(&c.scal[kDone])) close_subround(c, round);
 }
 
 // End of a round: the pins of every net stamped with the round's epoch
@@ -2118,7 +2202,13 @@ __global__ void k_expand_nets(RoundCtx c) {
   }
 }
 
-cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, PhaseTimer* timer) {
+cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, int S, PhaseTimer* timer) {
+  {
+    Scope sc(timer, "activate");
+    k_activate_round<<<grid_for(L, c.n, kPackThreads, occupancy((const void*)k_activate_round, kPackThreads, 0)),
+                       kPackThreads, 0, L.st>>>(c, S);
+    LAUNCHED("k_activate_round");
+  }
   if (c.m == 0) return cudaSuccess;
   Scope sc(timer, "expand");
   k_expand_nets<<<grid_for(L, c.m, 256, 4), 256, 0, L.st>>>(c);
@@ -2136,32 +2226,38 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
     if (e != cudaSuccess) return e;
   }
   const int g = grid_for(L, n, 256, 8);
+  // incidence kernels: one wave of resident CTAs striding over the sub-round
+  const int g_commit = grid_for(L, n, kPackThreads, occupancy((const void*)k_commit, kPackThreads, dw_smem));
+  const int g_eval = grid_for(L, n, kPackThreads, occupancy((const void*)k_revert_eval, kPackThreads, 0));
+  const int g_undo = grid_for(L, n, kPackThreads, occupancy((const void*)k_rollback, kPackThreads, dw_smem));
   {
     Scope sc(timer, "select");
     k_bin_moves<<<g, 256, 0, L.st>>>(c, sub);
     LAUNCHED("k_bin_moves");
-    k_select<<<(unsigned)std::min<int64_t>(k, 4 * (int64_t)L.num_sms), kSelThreads, 0, L.st>>>(c);
+    cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
+    cudaFuncSetAttribute(k_from_side, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
+    k_select<<<(unsigned)std::min<int64_t>(k, 4 * (int64_t)L.num_sms), kSelThreads, kSelSmem, L.st>>>(c);
     LAUNCHED("k_select");
-    k_from_side<<<1, kSelThreads, 0, L.st>>>(c, sub);
+    k_from_side<<<1, kSelThreads, kSelSmem, L.st>>>(c, sub);
     LAUNCHED("k_from_side");
   }
   const int last_commit = !c.revert && !c.rollback;
   {
     Scope sc(timer, "commit");
-    k_commit<<<g, 256, dw_smem, L.st>>>(c, round, sub, last_commit);
+    k_commit<<<g_commit, kPackThreads, dw_smem, L.st>>>(c, round, sub, last_commit);
     LAUNCHED("k_commit");
   }
   if (c.revert) {
     Scope sc(timer, "revert");
-    k_revert_eval<<<g, 256, 0, L.st>>>(c, sub);
+    k_revert_eval<<<g_eval, kPackThreads, 0, L.st>>>(c, sub);
     LAUNCHED("k_revert_eval");
-    k_undo<<<g, 256, dw_smem, L.st>>>(c, round, sub, 0, !c.rollback);
-    LAUNCHED("k_undo");
+    k_undo_reverts<<<g_undo, kPackThreads, dw_smem, L.st>>>(c, round, !c.rollback);
+    LAUNCHED("k_undo_reverts");
   }
   if (c.rollback) {
     Scope sc(timer, "rollback");
-    k_undo<<<g, 256, dw_smem, L.st>>>(c, round, sub, 1, 1);
-    LAUNCHED("k_undo");
+    k_rollback<<<g_undo, kPackThreads, dw_smem, L.st>>>(c, round, sub);
+    LAUNCHED("k_rollback");
   }
   return cudaSuccess;
 }

@@ -96,7 +96,7 @@ struct lpgpu_session_s {
   DevBuf<int64_t> bw, lmax, perfect;
   std::vector<int64_t> h_perfect;
   // refine scratch
-  DevBuf<int32_t> list, net_epoch, seg_w, heavy;
+  DevBuf<int32_t> list, net_epoch, seg_w, heavy, revl;
   DevBuf<int64_t> sub_off, blk64, scal, stats, tile_cnt, tile_off, scan_tmp;
   DevBuf<uint8_t> next_flag, status, over;
   DevBuf<int2> rec;
@@ -182,6 +182,7 @@ struct lpgpu_session_s {
     c.seg_key = seg_key.p;
     c.seg_w = seg_w.p;
     c.heavy = heavy.p;
+    c.revl = revl.p;
     c.scal = scal.p;
     c.stats = stats.p;
     if (cfg) {
@@ -213,7 +214,7 @@ struct lpgpu_session_s {
     release_partition();
     DevBuf<int64_t>* b64[] = {&net_off, &vtx_off, &sub_off, &stats, &tile_cnt, &tile_off, &scan_tmp};
     for (auto* b : b64) b->release(&footprint);
-    DevBuf<int32_t>* b32[] = {&pins, &inets, &w_v, &w_e, &list, &net_epoch, &seg_w, &heavy};
+    DevBuf<int32_t>* b32[] = {&pins, &inets, &w_v, &w_e, &list, &net_epoch, &seg_w, &heavy, &revl};
     for (auto* b : b32) b->release(&footprint);
     next_flag.release(&footprint);
     saved_part.release(&footprint);
@@ -382,6 +383,7 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const in
   CK(s->seg_key.alloc(n, fp));
   CK(s->seg_w.alloc(n, fp));
   CK(s->heavy.alloc(n, fp));
+  CK(s->revl.alloc(n, fp));
   CK(s->vout.alloc(kVSums + 2 * (int64_t)I, fp));
   CK(s->sub_off.alloc(kMaxSubrounds + 1, fp));
   const int64_t tiles = tiles_for(n);
@@ -674,7 +676,7 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
         return e;
       for (int sub = 0; sub < S; ++sub)
         if ((e = launch_subround(L, c, r, sub, tm)) != cudaSuccess) return e;
-      if (r + 1 < R && (e = launch_expand_nets(L, c, tm)) != cudaSuccess) return e;
+      if (r + 1 < R && (e = launch_expand_nets(L, c, S, tm)) != cudaSuccess) return e;
     }
     // drop flags left by the last round
     if (s->n > 0 && (e = cudaMemsetAsync(s->next_flag.p, 0, s->n, st)) != cudaSuccess) return e;
@@ -989,7 +991,7 @@ int64_t lpgpu_estimate_footprint(int64_t n, int64_t m, int64_t P, int32_t k, int
   const int64_t tiles = tiles_for(n);
   int64_t b = 0;
   b += 8 * (m + 1) + 8 * (n + 1) + 4 * P * 2 + 4 * n + 4 * m;          // CSR + weights
-  b += 4 * m + 4 * n + n + n + 8 * n + 8 * n + 4 * n + 4 * n;          // epoch, list, flags, status, rec, seg, heavy
+  b += 4 * m + 4 * n + n + n + 8 * n + 8 * n + 4 * n + 8 * n;          // epoch, list, flags, status, rec, seg, queues
   b += 8 * (kMaxSubrounds + 1) + 2 * 8 * kMaxSubrounds * tiles;        // sub-round bins
   b += 8 * (scan_tmp_elems(std::max(n + 1, kMaxSubrounds * tiles)) + 1);
   b += 4 * n + 4 * m * (int64_t)k + 8 * m * W;                         // part, Φ, Λ + Λ1
