@@ -72,6 +72,15 @@ static int grid_for(const Launch& L, int64_t work_items, int threads, int per_sm
   return (int)std::max<int64_t>(1, std::min<int64_t>(cap, need));
 }
 
+// Resident CTAs per SM of `kern` (at least 1).
+static int occupancy(const void* kern, int threads, size_t smem) {
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, threads, smem) != cudaSuccess ||
+      blocks < 1)
+    blocks = 1;
+  return blocks;
+}
+
 // Reports the kernel that failed to launch (and a sticky error left by an
 // earlier call) through the library's error text.
 static thread_local int64_t t_launches = 0;
@@ -223,46 +232,162 @@ __global__ void k_block_weights(RoundCtx c) {
   }
 }
 
-// Φ, Λ and Λ1 (blocks holding exactly one pin of the net) from scratch, warp
-// per net with a per-warp k-bin shared histogram (initializePinCountInPart,
-// h:1086-1110), fused with the km1 / cut sums. Net e's record is
-// conn[e * 2W .. e * 2W + 2W): W words of Λ(e), then W words of Λ1(e).
-__global__ void k_pin_counts(RoundCtx c) {
+// Incidence packing shared by the kernels that walk the incidences of a set
+// of vertices (one per lane). Vertices of degree 1..32 are packed greedily
+// into groups of <= 32 incidences (lane = incidence, contiguous per vertex);
+// longer vertices are walked alone in 32-incidence chunks. For every group
+// `body(has, ow, j, seg_end)` runs on all lanes: lane `has` holds incidence j
+// (index into inets) of the vertex held by lane `ow`. The return value is, on
+// each selected lane, the sum over its vertex's incidences of the ints
+// returned by body (segmented sums inside a group).
+template <typename Body>
+__device__ __forceinline__ int packed_incidences(bool sel, int64_t o0, int deg,
+                                                 unsigned char* __restrict__ s_owner, Body&& body) {
+  const int lane = lane_id();
+  int my_total = 0;
+  const bool small = sel && deg >= 1 && deg <= 32;
+  const int dsm = small ? deg : 0;
+  int incl = dsm;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(FULLMASK, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int excl = incl - dsm;
+  unsigned rem = __ballot_sync(FULLMASK, small);
+  while (rem) {
+    const int q = __ffs(rem) - 1;
+    const int start = __shfl_sync(FULLMASK, excl, q);
+    const bool inpack = ((rem >> lane) & 1u) && incl - start <= 32;
+    const unsigned pmask = __ballot_sync(FULLMASK, inpack);
+    const int D = __shfl_sync(FULLMASK, incl, 31 - __clz(pmask)) - start;
+    const int st = excl - start;
+    __syncwarp();
+    if (inpack) s_owner[__popc(pmask & lanemask_lt())] = (unsigned char)lane;
+    const unsigned starts = __reduce_or_sync(FULLMASK, inpack ? (1u << st) : 0u);
+    __syncwarp();
+    const bool has = lane < D;
+    const int ow = has ? s_owner[__popc(starts & ((2u << lane) - 1u)) - 1] : lane;
+    const int64_t o_ow = __shfl_sync(FULLMASK, o0, ow);
+    const int st_ow = __shfl_sync(FULLMASK, st, ow);
+    const int d_ow = __shfl_sync(FULLMASK, deg, ow);
+    const int seg_end = has ? st_ow + d_ow : lane + 1;
+    int x = body(has, ow, has ? o_ow + lane - st_ow : (int64_t)0);
+    // segmented suffix sums: the first lane of every vertex gets its total
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_down_sync(FULLMASK, x, o);
+      if (lane + o < seg_end) x += y;
+    }
+    const int tot = __shfl_sync(FULLMASK, x, inpack ? st : 0);
+    if (inpack) my_total = tot;
+    rem &= ~pmask;
+  }
+  unsigned bigm = __ballot_sync(FULLMASK, sel && deg > 32);
+  while (bigm) {
+    const int j = __ffs(bigm) - 1;
+    bigm &= bigm - 1;
+    const int64_t oj = __shfl_sync(FULLMASK, o0, j);
+    const int dj = __shfl_sync(FULLMASK, deg, j);
+    int acc = 0;
+    for (int base = 0; base < dj; base += 32) {
+      const bool has = base + lane < dj;
+      acc += body(has, j, has ? oj + base + lane : (int64_t)0);
+    }
+    acc = warp_sum(acc);
+    if (lane == j) my_total = acc;
+  }
+  return my_total;
+}
+
+// Φ, Λ and Λ1 (blocks holding exactly one pin of the net) from scratch
+// (initializePinCountInPart, h:1086-1110), fused with the km1 / cut sums, on
+// zeroed Φ and Λ / Λ1. A warp takes 32 nets. Nets of up to 32 pins are packed
+// into 32-pin groups (lane = pin): lanes with the same (net, block) find each
+// other with a match, and the lowest writes Φ(e, b) and sets the Λ / Λ1 bits;
+// λ(e) is the number of such lanes. Larger nets are counted one at a time in a
+// per-warp shared k-bin histogram. Net e's record is conn[e * 2W .. e * 2W + 2W):
+// W words of Λ(e), then W words of Λ1(e).
+__global__ void __launch_bounds__(256) k_pin_counts(RoundCtx c) {
   extern __shared__ int s_hist[];
+  __shared__ unsigned char s_own[256];
   const int k = c.kmax, W = c.W;
   int* hist = s_hist + (threadIdx.x >> 5) * k;
+  unsigned char* own = s_own + (threadIdx.x & ~31);
   const int lane = lane_id();
   for (int b = lane; b < k; b += 32) hist[b] = 0;
   __syncwarp();
   int64_t km1 = 0, cut = 0;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < c.m; e += warps) {
-    const int64_t b0 = c.net_off[e], b1 = c.net_off[e + 1];
-    const int bo = (c.batched && b1 > b0) ? block_offset(c, c.pins[b0]) : 0;
-    for (int64_t i = b0 + lane; i < b1; i += 32) atomicAdd(&hist[c.part[c.pins[i]] - bo], 1);
-    __syncwarp();
-    int lam = 0;
-    for (int w = 0; w < W; ++w) {
-      const int b = w * 32 + lane;
-      int cnt = 0;
-      if (b < k) {
-        cnt = hist[b];
-        hist[b] = 0;
-        c.phi[e * k + b] = cnt;
-      }
-      const unsigned bits = __ballot_sync(FULLMASK, cnt > 0);
-      const unsigned ones = __ballot_sync(FULLMASK, cnt == 1);
-      if (lane == 0) {
-        c.conn[e * 2 * W + w] = bits;
-        c.conn[e * 2 * W + W + w] = ones;
-      }
-      lam += __popc(bits);
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < c.m;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = base + lane;
+    int64_t b0 = 0;
+    int deg = 0, bo = 0;
+    if (e < c.m) {
+      b0 = c.net_off[e];
+      const int64_t d = c.net_off[e + 1] - b0;
+      deg = d > INT32_MAX ? INT32_MAX : (int)d;
+      if (c.batched && d > 0) bo = block_offset(c, c.pins[b0]);
     }
-    __syncwarp();
-    if (lane == 0) {
+    const bool small = deg >= 1 && deg <= 32;
+    const int lam = packed_incidences(small, b0, deg, own, [&](bool has, int ow, int64_t j) -> int {
+      const int64_t e_ow = __shfl_sync(FULLMASK, e, ow);
+      const int bo_ow = __shfl_sync(FULLMASK, bo, ow);
+      int b = 0;
+      unsigned key = 0x80000000u | (unsigned)lane;  // lanes without a pin match nobody
+      if (has) {
+        b = c.part[c.pins[j]] - bo_ow;
+        key = ((unsigned)ow << 11) | (unsigned)b;
+      }
+      const unsigned peers = __match_any_sync(FULLMASK, key);
+      const bool leader = has && __ffs(peers) - 1 == lane;
+      if (leader) {
+        const int cnt = __popc(peers);
+        c.phi[e_ow * k + b] = cnt;
+        uint32_t* rec = c.conn + e_ow * 2 * W;
+        atomicOr(&rec[b >> 5], 1u << (b & 31));
+        if (cnt == 1) atomicOr(&rec[W + (b >> 5)], 1u << (b & 31));
+      }
+      return leader ? 1 : 0;
+    });
+    if (small) {
       const int64_t we = c.w_e[e];
       km1 += (int64_t)(lam > 1 ? lam - 1 : 0) * we;
       cut += lam > 1 ? we : 0;
+    }
+    unsigned bigm = __ballot_sync(FULLMASK, deg > 32);
+    while (bigm) {
+      const int q = __ffs(bigm) - 1;
+      bigm &= bigm - 1;
+      const int64_t eq = __shfl_sync(FULLMASK, e, q);
+      const int64_t bq = __shfl_sync(FULLMASK, b0, q);
+      const int dq = __shfl_sync(FULLMASK, deg, q);
+      const int boq = __shfl_sync(FULLMASK, bo, q);
+      for (int64_t i = bq + lane; i < bq + dq; i += 32) atomicAdd(&hist[c.part[c.pins[i]] - boq], 1);
+      __syncwarp();
+      int lq = 0;
+      for (int w = 0; w < W; ++w) {
+        const int b = w * 32 + lane;
+        int cnt = 0;
+        if (b < k) {
+          cnt = hist[b];
+          hist[b] = 0;
+          if (cnt) c.phi[eq * k + b] = cnt;
+        }
+        const unsigned bits = __ballot_sync(FULLMASK, cnt > 0);
+        const unsigned ones = __ballot_sync(FULLMASK, cnt == 1);
+        if (lane == 0) {
+          c.conn[eq * 2 * W + w] = bits;
+          c.conn[eq * 2 * W + W + w] = ones;
+        }
+        lq += __popc(bits);
+      }
+      __syncwarp();
+      if (lane == 0) {
+        const int64_t we = c.w_e[eq];
+        km1 += (int64_t)(lq > 1 ? lq - 1 : 0) * we;
+        cut += lq > 1 ? we : 0;
+      }
     }
   }
   km1 = block_sum_i64(km1);
@@ -282,8 +407,10 @@ cudaError_t launch_init_partition(const Launch& L, const RoundCtx& c) {
     LAUNCHED("k_block_weights");
   }
   if (c.m > 0) {
+    if ((e = cudaMemsetAsync(c.phi, 0, sizeof(int32_t) * (size_t)c.m * c.kmax, L.st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(c.conn, 0, sizeof(uint32_t) * (size_t)c.m * 2 * c.W, L.st)) != cudaSuccess) return e;
     const size_t smem = sizeof(int) * c.kmax * 8;
-    k_pin_counts<<<grid_for(L, c.m * 32, 256), 256, smem, L.st>>>(c);
+    k_pin_counts<<<grid_for(L, c.m, 256, occupancy((const void*)k_pin_counts, 256, smem)), 256, smem, L.st>>>(c);
     LAUNCHED("k_pin_counts");
   }
   return cudaSuccess;
@@ -1119,13 +1246,6 @@ static int word_class(int W) {
   return w;
 }
 
-static int occupancy(const void* kern, int threads, size_t smem) {
-  int blocks = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, threads, smem) != cudaSuccess ||
-      blocks < 1)
-    blocks = 1;
-  return blocks;
-}
 
 static size_t sweep_smem(int k, int W, bool batched) {
   const size_t fm = (W <= 4 && !batched) ? sizeof(uint32_t) * kLvWeights * W : 0;
@@ -1661,9 +1781,29 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const i
     }
     for (int i = threadIdx.x; i < NW * 256; i += blockDim.x) (&hist[0][0])[i] = 0;
     __syncthreads();
-    for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
-      const uint64_t key = keys[i];
-      if ((key & mask) == prefix) atomicAdd(&hist[wid][(key >> shift) & 255], (unsigned)ws[i]);
+    if (shift < 32) {  // vertex-id bytes: digits are spread, plain atomics
+      for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+        const uint64_t key = keys[i];
+        if ((key & mask) == prefix) atomicAdd(&hist[wid][(key >> shift) & 255], (unsigned)ws[i]);
+      }
+    } else {
+    // gain bytes: few distinct digits, so lanes with the same digit add once
+    for (int64_t base = threadIdx.x - lane; base < cnt; base += blockDim.x) {
+      const int64_t i = base + lane;
+      uint64_t key = 0;
+      bool in = false;
+      if (i < cnt) {
+        key = keys[i];
+        in = (key & mask) == prefix;
+      }
+      const unsigned act = __ballot_sync(FULLMASK, in);
+      if (in) {
+        const unsigned dig = (unsigned)(key >> shift) & 255u;
+        const unsigned peers = __match_any_sync(act, dig);
+        const unsigned sum = __reduce_add_sync(peers, (unsigned)ws[i]);
+        if (lane == __ffs(peers) - 1) atomicAdd(&hist[wid][dig], sum);
+      }
+    }
     }
     __syncthreads();
     for (int bin = threadIdx.x; bin < 256; bin += blockDim.x) {
@@ -1806,74 +1946,6 @@ __device__ void close_subround(const RoundCtx& c, int round) {
   }
   if (c.batched)
     for (int i = threadIdx.x; i < c.num_inst; i += blockDim.x) c.inst_delta[i] = 0;
-}
-
-// Incidence packing shared by the kernels that walk the incidences of a set
-// of vertices (one per lane). Vertices of degree 1..32 are packed greedily
-// into groups of <= 32 incidences (lane = incidence, contiguous per vertex);
-// longer vertices are walked alone in 32-incidence chunks. For every group
-// `body(has, ow, j, seg_end)` runs on all lanes: lane `has` holds incidence j
-// (index into inets) of the vertex held by lane `ow`. The return value is, on
-// each selected lane, the sum over its vertex's incidences of the ints
-// returned by body (segmented sums inside a group).
-template <typename Body>
-__device__ __forceinline__ int packed_incidences(bool sel, int64_t o0, int deg,
-                                                 unsigned char* __restrict__ s_owner, Body&& body) {
-  const int lane = lane_id();
-  int my_total = 0;
-  const bool small = sel && deg >= 1 && deg <= 32;
-  const int dsm = small ? deg : 0;
-  int incl = dsm;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(FULLMASK, incl, o);
-    if (lane >= o) incl += y;
-  }
-  const int excl = incl - dsm;
-  unsigned rem = __ballot_sync(FULLMASK, small);
-  while (rem) {
-    const int q = __ffs(rem) - 1;
-    const int start = __shfl_sync(FULLMASK, excl, q);
-    const bool inpack = ((rem >> lane) & 1u) && incl - start <= 32;
-    const unsigned pmask = __ballot_sync(FULLMASK, inpack);
-    const int D = __shfl_sync(FULLMASK, incl, 31 - __clz(pmask)) - start;
-    const int st = excl - start;
-    __syncwarp();
-    if (inpack) s_owner[__popc(pmask & lanemask_lt())] = (unsigned char)lane;
-    const unsigned starts = __reduce_or_sync(FULLMASK, inpack ? (1u << st) : 0u);
-    __syncwarp();
-    const bool has = lane < D;
-    const int ow = has ? s_owner[__popc(starts & ((2u << lane) - 1u)) - 1] : lane;
-    const int64_t o_ow = __shfl_sync(FULLMASK, o0, ow);
-    const int st_ow = __shfl_sync(FULLMASK, st, ow);
-    const int d_ow = __shfl_sync(FULLMASK, deg, ow);
-    const int seg_end = has ? st_ow + d_ow : lane + 1;
-    int x = body(has, ow, has ? o_ow + lane - st_ow : (int64_t)0);
-    // segmented suffix sums: the first lane of every vertex gets its total
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_down_sync(FULLMASK, x, o);
-      if (lane + o < seg_end) x += y;
-    }
-    const int tot = __shfl_sync(FULLMASK, x, inpack ? st : 0);
-    if (inpack) my_total = tot;
-    rem &= ~pmask;
-  }
-  unsigned bigm = __ballot_sync(FULLMASK, sel && deg > 32);
-  while (bigm) {
-    const int j = __ffs(bigm) - 1;
-    bigm &= bigm - 1;
-    const int64_t oj = __shfl_sync(FULLMASK, o0, j);
-    const int dj = __shfl_sync(FULLMASK, deg, j);
-    int acc = 0;
-    for (int base = 0; base < dj; base += 32) {
-      const bool has = base + lane < dj;
-      acc += body(has, j, has ? oj + base + lane : (int64_t)0);
-    }
-    acc = warp_sum(acc);
-    if (lane == j) my_total = acc;
-  }
-  return my_total;
 }
 
 // One incidence of a move from f to t: atomic decrement of Φ(e,f) and
@@ -2184,21 +2256,27 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_activate_round(RoundCtx c, 
 }
 
 // End of a round: the pins of every net stamped with the round's epoch
-// become active for the next round.
-__global__ void k_expand_nets(RoundCtx c) {
+// become active for the next round. A warp takes 32 nets and walks the pins
+// of the stamped ones in packed 32-pin groups.
+__global__ void __launch_bounds__(256) k_expand_nets(RoundCtx c) {
+  __shared__ unsigned char s_own[256];
   const int epoch = (int)c.scal[kEpoch];
   const int lane = lane_id();
+  unsigned char* own = s_own + (threadIdx.x & ~31);
   for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < c.m;
        base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t e = base + lane;
     const bool hit = e < c.m && c.net_epoch[e] == epoch;
-    unsigned mask = __ballot_sync(FULLMASK, hit);
-    while (mask) {
-      const int j = __ffs(mask) - 1;
-      mask &= mask - 1;
-      const int64_t ej = base + j;
-      for (int64_t p = c.net_off[ej] + lane; p < c.net_off[ej + 1]; p += 32) c.next_flag[c.pins[p]] = 1;
+    int64_t o0 = 0;
+    int deg = 0;
+    if (hit) {
+      o0 = c.net_off[e];
+      deg = (int)(c.net_off[e + 1] - o0);  // stamped nets have at most the activation threshold of pins
     }
+    packed_incidences(hit, o0, deg, own, [&](bool has, int, int64_t j) -> int {
+      if (has) c.next_flag[c.pins[j]] = 1;
+      return 0;
+    });
   }
 }
 
@@ -2211,7 +2289,7 @@ cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, int S, PhaseT
   }
   if (c.m == 0) return cudaSuccess;
   Scope sc(timer, "expand");
-  k_expand_nets<<<grid_for(L, c.m, 256, 4), 256, 0, L.st>>>(c);
+  k_expand_nets<<<grid_for(L, c.m, 256, occupancy((const void*)k_expand_nets, 256, 0)), 256, 0, L.st>>>(c);
   LAUNCHED("k_expand_nets");
   return cudaSuccess;
 }
@@ -2230,9 +2308,10 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
   const int g_commit = grid_for(L, n, kPackThreads, occupancy((const void*)k_commit, kPackThreads, dw_smem));
   const int g_eval = grid_for(L, n, kPackThreads, occupancy((const void*)k_revert_eval, kPackThreads, 0));
   const int g_undo = grid_for(L, n, kPackThreads, occupancy((const void*)k_rollback, kPackThreads, dw_smem));
+  const int g_bin = grid_for(L, n, 256, occupancy((const void*)k_bin_moves, 256, 0));
   {
     Scope sc(timer, "select");
-    k_bin_moves<<<g, 256, 0, L.st>>>(c, sub);
+    k_bin_moves<<<g_bin, 256, 0, L.st>>>(c, sub);
     LAUNCHED("k_bin_moves");
     cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
     cudaFuncSetAttribute(k_from_side, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
