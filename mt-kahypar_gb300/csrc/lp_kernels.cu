@@ -1723,8 +1723,46 @@ __global__ void k_bin_moves(RoundCtx c, int sub) {
 // folds them before one warp scans the bins. Returns the threshold to every
 // thread.
 constexpr int kSelThreads = 512;
-constexpr int kSelStage = 12288;  // keys (8 B) + weights (4 B) staged in shared memory
+constexpr int kSelStage = 16384;  // keys (8 B) + weights (4 B) staged in shared memory
 constexpr size_t kSelSmem = (size_t)kSelStage * 12;
+
+// One histogram pass: the weights of the keys matching `prefix` under `mask`,
+// binned by the byte at `shift`, into this warp's 256 bins. Trips are
+// warp-uniform; U keys per lane are loaded before any is binned. On gain
+// bytes (few distinct digits) lanes with the same digit add once.
+template <int U>
+__device__ __forceinline__ void sel_hist(const uint64_t* __restrict__ keys, const int32_t* __restrict__ ws,
+                                         int64_t cnt, uint64_t mask, uint64_t prefix, int shift,
+                                         unsigned* __restrict__ h) {
+  const int lane = lane_id();
+  const bool agg = shift >= 32;
+  for (int64_t base = threadIdx.x - lane; base < cnt; base += (int64_t)U * blockDim.x) {
+    uint64_t kv[U];
+    int32_t wv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + (int64_t)u * blockDim.x + lane;
+      kv[u] = i < cnt ? keys[i] : ~prefix;
+      wv[u] = i < cnt ? ws[i] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + (int64_t)u * blockDim.x + lane;
+      const bool in = i < cnt && (kv[u] & mask) == prefix;
+      const unsigned dig = (unsigned)(kv[u] >> shift) & 255u;
+      if (agg) {
+        const unsigned act = __ballot_sync(FULLMASK, in);
+        if (in) {
+          const unsigned peers = __match_any_sync(act, dig);
+          const unsigned sum = __reduce_add_sync(peers, (unsigned)wv[u]);
+          if (lane == __ffs(peers) - 1) atomicAdd(&h[dig], sum);
+        }
+      } else if (in) {
+        atomicAdd(&h[dig], (unsigned)wv[u]);
+      }
+    }
+  }
+}
 
 __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const int32_t* __restrict__ gws,
                                      int64_t cnt, int64_t budget0) {
@@ -1740,6 +1778,7 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const i
   uint64_t* skeys = reinterpret_cast<uint64_t*>(sel_smem);
   int32_t* sws = reinterpret_cast<int32_t*>(skeys + kSelStage);
   uint64_t ka = ~0ull, ko = 0;
+#pragma unroll 4
   for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
     const uint64_t key = gkeys[i];
     if (staged) {
@@ -1769,8 +1808,6 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const i
   __syncthreads();
   ka = s_and[0];
   ko = s_or[0];
-  const uint64_t* keys = staged ? skeys : gkeys;
-  const int32_t* ws = staged ? sws : gws;
   uint64_t prefix = 0, mask = 0;
   for (int byte = 7; byte >= 0; --byte) {
     const int shift = 8 * byte;
@@ -1781,30 +1818,10 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const i
     }
     for (int i = threadIdx.x; i < NW * 256; i += blockDim.x) (&hist[0][0])[i] = 0;
     __syncthreads();
-    if (shift < 32) {  // vertex-id bytes: digits are spread, plain atomics
-      for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
-        const uint64_t key = keys[i];
-        if ((key & mask) == prefix) atomicAdd(&hist[wid][(key >> shift) & 255], (unsigned)ws[i]);
-      }
-    } else {
-    // gain bytes: few distinct digits, so lanes with the same digit add once
-    for (int64_t base = threadIdx.x - lane; base < cnt; base += blockDim.x) {
-      const int64_t i = base + lane;
-      uint64_t key = 0;
-      bool in = false;
-      if (i < cnt) {
-        key = keys[i];
-        in = (key & mask) == prefix;
-      }
-      const unsigned act = __ballot_sync(FULLMASK, in);
-      if (in) {
-        const unsigned dig = (unsigned)(key >> shift) & 255u;
-        const unsigned peers = __match_any_sync(act, dig);
-        const unsigned sum = __reduce_add_sync(peers, (unsigned)ws[i]);
-        if (lane == __ffs(peers) - 1) atomicAdd(&hist[wid][dig], sum);
-      }
-    }
-    }
+    if (staged)
+      sel_hist<1>(skeys, sws, cnt, mask, prefix, shift, hist[wid]);
+    else
+      sel_hist<8>(gkeys, gws, cnt, mask, prefix, shift, hist[wid]);
     __syncthreads();
     for (int bin = threadIdx.x; bin < 256; bin += blockDim.x) {
       unsigned t = 0;
