@@ -279,7 +279,7 @@ void lpgpu_config_default(lpgpu_config* cfg) {
   cfg->rounds = 5;
   cfg->activation_threshold = 100;
   cfg->rebalancing = 1;
-  cfg->subrounds = 16;
+  cfg->subrounds = 8;
   cfg->revert = 1;
   cfg->rollback = 1;
   cfg->flags = 0;
