@@ -365,6 +365,30 @@ def e2e_leg(args, inst, cfg, device, dist):
             "path": "lpgpu_session_upload + set_partition + refine + get_partition from pinned host buffers"}
 
 
+def pinned_instances(lpgpu, gen, insts):
+    """Copies every instance's CSR, weights and start partition into views of a
+    few page-locked arenas (host buffers as a caller would pin them), plus
+    page-locked output partitions."""
+    def arena(arrays, dtype):
+        a = lpgpu.PinnedArray((max(1, sum(len(x) for x in arrays)),), dtype)
+        views, o = [], 0
+        for x in arrays:
+            v = a.array[o:o + len(x)]
+            v[...] = x
+            views.append(v)
+            o += len(x)
+        return a, views
+    hs = [x.hg for x in insts]
+    a_off, offs = arena([h.net_off for h in hs], np.int64)
+    a_pin, pins = arena([h.pins for h in hs], np.int32)
+    a_wv, wvs = arena([h.w_v for h in hs], np.int32)
+    a_we, wes = arena([h.w_e for h in hs], np.int32)
+    a_pt, parts = arena([x.part for x in insts], np.int32)
+    a_out, outs = arena([np.zeros(h.n, np.int32) for h in hs], np.int32)
+    hgs = [gen.Hypergraph(h.n, h.m, offs[i], pins[i], wvs[i], wes[i]) for i, h in enumerate(hs)]
+    return hgs, parts, outs, (a_off, a_pin, a_wv, a_we, a_pt, a_out)
+
+
 def batch_arm(args):
     """Many small hypergraphs (vertex counts log-uniform in [1,024, 65,536], nets 1.1x,
     geometric net sizes, k in {2,4,8,16}): one batched session refining all of them
@@ -372,20 +396,19 @@ def batch_arm(args):
     from host buffers (upload, set partition, 5 rounds, download). Per-instance km1
     must be identical."""
     import lpgpu
-    from lpgpu import gen
+    from lpgpu import I32P, _check, gen, lib
     insts = gen.generate_many("batch_instance", args.seed, args.instances or 4096)  # before any CUDA call
     lpgpu.build()
-    hgs = [x.hg for x in insts]
+    hgs, parts, outs, arenas = pinned_instances(lpgpu, gen, insts)
     ks = [x.k for x in insts]
-    parts = [x.part for x in insts]
     cfg = lpgpu.default_config(rounds=5, subrounds=args.subrounds)
     pins_total = sum(h.num_pins for h in hgs)
 
     def batched_once(s):
-        s.upload_batch(hgs)
-        s.set_partition_batch(ks, parts, eps=0.03)
+        s.upload_instances(hgs)
+        s.set_partition_instances(ks, parts, eps=0.03)
         r = s.refine(cfg)
-        s.partition()
+        s.partition_instances(outs)
         return r.pins_processed, s.instance_km1()
 
     with lpgpu.Session(0) as s:
@@ -419,10 +442,10 @@ def batch_arm(args):
             pp = 0
             t0 = time.perf_counter()
             for i, x in enumerate(insts):
-                s.upload(x.hg)
-                s.set_partition(x.k, x.part, eps=0.03)
+                s.upload(hgs[i])
+                s.set_partition(x.k, parts[i], eps=0.03)
                 r = s.refine(pcfg)
-                s.partition()
+                _check(lib().lpgpu_session_get_partition(s._h, outs[i].ctypes.data_as(I32P)))
                 km_p[i] = r.km1_after
                 pp += r.pins_processed
             t_plain = time.perf_counter() - t0

@@ -182,6 +182,32 @@ LPGPU_API lpgpu_status lpgpu_session_set_partition_batch(lpgpu_session* s, const
 /* km1 of every instance (num_instances values; one value for a plain session). */
 LPGPU_API lpgpu_status lpgpu_session_instance_km1(lpgpu_session* s, int64_t* km1);
 
+/* One instance of a batch in its own ids: pins in [0, num_vertices), net
+ * offsets from 0 (num_nets + 1 entries). Weights may be NULL (unit). */
+typedef struct lpgpu_instance {
+  int64_t num_vertices;
+  int64_t num_nets;
+  const int64_t* net_offsets;
+  const int32_t* pins;
+  const int32_t* vertex_weights;
+  const int32_t* net_weights;
+} lpgpu_instance;
+
+/* lpgpu_session_upload_batch from one buffer set per instance (for example
+ * one per served request): no union is built on the host; every instance is
+ * copied into place and shifted to union ids on the device. */
+LPGPU_API lpgpu_status lpgpu_session_upload_instances(lpgpu_session* s, int32_t num_instances,
+                                                      const lpgpu_instance* instances);
+
+/* lpgpu_session_set_partition_batch with one instance-local partition array
+ * per instance. */
+LPGPU_API lpgpu_status lpgpu_session_set_partition_instances(lpgpu_session* s, const int32_t* instance_k,
+                                                             const double* instance_eps,
+                                                             const int32_t* const* partitions);
+
+/* Instance-local blocks of every instance, one output array per instance. */
+LPGPU_API lpgpu_status lpgpu_session_get_partition_instances(lpgpu_session* s, int32_t* const* partitions);
+
 /* Runs the LP refinement on the device-resident state. Replaces
  * IRefiner::refine of LabelPropagationRefiner<Km1Policy>
  * (label_propagation_refiner.cpp:34-68). refinement_nodes (may be NULL with

@@ -100,7 +100,7 @@ struct RoundCtx {
   uint8_t* next_flag;    // n
   int32_t* net_epoch;    // m: round stamp of nets to expand
   // per list position
-  int2* rec;             // (to, gain); to < 0: no candidate
+  int4* rec;             // (to, gain, vertex, from), global blocks; to < 0: no candidate
   uint8_t* status;       // 0 none, 1 moved, 2 reverted, 3 rolled back
   // per block scratch
   int64_t* in_w;         // candidate weight by target block (sweep)
@@ -183,6 +183,15 @@ cudaError_t launch_validate_csr(const Launch& L, int64_t n, int64_t m, int64_t P
 // `vinst` is given, and turns local ids into global ones.
 cudaError_t launch_check_partition(const Launch& L, int64_t n, int32_t* part, int k, const int32_t* vinst,
                                    const int32_t* inst_boff, const int32_t* inst_k, int64_t* out);
+
+// Batches uploaded one instance at a time (validate.cu): instance i's local
+// pins and net offsets, copied into place, are shifted to union ids.
+cudaError_t launch_rebase_instances(const Launch& L, int I, const int64_t* inst_voff, const int64_t* inst_noff,
+                                    const int64_t* inst_poff, int64_t* net_off, int32_t* pins);
+cudaError_t launch_fill_ones(const Launch& L, int32_t* p, int64_t count);
+// Global block ids of a batch back to instance-local ids.
+cudaError_t launch_local_blocks(const Launch& L, int64_t n, const int32_t* part, const int32_t* vinst,
+                                const int32_t* inst_boff, int32_t* out);
 
 // Round phases (the sub-round pipeline). `timer` may be null.
 struct PhaseTimer;

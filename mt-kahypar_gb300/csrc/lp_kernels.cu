@@ -790,7 +790,7 @@ __device__ __forceinline__ void lv_vertex(const RoundCtx& c, int64_t o0, int d, 
 // ballots. A vertex that straddles windows carries its partial sums. Cost per
 // incidence is independent of |Λ(e)|.
 //
-// Outputs: sub-round mode writes rec[pos] = (to, gain) or to = -1 and the
+// Outputs: sub-round mode writes rec[pos] = (to, gain, v, from) (to = -1: none) and the
 // per-block candidate totals, and its last CTA plans the selection; query
 // mode (dbg_to != null) writes to / gain / border for every vertex (list =
 // all vertices, no zero-gain moves).
@@ -1057,9 +1057,10 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(Round
         if (dbg_gain) dbg_gain[v] = my_gain;
         if (dbg_border) dbg_border[v] = my_border;
       } else {
-        int2 r = make_int2(-1, 0);
+        int4 r = make_int4(-1, 0, (int)v, from + bo);
         if (my_to != from) {
-          r = make_int2(my_to + bo, my_gain);  // global target block
+          r.x = my_to + bo;  // global target block
+          r.y = my_gain;
           if (batched) {
             atomicAdd(reinterpret_cast<ull*>(&c.in_w[my_to + bo]), (ull)(int64_t)wv);
             atomicAdd(reinterpret_cast<ull*>(&c.in_cnt[my_to + bo]), 1ull);
@@ -1206,9 +1207,10 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep_heavy(RoundCtx c, int r
           if (dbg_gain) dbg_gain[v] = gain;
           if (dbg_border) dbg_border[v] = bd;
         } else {
-          int2 r = make_int2(-1, 0);
+          int4 r = make_int4(-1, 0, (int)v, from + bo);
           if (to != from) {
-            r = make_int2(to + bo, gain);
+            r.x = to + bo;
+            r.y = gain;
             atomicAdd(reinterpret_cast<ull*>(&c.in_w[to + bo]), (ull)(int64_t)wv);
             atomicAdd(reinterpret_cast<ull*>(&c.in_cnt[to + bo]), 1ull);
             atomicAdd(reinterpret_cast<ull*>(&c.cand_out[from + bo]), (ull)(int64_t)wv);
@@ -1690,12 +1692,11 @@ __global__ void k_bin_moves(RoundCtx c, int sub) {
     uint64_t key = 0;
     int w = 0;
     if (pos < end) {
-      const int2 r = c.rec[pos];
+      const int4 r = c.rec[pos];
       if (r.x >= 0 && c.over_to[r.x]) {
-        const int32_t v = c.list[pos];
-        key = move_key(r.y, v);
+        key = move_key(r.y, r.z);
         grp = r.x;
-        w = c.w_v[v];
+        w = c.w_v[r.z];
       }
     }
     // warp-aggregated segment allocation per group
@@ -1897,13 +1898,11 @@ __global__ void __launch_bounds__(kSelThreads) k_from_side(RoundCtx c, int sub) 
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
   // target-accepted weight and count per source block (acc_w / acc_cnt are cleared by the plan)
   for (int64_t pos = beg + threadIdx.x; pos < end; pos += blockDim.x) {
-    const int2 r = c.rec[pos];
+    const int4 r = c.rec[pos];
     if (r.x < 0) continue;
-    const int32_t v = c.list[pos];
-    if (move_key(r.y, v) < c.thr_to[r.x]) {
-      const int f = c.part[v];
-      atomicAdd(reinterpret_cast<ull*>(&c.acc_w[f]), (ull)(int64_t)c.w_v[v]);
-      atomicAdd(reinterpret_cast<ull*>(&c.acc_cnt[f]), 1ull);
+    if (move_key(r.y, r.z) < c.thr_to[r.x]) {
+      atomicAdd(reinterpret_cast<ull*>(&c.acc_w[r.w]), (ull)(int64_t)c.w_v[r.z]);
+      atomicAdd(reinterpret_cast<ull*>(&c.acc_cnt[r.w]), 1ull);
     }
   }
   __syncthreads();
@@ -1929,15 +1928,14 @@ __global__ void __launch_bounds__(kSelThreads) k_from_side(RoundCtx c, int sub) 
   }
   if (!s_any) return;
   for (int64_t pos = beg + threadIdx.x; pos < end; pos += blockDim.x) {
-    const int2 r = c.rec[pos];
+    const int4 r = c.rec[pos];
     if (r.x < 0) continue;
-    const int32_t v = c.list[pos];
-    const uint64_t key = move_key(r.y, v);
-    const int f = c.part[v];
+    const uint64_t key = move_key(r.y, r.z);
+    const int f = r.w;
     if (key < c.thr_to[r.x] && c.over_from[f]) {
       const ull slot = atomicAdd(reinterpret_cast<ull*>(&c.cursor[f]), 1ull);
       c.seg_key[slot] = key;
-      c.seg_w[slot] = c.w_v[v];
+      c.seg_w[slot] = c.w_v[r.z];
     }
   }
   __syncthreads();
@@ -1996,64 +1994,215 @@ __device__ __forceinline__ void activate_incidence(const RoundCtx& c, int64_t e,
 
 constexpr int kPackThreads = 256;
 
+// ---- CTA-flat incidence walks
+//
+// A CTA collects the selected vertices of a range of list positions in shared
+// memory (first incidence and degree), scans the degrees, and then spreads
+// every incidence of every collected vertex over all its threads: thread t
+// takes incidences t, t + blockDim, ... and finds its vertex by binary search
+// in the scanned degrees. Hub vertices are split across the whole CTA, and the
+// gathers and atomics of different vertices are in flight together.
+constexpr int kFlatThreads = 256;
+constexpr int kFlatItems = 1024;  // list positions (and so at most this many vertices) per CTA pass
+
+struct FlatSmem {
+  int64_t o0[kFlatItems];    // first incidence
+  int pre[kFlatItems + 1];   // degrees, then their exclusive prefix sums
+  int ft[kFlatItems];        // local from | local to << 16
+  int att[kFlatItems];       // per-vertex summed attributed delta (batched)
+  int inst[kFlatItems];      // instance (batched)
+  int wsum[kFlatThreads / 32];
+  int n;
+};
+
+// Appends the lanes with `sel` to the CTA's item list; returns each lane's slot.
+__device__ __forceinline__ int flat_append(FlatSmem& f, bool sel) {
+  const unsigned m = __ballot_sync(FULLMASK, sel);
+  if (!m) return -1;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane_id() == leader) base = atomicAdd(&f.n, __popc(m));
+  base = __shfl_sync(FULLMASK, base, leader);
+  return sel ? base + __popc(m & lanemask_lt()) : -1;
+}
+
+// In-place exclusive scan of f.pre[0 .. n) (n <= kFlatItems); f.pre[n] = total.
+__device__ __forceinline__ int flat_scan(FlatSmem& f, int n) {
+  constexpr int PER = kFlatItems / kFlatThreads;
+  const int t = threadIdx.x, lane = lane_id(), wid = t >> 5;
+  int v[PER], sum = 0;
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int i = t * PER + q;
+    v[q] = i < n ? f.pre[i] : 0;
+    sum += v[q];
+  }
+  int incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(FULLMASK, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) f.wsum[wid] = incl;
+  __syncthreads();
+  int wbase = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < kFlatThreads / 32; ++w) {
+    const int x = f.wsum[w];
+    if (w < wid) wbase += x;
+    total += x;
+  }
+  int run = wbase + incl - sum;
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int i = t * PER + q;
+    if (i < n) f.pre[i] = run;
+    run += v[q];
+  }
+  if (t == 0) f.pre[n] = total;
+  __syncthreads();
+  return total;
+}
+
+// Vertex of flat incidence index x: the largest i with pre[i] <= x.
+__device__ __forceinline__ int flat_find(const FlatSmem& f, int n, int x) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (f.pre[mid] <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Φ / Λ / Λ1 update of two incidences at once (the four Φ atomics are issued
+// before any result is used); see commit_incidence. Returns the summed
+// attributed delta and each incidence's part of it.
+__device__ __forceinline__ void commit_pair(const RoundCtx& c, bool h0, int64_t e0, int f0, int t0, bool h1,
+                                            int64_t e1, int f1, int t1, int& a0, int& a1) {
+  const int W = c.W;
+  const int64_t k = c.kmax;
+  int of0 = 0, ot0 = 0, of1 = 0, ot1 = 0;
+  if (h0) {
+    of0 = atomicSub(&c.phi[e0 * k + f0], 1);
+    ot0 = atomicAdd(&c.phi[e0 * k + t0], 1);
+  }
+  if (h1) {
+    of1 = atomicSub(&c.phi[e1 * k + f1], 1);
+    ot1 = atomicAdd(&c.phi[e1 * k + t1], 1);
+  }
+  a0 = a1 = 0;
+  if (h0) {
+    const int we = c.unit_nets ? 1 : c.w_e[e0];
+    uint32_t* rec = c.conn + e0 * 2 * W;
+    if (of0 == 1) { atomicXor(&rec[f0 >> 5], 1u << (f0 & 31)); a0 -= we; }
+    if (of0 == 1 || of0 == 2) atomicXor(&rec[W + (f0 >> 5)], 1u << (f0 & 31));
+    if (ot0 == 0) { atomicXor(&rec[t0 >> 5], 1u << (t0 & 31)); a0 += we; }
+    if (ot0 == 0 || ot0 == 1) atomicXor(&rec[W + (t0 >> 5)], 1u << (t0 & 31));
+  }
+  if (h1) {
+    const int we = c.unit_nets ? 1 : c.w_e[e1];
+    uint32_t* rec = c.conn + e1 * 2 * W;
+    if (of1 == 1) { atomicXor(&rec[f1 >> 5], 1u << (f1 & 31)); a1 -= we; }
+    if (of1 == 1 || of1 == 2) atomicXor(&rec[W + (f1 >> 5)], 1u << (f1 & 31));
+    if (ot1 == 0) { atomicXor(&rec[t1 >> 5], 1u << (t1 & 31)); a1 += we; }
+    if (ot1 == 0 || ot1 == 1) atomicXor(&rec[W + (t1 >> 5)], 1u << (t1 & 31));
+  }
+}
+
+// Moves every incidence of the CTA's collected vertices from their `from` to
+// their `to` block (flat over the CTA). Returns this thread's summed delta;
+// per-vertex sums go to f.att when `per_item`.
+__device__ __forceinline__ int64_t flat_commit(const RoundCtx& c, FlatSmem& f, int n, int total, bool per_item) {
+  int64_t att = 0;
+  for (int x0 = threadIdx.x; x0 < total; x0 += 2 * kFlatThreads) {
+    const int x1 = x0 + kFlatThreads;
+    const bool h1 = x1 < total;
+    const int i0 = flat_find(f, n, x0), i1 = h1 ? flat_find(f, n, x1) : i0;
+    const int64_t e0 = c.inets[f.o0[i0] + (x0 - f.pre[i0])];
+    const int64_t e1 = h1 ? c.inets[f.o0[i1] + (x1 - f.pre[i1])] : 0;
+    const int ft0 = f.ft[i0], ft1 = f.ft[i1];
+    int a0, a1;
+    commit_pair(c, true, e0, ft0 & 0xffff, ft0 >> 16, h1, e1, ft1 & 0xffff, ft1 >> 16, a0, a1);
+    att += a0 + a1;
+    if (per_item) {
+      if (a0) atomicAdd(&f.att[i0], a0);
+      if (a1) atomicAdd(&f.att[i1], a1);
+    }
+  }
+  return att;
+}
+
 // Commit of the accepted moves (changeNodePart, h:539-563, without the
 // per-move weight check: the selection already guarantees both bounds).
-// Marks status[pos] = 1 for committed moves and overwrites rec[pos].y with
-// the source block (the gain is no longer needed). With `last`, the moves
-// are final and the sub-round is closed; kept moves are activated at the end
-// of the round (k_activate_round).
-__global__ void __launch_bounds__(kPackThreads, 4) k_commit(RoundCtx c, int round, int sub, int last) {
+// Marks status[pos] = 1 for committed moves. CTA-flat over ranges of
+// kFlatItems list positions. With `last`, the moves are final and the
+// sub-round is closed; kept moves are activated at the end of the round
+// (k_activate_round).
+__global__ void __launch_bounds__(kFlatThreads) k_commit(RoundCtx c, int round, int sub, int last) {
   extern __shared__ ull s_dw[];
-  __shared__ unsigned char s_own[kPackThreads];
+  __shared__ FlatSmem f;
   // block-weight deltas: shared memory for one instance, global atomics for a batch
-  ull* dw = c.batched ? reinterpret_cast<ull*>(c.bw) : s_dw;
-  const int kdw = c.batched ? 0 : c.k;
+  const bool batched = c.batched != 0;
+  ull* dw = batched ? reinterpret_cast<ull*>(c.bw) : s_dw;
+  const int kdw = batched ? 0 : c.k;
   for (int b = threadIdx.x; b < kdw; b += blockDim.x) s_dw[b] = 0;
-  __syncthreads();
-  const int lane = lane_id();
-  unsigned char* own = s_own + (threadIdx.x & ~31);
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
+  constexpr int PER = kFlatItems / kFlatThreads;
   int64_t att = 0, moved = 0;
-  const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
-  for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
-       base += stride) {
-    const int64_t pos = base + lane;
-    int2 r = make_int2(-1, 0);
-    int32_t v = 0;
-    int f = 0, deg = 0, bo = 0;
-    int64_t o0 = 0;
-    bool acc = false;
-    if (pos < end) {
-      r = c.rec[pos];
-      if (r.x >= 0) {
-        v = c.list[pos];
-        f = c.part[v];
-        const uint64_t key = move_key(r.y, v);
-        acc = key < c.thr_to[r.x] && key < c.thr_from[f];
-        if (acc) {
-          c.rec[pos].y = f;
-          o0 = c.vtx_off[v];
-          deg = (int)(c.vtx_off[v + 1] - o0);
-          bo = block_offset(c, v);
-        }
+  for (int64_t r0 = beg + (int64_t)blockIdx.x * kFlatItems; r0 < end; r0 += (int64_t)gridDim.x * kFlatItems) {
+    if (threadIdx.x == 0) f.n = 0;
+    __syncthreads();
+    int4 rv[PER];
+    bool acc[PER];
+    int64_t o0[PER], o1[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int64_t pos = r0 + q * kFlatThreads + threadIdx.x;
+      rv[q] = pos < end ? c.rec[pos] : make_int4(-1, 0, 0, 0);
+    }
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      acc[q] = false;
+      o0[q] = o1[q] = 0;
+      if (rv[q].x >= 0) {
+        const uint64_t key = move_key(rv[q].y, rv[q].z);
+        acc[q] = key < c.thr_to[rv[q].x] && key < c.thr_from[rv[q].w];
+        o0[q] = c.vtx_off[rv[q].z];
+        o1[q] = c.vtx_off[rv[q].z + 1];
       }
-      c.status[pos] = acc ? 1 : 0;
     }
-    const int tot = packed_incidences(acc, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
-      const int bow = __shfl_sync(FULLMASK, bo, ow);
-      const int fo = __shfl_sync(FULLMASK, f, ow) - bow;   // local blocks
-      const int to = __shfl_sync(FULLMASK, r.x, ow) - bow;
-      return has ? commit_incidence(c, c.inets[j], fo, to) : 0;
-    });
-    if (acc) {
-      att += tot;
-      if (c.batched) atomicAdd(reinterpret_cast<ull*>(&c.inst_delta[c.vinst[v]]), (ull)(int64_t)tot);
-      c.part[v] = r.x;
-      const int64_t wv = c.w_v[v];
-      atomicAdd(&dw[r.x], (ull)wv);
-      atomicAdd(&dw[f], (ull)(-wv));
-      ++moved;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int64_t pos = r0 + q * kFlatThreads + threadIdx.x;
+      if (pos < end) c.status[pos] = acc[q] ? 1 : 0;
+      const int slot = flat_append(f, acc[q]);
+      if (acc[q]) {
+        const int v = rv[q].z;
+        int bo = 0;
+        if (batched) {
+          const int i = c.vinst[v];
+          bo = c.inst_boff[i];
+          f.inst[slot] = i;
+          f.att[slot] = 0;
+        }
+        f.o0[slot] = o0[q];
+        f.pre[slot] = (int)(o1[q] - o0[q]);
+        f.ft[slot] = (rv[q].w - bo) | ((rv[q].x - bo) << 16);
+        c.part[v] = rv[q].x;
+        const int64_t wv = c.w_v[v];
+        atomicAdd(&dw[rv[q].x], (ull)wv);
+        atomicAdd(&dw[rv[q].w], (ull)(-wv));
+        ++moved;
+      }
     }
+    __syncthreads();
+    const int n = f.n;
+    const int total = flat_scan(f, n);
+    att += flat_commit(c, f, n, total, batched);
+    __syncthreads();
+    if (batched)
+      for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (f.att[i]) atomicAdd(reinterpret_cast<ull*>(&c.inst_delta[f.inst[i]]), (ull)(int64_t)f.att[i]);
   }
   att = block_sum_i64(att);
   moved = block_sum_i64(moved);
@@ -2087,8 +2236,9 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_revert_eval(RoundCtx c, int
     int64_t o0 = 0;
     int deg = 0;
     if (moved) {
-      r = c.rec[pos];
-      const int64_t v = c.list[pos];
+      const int4 rv = c.rec[pos];
+      r = make_int2(rv.x, rv.w);
+      const int64_t v = rv.z;
       o0 = c.vtx_off[v];
       deg = (int)(c.vtx_off[v + 1] - o0);
       const int bo = block_offset(c, v);
@@ -2189,9 +2339,9 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_undo_reverts(RoundCtx c, in
     int2 r = make_int2(0, 0);  // (to, from), global blocks
     int bo = 0;
     if (sel) {
-      const int32_t pos = c.revl[i];
-      v = c.list[pos];
-      r = c.rec[pos];
+      const int4 rv = c.rec[c.revl[i]];
+      v = rv.z;
+      r = make_int2(rv.x, rv.w);
       bo = block_offset(c, v);
     }
     att += undo_tile(c, sel, v, r, bo, own, dw, c.batched != 0);
@@ -2232,7 +2382,11 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_rollback(RoundCtx c, int ro
         sel = c.inst_delta[i] > 0;  // rollback is decided per instance
       }
     }
-    const int2 r = sel ? c.rec[pos] : make_int2(0, 0);
+    int2 r = make_int2(0, 0);
+    if (sel) {
+      const int4 rv = c.rec[pos];
+      r = make_int2(rv.x, rv.w);
+    }
     att += undo_tile(c, sel, v, r, bo, own, dw, false);
     if (sel) {
       c.status[pos] = 3;
@@ -2322,7 +2476,7 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
   }
   const int g = grid_for(L, n, 256, 8);
   // incidence kernels: one wave of resident CTAs striding over the sub-round
-  const int g_commit = grid_for(L, n, kPackThreads, occupancy((const void*)k_commit, kPackThreads, dw_smem));
+  const int g_commit = grid_for(L, n, kFlatItems, occupancy((const void*)k_commit, kFlatThreads, dw_smem));
   const int g_eval = grid_for(L, n, kPackThreads, occupancy((const void*)k_revert_eval, kPackThreads, 0));
   const int g_undo = grid_for(L, n, kPackThreads, occupancy((const void*)k_rollback, kPackThreads, dw_smem));
   const int g_bin = grid_for(L, n, 256, occupancy((const void*)k_bin_moves, 256, 0));
@@ -2340,7 +2494,7 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
   const int last_commit = !c.revert && !c.rollback;
   {
     Scope sc(timer, "commit");
-    k_commit<<<g_commit, kPackThreads, dw_smem, L.st>>>(c, round, sub, last_commit);
+    k_commit<<<g_commit, kFlatThreads, dw_smem, L.st>>>(c, round, sub, last_commit);
     LAUNCHED("k_commit");
   }
   if (c.revert) {

@@ -99,7 +99,7 @@ struct lpgpu_session_s {
   DevBuf<int32_t> list, net_epoch, seg_w, heavy, revl;
   DevBuf<int64_t> sub_off, blk64, scal, stats, tile_cnt, tile_off, scan_tmp;
   DevBuf<uint8_t> next_flag, status, over;
-  DevBuf<int2> rec;
+  DevBuf<int4> rec;
   DevBuf<uint64_t> seg_key, thr;
   DevBuf<int32_t> saved_part;
   int64_t scan_tmp_n = 0;
@@ -352,12 +352,13 @@ lpgpu_status lpgpu_session_destroy(lpgpu_session* s) {
   return LPGPU_OK;
 }
 
-static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const int64_t* net_off,
+// Upload of a union CSR (`insts` null) or of per-instance buffers (`insts`
+// with the host-computed instance vertex / net / pin offsets). Shapes are
+// checked by the caller.
+static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t P, const int64_t* net_off,
                                 const int32_t* pins, const int32_t* w_v, const int32_t* w_e,
-                                int32_t num_inst, const int64_t* inst_voff, const int64_t* inst_noff) {
-  if (!s) return invalid("null session");
-  lpgpu_status vs = check_shape(n, m, net_off, pins, num_inst, inst_voff, inst_noff);
-  if (vs != LPGPU_OK) return vs;
+                                int32_t num_inst, const int64_t* inst_voff, const int64_t* inst_noff,
+                                const lpgpu_instance* insts = nullptr, const int64_t* inst_poff = nullptr) {
   DeviceGuard g(s->device);
   CK(cudaStreamSynchronize(s->st));
   // buffers of the same size are reused; the partition must be set again
@@ -365,10 +366,9 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const in
   s->has_hg = false;
   s->n = n;
   s->m = m;
-  s->P = net_off[m];
+  s->P = P;
   const int32_t I = inst_voff ? num_inst : 1;
   int64_t* fp = &s->footprint;
-  const int64_t P = s->P;
   CK(s->net_off.alloc(m + 1, fp));
   CK(s->vtx_off.alloc(n + 1, fp));
   CK(s->pins.alloc(P, fp));
@@ -392,28 +392,42 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const in
   s->scan_tmp_n = std::max<int64_t>(1, std::max(scan_tmp_elems(n + 1), scan_tmp_elems(kMaxSubrounds * tiles)));
   CK(s->scan_tmp.alloc(s->scan_tmp_n, fp));
   cudaStream_t st = s->st;
-  CK(cudaMemcpyAsync(s->net_off.p, net_off, sizeof(int64_t) * (m + 1), cudaMemcpyHostToDevice, st));
-  if (P > 0) CK(cudaMemcpyAsync(s->pins.p, pins, sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
-  if (n > 0) {
-    if (w_v) {
-      CK(cudaMemcpyAsync(s->w_v.p, w_v, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
-    } else {
-      std::vector<int32_t> ones(n, 1);
-      CK(cudaMemcpyAsync(s->w_v.p, ones.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
-      CK(cudaStreamSynchronize(st));
+  const Launch L = s->launch();
+  if (!insts) {
+    CK(cudaMemcpyAsync(s->net_off.p, net_off, sizeof(int64_t) * (m + 1), cudaMemcpyHostToDevice, st));
+    if (P > 0) CK(cudaMemcpyAsync(s->pins.p, pins, sizeof(int32_t) * P, cudaMemcpyHostToDevice, st));
+    if (n > 0) {
+      if (w_v) CK(cudaMemcpyAsync(s->w_v.p, w_v, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+      else CK(launch_fill_ones(L, s->w_v.p, n));
     }
-    CK(cudaMemsetAsync(s->next_flag.p, 0, n, st));
-  }
-  if (m > 0) {
-    if (w_e) {
-      CK(cudaMemcpyAsync(s->w_e.p, w_e, sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
-    } else {
-      std::vector<int32_t> ones(m, 1);
-      CK(cudaMemcpyAsync(s->w_e.p, ones.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
-      CK(cudaStreamSynchronize(st));
+    if (m > 0) {
+      if (w_e) CK(cudaMemcpyAsync(s->w_e.p, w_e, sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
+      else CK(launch_fill_ones(L, s->w_e.p, m));
     }
-    CK(cudaMemsetAsync(s->net_epoch.p, 0, sizeof(int32_t) * m, st));
+  } else {
+    // unit weights first, then every instance's own buffers into place (stream order)
+    bool unit_v = false, unit_e = false;
+    for (int32_t i = 0; i < I; ++i) {
+      unit_v = unit_v || !insts[i].vertex_weights;
+      unit_e = unit_e || !insts[i].net_weights;
+    }
+    if (unit_v) CK(launch_fill_ones(L, s->w_v.p, n));
+    if (unit_e) CK(launch_fill_ones(L, s->w_e.p, m));
+    for (int32_t i = 0; i < I; ++i) {
+      const lpgpu_instance& x = insts[i];
+      const int64_t ni = x.num_vertices, mi = x.num_nets, pi = inst_poff[i + 1] - inst_poff[i];
+      if (mi > 0)
+        CK(cudaMemcpyAsync(s->net_off.p + inst_noff[i], x.net_offsets, sizeof(int64_t) * mi, cudaMemcpyHostToDevice, st));
+      if (pi > 0) CK(cudaMemcpyAsync(s->pins.p + inst_poff[i], x.pins, sizeof(int32_t) * pi, cudaMemcpyHostToDevice, st));
+      if (ni > 0 && x.vertex_weights)
+        CK(cudaMemcpyAsync(s->w_v.p + inst_voff[i], x.vertex_weights, sizeof(int32_t) * ni, cudaMemcpyHostToDevice, st));
+      if (mi > 0 && x.net_weights)
+        CK(cudaMemcpyAsync(s->w_e.p + inst_noff[i], x.net_weights, sizeof(int32_t) * mi, cudaMemcpyHostToDevice, st));
+    }
+    CK(cudaMemcpyAsync(s->net_off.p + m, &P, sizeof(int64_t), cudaMemcpyHostToDevice, st));  // synchronized below
   }
+  if (n > 0) CK(cudaMemsetAsync(s->next_flag.p, 0, n, st));
+  if (m > 0) CK(cudaMemsetAsync(s->net_epoch.p, 0, sizeof(int32_t) * m, st));
   // instance ranges of a batched session
   s->batched = inst_voff != nullptr;
   s->num_inst = I;
@@ -429,6 +443,15 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const in
     CK(s->inst_noff.alloc(I + 1, fp));
     CK(cudaMemcpyAsync(s->inst_voff.p, inst_voff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(s->inst_noff.p, inst_noff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
+    if (insts) {  // local ids to union ids
+      DevBuf<int64_t> poff;
+      int64_t tmpfp = 0;
+      CK(poff.alloc(I + 1, &tmpfp));
+      CK(cudaMemcpyAsync(poff.p, inst_poff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
+      CK(launch_rebase_instances(L, I, s->inst_voff.p, s->inst_noff.p, poff.p, s->net_off.p, s->pins.p));
+      CK(cudaStreamSynchronize(st));
+      poff.release(&tmpfp);
+    }
   } else {
     s->vinst.release(fp);
     s->inst_voff.release(fp);
@@ -471,7 +494,32 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, const in
 
 lpgpu_status lpgpu_session_upload(lpgpu_session* s, int64_t n, int64_t m, const int64_t* net_off,
                                   const int32_t* pins, const int32_t* w_v, const int32_t* w_e) {
-  return upload_impl(s, n, m, net_off, pins, w_v, w_e, 1, nullptr, nullptr);
+  if (!s) return invalid("null session");
+  const lpgpu_status vs = check_shape(n, m, net_off, pins, 1, nullptr, nullptr);
+  if (vs != LPGPU_OK) return vs;
+  return upload_impl(s, n, m, net_off[m], net_off, pins, w_v, w_e, 1, nullptr, nullptr);
+}
+
+lpgpu_status lpgpu_session_upload_instances(lpgpu_session* s, int32_t num_instances,
+                                            const lpgpu_instance* instances) {
+  if (!s) return invalid("null session");
+  if (num_instances < 1 || !instances) return invalid("a batch needs at least one instance");
+  std::vector<int64_t> voff(num_instances + 1, 0), noff(num_instances + 1, 0), poff(num_instances + 1, 0);
+  for (int32_t i = 0; i < num_instances; ++i) {
+    const lpgpu_instance& x = instances[i];
+    if (x.num_vertices < 0 || x.num_nets < 0) return invalid("negative vertex or net count");
+    if (!x.net_offsets) return invalid("null CSR pointer");
+    if (x.net_offsets[0] != 0) return invalid("net_offsets[0] must be 0");
+    const int64_t pi = x.net_offsets[x.num_nets];
+    if (pi < 0) return invalid("net_offsets must be non-decreasing");
+    if (pi > 0 && !x.pins) return invalid("null CSR pointer");
+    voff[i + 1] = voff[i] + x.num_vertices;
+    noff[i + 1] = noff[i] + x.num_nets;
+    poff[i + 1] = poff[i] + pi;
+    if (voff[i + 1] > INT32_MAX || noff[i + 1] > INT32_MAX) return invalid("vertex and net ids must fit int32");
+  }
+  return upload_impl(s, voff[num_instances], noff[num_instances], poff[num_instances], nullptr, nullptr, nullptr,
+                     nullptr, num_instances, voff.data(), noff.data(), instances, poff.data());
 }
 
 lpgpu_status lpgpu_session_upload_batch(lpgpu_session* s, int32_t num_instances,
@@ -480,8 +528,12 @@ lpgpu_status lpgpu_session_upload_batch(lpgpu_session* s, int32_t num_instances,
                                         const int32_t* pins, const int32_t* w_v, const int32_t* w_e) {
   if (num_instances < 1 || !instance_vertex_offsets || !instance_net_offsets)
     return invalid("a batch needs at least one instance and its offsets");
+  if (!s) return invalid("null session");
   const int64_t n = instance_vertex_offsets[num_instances], m = instance_net_offsets[num_instances];
-  return upload_impl(s, n, m, net_off, pins, w_v, w_e, num_instances, instance_vertex_offsets,
+  const lpgpu_status vs = check_shape(n, m, net_off, pins, num_instances, instance_vertex_offsets,
+                                      instance_net_offsets);
+  if (vs != LPGPU_OK) return vs;
+  return upload_impl(s, n, m, net_off[m], net_off, pins, w_v, w_e, num_instances, instance_vertex_offsets,
                      instance_net_offsets);
 }
 
@@ -489,7 +541,8 @@ lpgpu_status lpgpu_session_upload_batch(lpgpu_session* s, int32_t num_instances,
 // and builds it from `part` (host): block ids in [0, K) for one instance, or
 // local ids per instance for a batch (turned into global ids on the device).
 static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax, const int32_t* part,
-                                       const std::vector<int64_t>& hl, const std::vector<int64_t>& hp) {
+                                       const std::vector<int64_t>& hl, const std::vector<int64_t>& hp,
+                                       const int32_t* const* parts = nullptr) {
   DeviceGuard g(s->device);
   CK(cudaStreamSynchronize(s->st));
   s->has_part = false;
@@ -517,7 +570,14 @@ static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax
     CK(cudaMemcpyAsync(s->inst_k.p, s->h_inst_k.data(), sizeof(int32_t) * s->num_inst, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(s->inst_delta.p, 0, sizeof(int64_t) * s->num_inst, st));
   }
-  if (s->n > 0) CK(cudaMemcpyAsync(s->part.p, part, sizeof(int32_t) * s->n, cudaMemcpyHostToDevice, st));
+  if (parts) {
+    for (int32_t i = 0; i < s->num_inst; ++i) {
+      const int64_t v0 = s->h_inst_voff[i], ni = s->h_inst_voff[i + 1] - v0;
+      if (ni > 0) CK(cudaMemcpyAsync(s->part.p + v0, parts[i], sizeof(int32_t) * ni, cudaMemcpyHostToDevice, st));
+    }
+  } else if (s->n > 0) {
+    CK(cudaMemcpyAsync(s->part.p, part, sizeof(int32_t) * s->n, cudaMemcpyHostToDevice, st));
+  }
   CK(launch_check_partition(s->launch(), s->n, s->part.p, K, s->batched ? s->vinst.p : nullptr,
                             s->inst_boff.p, s->inst_k.p, s->vout.p));
   int64_t verdict = 0;
@@ -535,14 +595,20 @@ static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax
   return LPGPU_OK;
 }
 
-lpgpu_status lpgpu_session_set_partition_batch(lpgpu_session* s, const int32_t* instance_k,
-                                               const double* instance_eps, const int32_t* partition) {
+// Per-instance k / eps of a batch; the partition comes as one union array
+// (`partition`) or one array per instance (`parts`).
+static lpgpu_status set_partition_batch_impl(lpgpu_session* s, const int32_t* instance_k,
+                                             const double* instance_eps, const int32_t* partition,
+                                             const int32_t* const* parts) {
   if (!s) return invalid("null session");
   if (!s->has_hg || !s->batched) {
     set_error("set_partition_batch needs a batched upload");
     return LPGPU_ERR_STATE;
   }
-  if (!instance_k || !instance_eps || (s->n > 0 && !partition)) return invalid("null argument");
+  if (!instance_k || !instance_eps || (s->n > 0 && !partition && !parts)) return invalid("null argument");
+  if (parts)
+    for (int32_t i = 0; i < s->num_inst; ++i)
+      if (!parts[i] && s->h_inst_voff[i + 1] > s->h_inst_voff[i]) return invalid("null argument");
   const int32_t I = s->num_inst;
   std::vector<int32_t> boff(I);
   int64_t K = 0;
@@ -567,7 +633,18 @@ lpgpu_status lpgpu_session_set_partition_batch(lpgpu_session* s, const int32_t* 
   }
   s->h_inst_boff = boff;
   s->h_inst_k.assign(instance_k, instance_k + I);
-  return set_partition_impl(s, (int32_t)K, kmax, partition, hl, hp);
+  return set_partition_impl(s, (int32_t)K, kmax, partition, hl, hp, parts);
+}
+
+lpgpu_status lpgpu_session_set_partition_batch(lpgpu_session* s, const int32_t* instance_k,
+                                               const double* instance_eps, const int32_t* partition) {
+  return set_partition_batch_impl(s, instance_k, instance_eps, partition, nullptr);
+}
+
+lpgpu_status lpgpu_session_set_partition_instances(lpgpu_session* s, const int32_t* instance_k,
+                                                   const double* instance_eps, const int32_t* const* partitions) {
+  if (!partitions) return invalid("null argument");
+  return set_partition_batch_impl(s, instance_k, instance_eps, nullptr, partitions);
 }
 
 lpgpu_status lpgpu_session_set_partition(lpgpu_session* s, int32_t k, double eps,
@@ -798,11 +875,33 @@ lpgpu_status lpgpu_session_get_partition(lpgpu_session* s, int32_t* partition) {
   lpgpu_status ps = need_part(s);
   if (ps != LPGPU_OK) return ps;
   DeviceGuard g(s->device);
-  if (s->n > 0) CK(cudaMemcpyAsync(partition, s->part.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
+  const int32_t* src = s->part.p;
+  if (s->batched) {  // global block ids back to instance-local ids, staged in the selection scratch
+    CK(launch_local_blocks(s->launch(), s->n, s->part.p, s->vinst.p, s->inst_boff.p, s->seg_w.p));
+    src = s->seg_w.p;
+  }
+  if (s->n > 0) CK(cudaMemcpyAsync(partition, src, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
-  if (s->batched)  // global block ids back to instance-local ids
-    for (int32_t i = 0; i < s->num_inst; ++i)
-      for (int64_t v = s->h_inst_voff[i]; v < s->h_inst_voff[i + 1]; ++v) partition[v] -= s->h_inst_boff[i];
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_get_partition_instances(lpgpu_session* s, int32_t* const* partitions) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  if (!s->batched) {
+    set_error("get_partition_instances needs a batched session");
+    return LPGPU_ERR_STATE;
+  }
+  if (!partitions) return invalid("null output");
+  for (int32_t i = 0; i < s->num_inst; ++i)
+    if (!partitions[i] && s->h_inst_voff[i + 1] > s->h_inst_voff[i]) return invalid("null output");
+  DeviceGuard g(s->device);
+  CK(launch_local_blocks(s->launch(), s->n, s->part.p, s->vinst.p, s->inst_boff.p, s->seg_w.p));
+  for (int32_t i = 0; i < s->num_inst; ++i) {
+    const int64_t v0 = s->h_inst_voff[i], ni = s->h_inst_voff[i + 1] - v0;
+    if (ni > 0) CK(cudaMemcpyAsync(partitions[i], s->seg_w.p + v0, sizeof(int32_t) * ni, cudaMemcpyDeviceToHost, s->st));
+  }
+  CK(cudaStreamSynchronize(s->st));
   return LPGPU_OK;
 }
 
@@ -991,7 +1090,7 @@ int64_t lpgpu_estimate_footprint(int64_t n, int64_t m, int64_t P, int32_t k, int
   const int64_t tiles = tiles_for(n);
   int64_t b = 0;
   b += 8 * (m + 1) + 8 * (n + 1) + 4 * P * 2 + 4 * n + 4 * m;          // CSR + weights
-  b += 4 * m + 4 * n + n + n + 8 * n + 8 * n + 4 * n + 8 * n;          // epoch, list, flags, status, rec, seg, queues
+  b += 4 * m + 4 * n + n + n + 16 * n + 8 * n + 4 * n + 8 * n;         // epoch, list, flags, status, rec, seg, queues
   b += 8 * (kMaxSubrounds + 1) + 2 * 8 * kMaxSubrounds * tiles;        // sub-round bins
   b += 8 * (scan_tmp_elems(std::max(n + 1, kMaxSubrounds * tiles)) + 1);
   b += 4 * n + 4 * m * (int64_t)k + 8 * m * W;                         // part, Φ, Λ + Λ1

@@ -141,6 +141,33 @@ __global__ void k_check_partition(int64_t n, int32_t* __restrict__ part, int k, 
   }
 }
 
+// CTA i shifts instance i's pins by its first vertex and its net offsets by
+// its first pin (the ranges come from the host, so no access depends on the
+// unchecked input).
+__global__ void k_rebase_instances(const int64_t* __restrict__ inst_voff, const int64_t* __restrict__ inst_noff,
+                                   const int64_t* __restrict__ inst_poff, int64_t* __restrict__ net_off,
+                                   int32_t* __restrict__ pins) {
+  const int i = blockIdx.x;
+  const int32_t v0 = (int32_t)inst_voff[i];
+  const int64_t p0 = inst_poff[i];
+  if (v0)
+    for (int64_t q = p0 + threadIdx.x; q < inst_poff[i + 1]; q += blockDim.x)
+      pins[q] = (int32_t)((uint32_t)pins[q] + (uint32_t)v0);  // wraps: out-of-range ids stay out of range
+  if (p0)
+    for (int64_t e = inst_noff[i] + threadIdx.x; e < inst_noff[i + 1]; e += blockDim.x) net_off[e] += p0;
+}
+
+__global__ void k_fill_ones(int32_t* __restrict__ p, int64_t count) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = 1;
+}
+
+__global__ void k_local_blocks(int64_t n, const int32_t* __restrict__ part, const int32_t* __restrict__ vinst,
+                               const int32_t* __restrict__ inst_boff, int32_t* __restrict__ out) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+    out[v] = part[v] - inst_boff[vinst[v]];
+}
+
 int grid(const Launch& L, int64_t items, int threads) {
   const int64_t need = (items + threads - 1) / threads;
   return (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)L.num_sms * 8));
@@ -167,6 +194,32 @@ cudaError_t launch_check_partition(const Launch& L, int64_t n, int32_t* part, in
   if (e != cudaSuccess) return e;
   if (n > 0) {
     k_check_partition<<<grid(L, n, 256), 256, 0, L.st>>>(n, part, k, vinst, inst_boff, inst_k, out);
+    add_kernel_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rebase_instances(const Launch& L, int I, const int64_t* inst_voff, const int64_t* inst_noff,
+                                    const int64_t* inst_poff, int64_t* net_off, int32_t* pins) {
+  if (I > 0) {
+    k_rebase_instances<<<I, 256, 0, L.st>>>(inst_voff, inst_noff, inst_poff, net_off, pins);
+    add_kernel_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_ones(const Launch& L, int32_t* p, int64_t count) {
+  if (count > 0) {
+    k_fill_ones<<<grid(L, count, 256), 256, 0, L.st>>>(p, count);
+    add_kernel_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_local_blocks(const Launch& L, int64_t n, const int32_t* part, const int32_t* vinst,
+                                const int32_t* inst_boff, int32_t* out) {
+  if (n > 0) {
+    k_local_blocks<<<grid(L, n, 256), 256, 0, L.st>>>(n, part, vinst, inst_boff, out);
     add_kernel_launches(1);
   }
   return cudaGetLastError();

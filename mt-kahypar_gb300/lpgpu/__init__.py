@@ -31,6 +31,12 @@ class Config(ctypes.Structure):
                 ("flags", ctypes.c_int32), ("reserved1", ctypes.c_int32)]
 
 
+class InstanceDesc(ctypes.Structure):
+    """lpgpu_instance: one batch instance in its own ids."""
+    _fields_ = [("num_vertices", ctypes.c_int64), ("num_nets", ctypes.c_int64),
+                ("net_offsets", I64P), ("pins", I32P), ("vertex_weights", I32P), ("net_weights", I32P)]
+
+
 class Result(ctypes.Structure):
     _fields_ = [("km1_before", ctypes.c_int64), ("km1_after", ctypes.c_int64),
                 ("delta", ctypes.c_int64), ("moves", ctypes.c_int64),
@@ -72,7 +78,8 @@ SYMBOLS = [
     "lpgpu_session_restore_partition", "lpgpu_kernel_launches", "lpgpu_host_alloc",
     "lpgpu_host_free", "lpgpu_session_event_record", "lpgpu_session_event_elapsed",
     "lpgpu_session_synchronize", "lpgpu_session_upload_batch", "lpgpu_session_set_partition_batch",
-    "lpgpu_session_instance_km1", "lpgpu_partition_metrics_noalloc",
+    "lpgpu_session_instance_km1", "lpgpu_partition_metrics_noalloc", "lpgpu_session_upload_instances",
+    "lpgpu_session_set_partition_instances", "lpgpu_session_get_partition_instances",
 ]
 
 
@@ -164,6 +171,47 @@ class Session:
                                                 _p(np.ascontiguousarray(net_off, np.int64), I64P),
                                                 _p(pins, I32P), _p(w_v, I32P), _p(w_e, I32P)))
         return self
+
+    def upload_instances(self, hgs):
+        """Uploads a list of hypergraphs as one batch from their own buffers
+        (lpgpu_session_upload_instances: no union is built on the host)."""
+        keep = []
+        descs = (InstanceDesc * len(hgs))()
+        for i, h in enumerate(hgs):
+            arrs = (np.ascontiguousarray(h.net_off, np.int64), np.ascontiguousarray(h.pins, np.int32),
+                    None if h.w_v is None else np.ascontiguousarray(h.w_v, np.int32),
+                    None if h.w_e is None else np.ascontiguousarray(h.w_e, np.int32))
+            keep.append(arrs)
+            descs[i] = InstanceDesc(h.n, h.m, _p(arrs[0], I64P), _p(arrs[1], I32P), _p(arrs[2], I32P),
+                                    _p(arrs[3], I32P))
+        nv = np.array([0] + [h.n for h in hgs], np.int64).cumsum()
+        ne = np.array([0] + [h.m for h in hgs], np.int64).cumsum()
+        _check(lib().lpgpu_session_upload_instances(self._h, ctypes.c_int32(len(hgs)), descs))
+        self.n, self.m = int(nv[-1]), int(ne[-1])
+        self.inst_voff, self.inst_noff = nv, ne
+        self.num_inst = len(hgs)
+        return self
+
+    def set_partition_instances(self, ks, parts, eps=0.03):
+        """Per-instance k and one instance-local partition array per instance."""
+        ks = np.ascontiguousarray(ks, np.int32)
+        ep = np.ascontiguousarray(np.broadcast_to(np.asarray(eps, np.float64), ks.shape), np.float64)
+        arrs = [np.ascontiguousarray(p, np.int32) for p in parts]
+        ptrs = (I32P * len(arrs))(*[_p(a, I32P) for a in arrs])
+        self.k = int(ks.max())
+        self.num_blocks = int(ks.sum())
+        _check(lib().lpgpu_session_set_partition_instances(self._h, _p(ks, I32P),
+                                                           ep.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ptrs))
+        return self
+
+    def partition_instances(self, out=None):
+        """Instance-local partitions, one array per instance (into `out` if given)."""
+        off = self.inst_voff
+        outs = out if out is not None else [np.empty(int(off[i + 1] - off[i]), np.int32)
+                                            for i in range(self.num_inst)]
+        ptrs = (I32P * len(outs))(*[_p(a, I32P) for a in outs])
+        _check(lib().lpgpu_session_get_partition_instances(self._h, ptrs))
+        return outs
 
     def set_partition_batch(self, ks, parts, eps=0.03):
         """Per-instance k and instance-local partitions (list of arrays)."""

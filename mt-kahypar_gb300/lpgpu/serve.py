@@ -73,15 +73,14 @@ class ServeStats:
 
 def _run_batch(session, reqs, subrounds, flags=FLAG_NO_GRAPH):
     """Refines `reqs` together on one batched session; returns pins processed."""
-    session.upload_batch([r.hg for r in reqs])
-    session.set_partition_batch([r.k for r in reqs], [r.part for r in reqs],
-                                eps=np.array([r.eps for r in reqs]))
+    session.upload_instances([r.hg for r in reqs])
+    session.set_partition_instances([r.k for r in reqs], [r.part for r in reqs],
+                                    eps=np.array([r.eps for r in reqs]))
     res = session.refine(default_config(rounds=reqs[0].rounds, subrounds=subrounds, flags=flags))
-    part = session.partition()
+    parts = session.partition_instances()
     km1 = session.instance_km1()
-    off = np.cumsum([0] + [r.hg.n for r in reqs])
     for i, r in enumerate(reqs):
-        r.result = part[off[i]:off[i + 1]].copy()
+        r.result = parts[i]
         r.km1 = int(km1[i])
     return res.pins_processed
 

@@ -74,3 +74,42 @@ def test_batch_state_and_errors(lp, orc):
         with pytest.raises(lp.LpgpuError) as e:
             s.upload_batch([broken, bad[1]])
         assert e.value.status == lp.ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_instance_buffers_equal_union(lp, seed):
+    """lpgpu_session_upload_instances / _set_partition_instances /
+    _get_partition_instances give the union API's results."""
+    insts = _instances(seed, 9)
+    cfg = lp.default_config(rounds=4, subrounds=4)
+    with lp.Session(0) as a, lp.Session(0) as b:
+        a.upload_batch([x.hg for x in insts])
+        a.set_partition_batch([x.k for x in insts], [x.part for x in insts], eps=0.05)
+        ra = a.refine(cfg)
+        pa = a.partition()
+        b.upload_instances([x.hg for x in insts])
+        b.set_partition_instances([x.k for x in insts], [x.part for x in insts], eps=0.05)
+        rb = b.refine(cfg)
+        pb = b.partition_instances()
+        assert (ra.km1_before, ra.km1_after, ra.delta) == (rb.km1_before, rb.km1_after, rb.delta)
+        assert np.array_equal(np.concatenate(pb), pa)
+        assert np.array_equal(a.instance_km1(), b.instance_km1())
+        assert np.array_equal(a.pin_counts(), b.pin_counts())
+
+
+def test_instance_buffers_are_checked(lp):
+    from lpgpu import gen
+    insts = _instances(5, 4)
+    bad = insts[2].hg
+    pins = bad.pins.copy()
+    pins[3] = bad.n  # one past the instance's own vertices
+    broken = gen.Hypergraph(bad.n, bad.m, bad.net_off, pins, bad.w_v, bad.w_e)
+    with lp.Session(0) as s:
+        with pytest.raises(lp.LpgpuError) as e:
+            s.upload_instances([insts[0].hg, insts[1].hg, broken, insts[3].hg])
+        assert e.value.status == lp.ERR_INVALID_ARG
+        unit = [gen.Hypergraph(x.hg.n, x.hg.m, x.hg.net_off, x.hg.pins, None, None) for x in insts]
+        s.upload_instances(unit)
+        s.set_partition_instances([x.k for x in insts], [x.part for x in insts])
+        bw = s.block_weights()
+        assert bw.sum() == sum(x.hg.n for x in insts)
