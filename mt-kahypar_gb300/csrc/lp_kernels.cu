@@ -614,6 +614,15 @@ __device__ void plan_to(const RoundCtx& c);
 // net weight stays below 2^PL take this path; the others take the
 // warp-cooperative windows below.
 constexpr int kLvWeights = 16;  // vertex weights 1..16 have precomputed feasibility masks
+// Incidences per lane whose gathers are issued together (a multiple of 4), and
+// resident CTAs per SM the k <= 128 sweep is compiled for.
+#ifndef LPGPU_LV_UNROLL
+#define LPGPU_LV_UNROLL 4
+#endif
+#ifndef LPGPU_SWEEP_MIN_BLOCKS
+#define LPGPU_SWEEP_MIN_BLOCKS 3
+#endif
+static_assert(LPGPU_LV_UNROLL % 4 == 0, "the carry-save adder takes four vectors at a time");
 
 // cnt += s0 + 2 s1 + 4 s2 (bit-sliced, ripple carry).
 template <int PL>
@@ -647,64 +656,67 @@ __device__ __forceinline__ void lv_add_weighted(uint32_t (&cnt)[PL], uint32_t x,
   }
 }
 
-// Best move of one vertex by its own lane: the same decision as `decide`
-// (Km1Policy::computeMaxGainMoveImpl with disable_randomization, plus the
-// zero-gain rebalancing rule of label_propagation_refiner.h:88-95). `from`,
-// `to` are local block ids; `bo` is the instance's first global block.
-template <int W, bool UNIT, int PL>
-__device__ __forceinline__ void lv_vertex(const RoundCtx& c, int64_t o0, int d, int from, int wv, int bo,
-                                          int inst, bool batched, int zero_gain,
-                                          const uint32_t* __restrict__ s_fmask, const int* __restrict__ s_slack,
-                                          const int64_t* __restrict__ s_bw, const int64_t* __restrict__ s_perf,
-                                          int& to, int& gain, bool& border) {
-  constexpr int U = 4;  // incidences whose loads are issued together
+// One step of a lane's vertex: the next U incidences (from index j) of the
+// vertex with incidences [o0, o0 + d) and source block `from` (local) are
+// added into the bit-sliced counters and the internal weight.
+template <int W, bool UNIT, int PL, int U>
+__device__ __forceinline__ void lv_accumulate(const RoundCtx& c, int64_t o0, int d, int j, int from,
+                                              uint32_t (&cnt)[W][PL], int& internal) {
   constexpr int W2 = 2 * W;
   const int fw = from >> 5;
   const uint32_t fbit = 1u << (from & 31);
-  uint32_t cnt[W][PL];
+  int32_t ee[U];
 #pragma unroll
-  for (int t = 0; t < W; ++t)
+  for (int u = 0; u < U; ++u) ee[u] = j + u < d ? __ldg(&c.inets[o0 + j + u]) : -1;
+  uint32_t wd[U][W], l1[U];
+  int we[U];
 #pragma unroll
-    for (int p = 0; p < PL; ++p) cnt[t][p] = 0;
-  int internal = 0;  // Σ w(e) over incident nets with Φ(e, from) > 1
-  for (int j = 0; j < d; j += U) {
-    int32_t ee[U];
+  for (int u = 0; u < U; ++u) {
 #pragma unroll
-    for (int u = 0; u < U; ++u) ee[u] = j + u < d ? __ldg(&c.inets[o0 + j + u]) : -1;
-    uint32_t wd[U][W], l1[U];
-    int we[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-#pragma unroll
-      for (int t = 0; t < W; ++t) wd[u][t] = 0;
-      l1[u] = fbit;
-      we[u] = 0;
-      if (ee[u] >= 0) {
-        const uint32_t* rec = c.conn + (int64_t)ee[u] * W2;
-        load_words<W>(rec, wd[u]);
-        l1[u] = __ldg(rec + W + fw);
-        we[u] = UNIT ? 1 : __ldg(&c.w_e[ee[u]]);
-      }
+    for (int t = 0; t < W; ++t) wd[u][t] = 0;
+    l1[u] = fbit;
+    we[u] = 0;
+    if (ee[u] >= 0) {
+      const uint32_t* rec = c.conn + (int64_t)ee[u] * W2;
+      load_words<W>(rec, wd[u]);
+      l1[u] = __ldg(rec + W + fw);
+      we[u] = UNIT ? 1 : __ldg(&c.w_e[ee[u]]);
     }
+  }
 #pragma unroll
-    for (int u = 0; u < U; ++u) internal += (l1[u] & fbit) ? 0 : we[u];
-    if constexpr (UNIT) {
-      // carry-save sum of the four vectors, then one 3-bit ripple add
+  for (int u = 0; u < U; ++u) internal += (l1[u] & fbit) ? 0 : we[u];
+  if constexpr (UNIT) {
+    // carry-save sum of each four vectors, then one 3-bit ripple add
+#pragma unroll
+    for (int g = 0; g < U; g += 4)
 #pragma unroll
       for (int t = 0; t < W; ++t) {
-        const uint32_t a = wd[0][t], b = wd[1][t], e = wd[2][t], f = wd[3][t];
+        const uint32_t a = wd[g][t], b = wd[g + 1][t], e = wd[g + 2][t], f = wd[g + 3][t];
         const uint32_t s = a ^ b ^ e;
         const uint32_t c1 = (a & b) | (e & (a ^ b));
         const uint32_t c2 = s & f;
         lv_add3<PL>(cnt[t], s ^ f, c1 ^ c2, c1 & c2);
       }
-    } else {
+  } else {
 #pragma unroll
-      for (int u = 0; u < U; ++u)
+    for (int u = 0; u < U; ++u)
 #pragma unroll
-        for (int t = 0; t < W; ++t) lv_add_weighted<PL>(cnt[t], wd[u][t], we[u]);
-    }
+      for (int t = 0; t < W; ++t) lv_add_weighted<PL>(cnt[t], wd[u][t], we[u]);
   }
+}
+
+// Best move of one vertex from its counters: the same decision as `decide`
+// (Km1Policy::computeMaxGainMoveImpl with disable_randomization, plus the
+// zero-gain rebalancing rule of label_propagation_refiner.h:88-95). `from`,
+// `to` are local block ids; `bo` is the instance's first global block.
+template <int W, int PL>
+__device__ __forceinline__ void lv_decide(const RoundCtx& c, const uint32_t (&cnt)[W][PL], int internal, int from,
+                                          int wv, int bo, int inst, bool batched, int zero_gain,
+                                          const uint32_t* __restrict__ s_fmask, const int* __restrict__ s_slack,
+                                          const int64_t* __restrict__ s_bw, const int64_t* __restrict__ s_perf,
+                                          int& to, int& gain, bool& border) {
+  const int fw = from >> 5;
+  const uint32_t fbit = 1u << (from & 31);
   // feasible targets: c(V_b) + w(v) <= L_max(b)
   uint32_t cand[W];
   if (!batched && wv >= 1 && wv <= kLvWeights) {
@@ -774,6 +786,26 @@ __device__ __forceinline__ void lv_vertex(const RoundCtx& c, int64_t o0, int d, 
   }
 }
 
+// Best move of one vertex by its own lane (accumulate all incidences, decide).
+template <int W, bool UNIT, int PL>
+__device__ __forceinline__ void lv_vertex(const RoundCtx& c, int64_t o0, int d, int from, int wv, int bo,
+                                          int inst, bool batched, int zero_gain,
+                                          const uint32_t* __restrict__ s_fmask, const int* __restrict__ s_slack,
+                                          const int64_t* __restrict__ s_bw, const int64_t* __restrict__ s_perf,
+                                          int& to, int& gain, bool& border) {
+  constexpr int U = LPGPU_LV_UNROLL;
+  uint32_t cnt[W][PL];
+#pragma unroll
+  for (int t = 0; t < W; ++t)
+#pragma unroll
+    for (int p = 0; p < PL; ++p) cnt[t][p] = 0;
+  int internal = 0;  // Σ w(e) over incident nets with Φ(e, from) > 1
+  for (int j = 0; j < d; j += U) lv_accumulate<W, UNIT, PL, U>(c, o0, d, j, from, cnt, internal);
+  lv_decide<W, PL>(c, cnt, internal, from, wv, bo, inst, batched, zero_gain, s_fmask, s_slack, s_bw, s_perf, to,
+                   gain, border);
+}
+
+
 // Sweep: the best move of every active vertex (moveVertex's isBorderNode +
 // computeMaxGainMove, label_propagation_refiner.h:82-95) on the current state.
 //
@@ -795,7 +827,7 @@ __device__ __forceinline__ void lv_vertex(const RoundCtx& c, int64_t o0, int d, 
 // mode (dbg_to != null) writes to / gain / border for every vertex (list =
 // all vertices, no zero-gain moves).
 template <int W, bool UNIT>
-__global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : 3)) k_sweep(RoundCtx c, int round, int sub,
+__global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : (W == 4 ? LPGPU_SWEEP_MIN_BLOCKS : 3))) k_sweep(RoundCtx c, int round, int sub,
                                                              int32_t* dbg_to, int32_t* dbg_gain,
                                                              uint8_t* dbg_border) {
   constexpr int B = W <= 8 ? 2 : 1;  // windows whose gathers are issued together (k > 128)
@@ -1963,36 +1995,11 @@ __device__ void close_subround(const RoundCtx& c, int round) {
     for (int i = threadIdx.x; i < c.num_inst; i += blockDim.x) c.inst_delta[i] = 0;
 }
 
-// One incidence of a move from f to t: atomic decrement of Φ(e,f) and
-// increment of Φ(e,t) with the Λ / Λ1 toggles of warp_commit_vertex; returns
-// the attributed delta of this incidence.
-__device__ __forceinline__ int commit_incidence(const RoundCtx& c, int64_t e, int f, int t) {
-  const int W = c.W;
-  const int we = c.unit_nets ? 1 : c.w_e[e];
-  uint32_t* rec = c.conn + e * 2 * W;
-  const uint32_t fbit = 1u << (f & 31), tbit = 1u << (t & 31);
-  int att = 0;
-  const int of = atomicSub(&c.phi[e * c.kmax + f], 1);  // Φ rows hold kmax entries
-  if (of == 1) {
-    atomicXor(&rec[f >> 5], fbit);
-    att -= we;
-  }
-  if (of == 1 || of == 2) atomicXor(&rec[W + (f >> 5)], fbit);
-  const int ot = atomicAdd(&c.phi[e * c.kmax + t], 1);
-  if (ot == 0) {
-    atomicXor(&rec[t >> 5], tbit);
-    att += we;
-  }
-  if (ot == 0 || ot == 1) atomicXor(&rec[W + (t >> 5)], tbit);
-  return att;
-}
-
 // Activation stamp of one incident net of a kept move (see k_expand_nets).
 __device__ __forceinline__ void activate_incidence(const RoundCtx& c, int64_t e, int epoch) {
   if (c.net_off[e + 1] - c.net_off[e] <= c.act_threshold) c.net_epoch[e] = epoch;
 }
 
-constexpr int kPackThreads = 256;
 
 // ---- CTA-flat incidence walks
 //
@@ -2009,22 +2016,26 @@ struct FlatSmem {
   int64_t o0[kFlatItems];    // first incidence
   int pre[kFlatItems + 1];   // degrees, then their exclusive prefix sums
   int ft[kFlatItems];        // local from | local to << 16
-  int att[kFlatItems];       // per-vertex summed attributed delta (batched)
+  int att[kFlatItems];       // per-vertex sums (attributed delta, or the reverse move's gain)
   int inst[kFlatItems];      // instance (batched)
+  int pos[kFlatItems];       // list position
   int wsum[kFlatThreads / 32];
   int n;
 };
 
-// Appends the lanes with `sel` to the CTA's item list; returns each lane's slot.
-__device__ __forceinline__ int flat_append(FlatSmem& f, bool sel) {
+// Warp-aggregated append to a shared counter; returns each selected lane's slot.
+__device__ __forceinline__ int flat_append_to(int* counter, bool sel) {
   const unsigned m = __ballot_sync(FULLMASK, sel);
   if (!m) return -1;
   const int leader = __ffs(m) - 1;
   int base = 0;
-  if (lane_id() == leader) base = atomicAdd(&f.n, __popc(m));
+  if (lane_id() == leader) base = atomicAdd(counter, __popc(m));
   base = __shfl_sync(FULLMASK, base, leader);
   return sel ? base + __popc(m & lanemask_lt()) : -1;
 }
+
+// Appends the lanes with `sel` to the CTA's item list; returns each lane's slot.
+__device__ __forceinline__ int flat_append(FlatSmem& f, bool sel) { return flat_append_to(&f.n, sel); }
 
 // In-place exclusive scan of f.pre[0 .. n) (n <= kFlatItems); f.pre[n] = total.
 __device__ __forceinline__ int flat_scan(FlatSmem& f, int n) {
@@ -2074,9 +2085,13 @@ __device__ __forceinline__ int flat_find(const FlatSmem& f, int n, int x) {
   return lo;
 }
 
-// Φ / Λ / Λ1 update of two incidences at once (the four Φ atomics are issued
-// before any result is used); see commit_incidence. Returns the summed
-// attributed delta and each incidence's part of it.
+// Φ / Λ / Λ1 update of two incidences at once; the four Φ atomics are issued
+// before any result is used. Per incidence of a move from f to t: atomic
+// decrement of Φ(e, f) and increment of Φ(e, t); Λ toggles when Φ(e, f)
+// reaches 0 or Φ(e, t) leaves 0, Λ1 when either passes through 1. The
+// attributed delta (km1Delta, hypergraph_common.h:133-140) is -w(e) when
+// Φ(e, f) reaches 0 and +w(e) when Φ(e, t) reaches 1; a0 / a1 are each
+// incidence's part.
 __device__ __forceinline__ void commit_pair(const RoundCtx& c, bool h0, int64_t e0, int f0, int t0, bool h1,
                                             int64_t e1, int f1, int t1, int& a0, int& a1) {
   const int W = c.W;
@@ -2220,80 +2235,119 @@ __global__ void __launch_bounds__(kFlatThreads) k_commit(RoundCtx c, int round, 
 // before any is undone: a move from f to t is marked for revert (status 2)
 // when moving the vertex back to f now strictly improves km1. This is the
 // deterministic counterpart of the realised-gain check of moveVertex
-// (label_propagation_refiner.h:100-137).
-__global__ void __launch_bounds__(kPackThreads, 4) k_revert_eval(RoundCtx c, int sub) {
-  __shared__ unsigned char s_own[kPackThreads];
-  const int lane = lane_id();
-  unsigned char* own = s_own + (threadIdx.x & ~31);
-  const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
-  const int64_t stride = ((int64_t)gridDim.x * blockDim.x);
+// (label_propagation_refiner.h:100-137). CTA-flat over ranges of list
+// positions; the marked positions are appended to the revert list with one
+// global atomic per range.
+__global__ void __launch_bounds__(kFlatThreads) k_revert_eval(RoundCtx c, int sub) {
+  __shared__ FlatSmem f;
+  __shared__ int s_rev, s_base;
+  const bool batched = c.batched != 0;
   const int W = c.W;
-  for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
-       base += stride) {
-    const int64_t pos = base + lane;
-    const bool moved = pos < end && c.status[pos] == 1;
-    int2 r = make_int2(0, 0);  // (to, from), local blocks
-    int64_t o0 = 0;
-    int deg = 0;
-    if (moved) {
-      const int4 rv = c.rec[pos];
-      r = make_int2(rv.x, rv.w);
-      const int64_t v = rv.z;
-      o0 = c.vtx_off[v];
-      deg = (int)(c.vtx_off[v + 1] - o0);
-      const int bo = block_offset(c, v);
-      r.x -= bo;
-      r.y -= bo;
+  const int lane = lane_id();
+  const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
+  constexpr int PER = kFlatItems / kFlatThreads;
+  for (int64_t r0 = beg + (int64_t)blockIdx.x * kFlatItems; r0 < end; r0 += (int64_t)gridDim.x * kFlatItems) {
+    if (threadIdx.x == 0) {
+      f.n = 0;
+      s_rev = 0;
     }
-    const int score = packed_incidences(moved, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
-      const int t = __shfl_sync(FULLMASK, r.x, ow);
-      const int f = __shfl_sync(FULLMASK, r.y, ow);
-      int x = 0;
-      if (has) {
-        const int64_t e = c.inets[j];
-        const int we = c.unit_nets ? 1 : c.w_e[e];
-        const uint32_t* rec = c.conn + e * 2 * W;
-        if (!((rec[W + (t >> 5)] >> (t & 31)) & 1u)) x += we;  // Φ(e, t) > 1
-        if ((rec[f >> 5] >> (f & 31)) & 1u) x -= we;           // f in Λ(e)
+    __syncthreads();
+    uint8_t st[PER];
+    int4 rv[PER];
+    int64_t o0[PER], o1[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int64_t pos = r0 + q * kFlatThreads + threadIdx.x;
+      st[q] = pos < end ? c.status[pos] : 0;
+      rv[q] = pos < end ? c.rec[pos] : make_int4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      o0[q] = o1[q] = 0;
+      if (st[q] == 1) {
+        o0[q] = c.vtx_off[rv[q].z];
+        o1[q] = c.vtx_off[rv[q].z + 1];
       }
-      return x;
-    });
-    const bool rev = moved && score < 0;
-    if (rev) c.status[pos] = 2;
-    const unsigned rm = __ballot_sync(FULLMASK, rev);
-    if (rm) {
-      const int leader = __ffs(rm) - 1;
-      ull base = 0;
-      if (lane == leader) base = atomicAdd(reinterpret_cast<ull*>(&c.scal[kRevCount]), (ull)__popc(rm));
-      base = __shfl_sync(FULLMASK, base, leader);
-      if (rev) c.revl[base + __popc(rm & lanemask_lt())] = (int32_t)pos;
     }
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int slot = flat_append(f, st[q] == 1);
+      if (slot >= 0) {
+        const int bo = batched ? c.inst_boff[c.vinst[rv[q].z]] : 0;
+        f.o0[slot] = o0[q];
+        f.pre[slot] = (int)(o1[q] - o0[q]);
+        f.ft[slot] = (rv[q].w - bo) | ((rv[q].x - bo) << 16);
+        f.att[slot] = 0;
+        f.pos[slot] = (int)(r0 + q * kFlatThreads + threadIdx.x);
+      }
+    }
+    __syncthreads();
+    const int n = f.n;
+    const int total = flat_scan(f, n);
+    // gain of moving back: + w(e) if Φ(e, t) > 1, - w(e) if f in Λ(e)
+    for (int x0 = threadIdx.x; x0 < total; x0 += 2 * kFlatThreads) {
+      const int x1 = x0 + kFlatThreads;
+      const bool h1 = x1 < total;
+      const int i0 = flat_find(f, n, x0), i1 = h1 ? flat_find(f, n, x1) : i0;
+      const int64_t e0 = c.inets[f.o0[i0] + (x0 - f.pre[i0])];
+      const int64_t e1 = h1 ? c.inets[f.o0[i1] + (x1 - f.pre[i1])] : 0;
+      const int ft0 = f.ft[i0], ft1 = f.ft[i1];
+      const int fa = ft0 & 0xffff, ta = ft0 >> 16, fb = ft1 & 0xffff, tb = ft1 >> 16;
+      const uint32_t* ra = c.conn + e0 * 2 * W;
+      const uint32_t* rb = c.conn + e1 * 2 * W;
+      const uint32_t l1a = ra[W + (ta >> 5)], lfa = ra[fa >> 5];
+      uint32_t l1b = 0, lfb = 0;
+      if (h1) {
+        l1b = rb[W + (tb >> 5)];
+        lfb = rb[fb >> 5];
+      }
+      const int wa = c.unit_nets ? 1 : c.w_e[e0];
+      const int wb = h1 ? (c.unit_nets ? 1 : c.w_e[e1]) : 0;
+      const int xa = (((l1a >> (ta & 31)) & 1u) ? 0 : wa) - (((lfa >> (fa & 31)) & 1u) ? wa : 0);
+      const int xb = h1 ? (((l1b >> (tb & 31)) & 1u) ? 0 : wb) - (((lfb >> (fb & 31)) & 1u) ? wb : 0) : 0;
+      if (xa) atomicAdd(&f.att[i0], xa);
+      if (xb) atomicAdd(&f.att[i1], xb);
+    }
+    __syncthreads();
+    // mark, collect locally (in f.pre, no longer needed), then one global append
+    for (int base = threadIdx.x - lane; base < n; base += blockDim.x) {
+      const int i = base + lane;
+      const bool rev = i < n && f.att[i] < 0;
+      const int slot = flat_append_to(&s_rev, rev);
+      if (rev) {
+        c.status[f.pos[i]] = 2;
+        f.pre[slot] = f.pos[i];
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_rev)
+      s_base = (int)atomicAdd(reinterpret_cast<ull*>(&c.scal[kRevCount]), (ull)s_rev);
+    __syncthreads();
+    for (int i = threadIdx.x; i < s_rev; i += blockDim.x) c.revl[s_base + i] = f.pre[i];
+    __syncthreads();
   }
 }
 
-// Undo of one tile of moves (lane = move): Φ / Λ / Λ1 back from t to f,
-// part and block weights restored. Returns the summed attributed delta.
-__device__ __forceinline__ int64_t undo_tile(const RoundCtx& c, bool sel, int64_t v, int2 r, int bo,
-                                             unsigned char* own, ull* dw, bool inst_delta) {
-  int64_t o0 = 0;
-  int deg = 0;
-  if (sel) {
-    o0 = c.vtx_off[v];
-    deg = (int)(c.vtx_off[v + 1] - o0);
+// Collects undo items: vertex v moved from global block `from` to `to`; the
+// item moves it back (its Φ / Λ / Λ1 from `to` to `from`), and part and the
+// CTA's block-weight deltas are restored right away.
+__device__ __forceinline__ void flat_undo_item(const RoundCtx& c, FlatSmem& f, int slot, int v, int to, int from,
+                                               int64_t o0, int64_t o1, ull* dw, bool per_item) {
+  int bo = 0;
+  if (c.batched) {
+    const int i = c.vinst[v];
+    bo = c.inst_boff[i];
+    f.inst[slot] = i;
   }
-  const int tot = packed_incidences(sel, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
-    const int bow = __shfl_sync(FULLMASK, bo, ow);
-    const int t = __shfl_sync(FULLMASK, r.x, ow) - bow;
-    const int f = __shfl_sync(FULLMASK, r.y, ow) - bow;
-    return has ? commit_incidence(c, c.inets[j], t, f) : 0;
-  });
-  if (!sel) return 0;
-  if (inst_delta) atomicAdd(reinterpret_cast<ull*>(&c.inst_delta[c.vinst[v]]), (ull)(int64_t)tot);
-  c.part[v] = r.y;
+  f.att[slot] = 0;
+  f.o0[slot] = o0;
+  f.pre[slot] = (int)(o1 - o0);
+  f.ft[slot] = (to - bo) | ((from - bo) << 16);
+  (void)per_item;
+  c.part[v] = from;
   const int64_t wv = c.w_v[v];
-  atomicAdd(&dw[r.y], (ull)wv);
-  atomicAdd(&dw[r.x], (ull)(-wv));
-  return tot;
+  atomicAdd(&dw[from], (ull)wv);
+  atomicAdd(&dw[to], (ull)(-wv));
 }
 
 // Books undone moves into the sub-round's delta and statistics and flushes
@@ -2314,38 +2368,48 @@ __device__ __forceinline__ void undo_epilogue(const RoundCtx& c, int round, int6
 }
 
 // Undo of the moves the hindsight check marked (status 2), from the compact
-// list k_revert_eval wrote. With `last` the sub-round is closed.
-__global__ void __launch_bounds__(kPackThreads, 4) k_undo_reverts(RoundCtx c, int round, int last) {
+// list k_revert_eval wrote, spread over all CTAs (each takes a short range and
+// walks its moves' incidences flat). With `last` the sub-round is closed.
+__global__ void __launch_bounds__(kFlatThreads) k_undo_reverts(RoundCtx c, int round, int last) {
   extern __shared__ ull s_dw[];
-  __shared__ unsigned char s_own[kPackThreads];
-  ull* dw = c.batched ? reinterpret_cast<ull*>(c.bw) : s_dw;
-  const int kdw = c.batched ? 0 : c.k;
+  __shared__ FlatSmem f;
+  const bool batched = c.batched != 0;
+  ull* dw = batched ? reinterpret_cast<ull*>(c.bw) : s_dw;
+  const int kdw = batched ? 0 : c.k;
   for (int b = threadIdx.x; b < kdw; b += blockDim.x) s_dw[b] = 0;
-  __syncthreads();
-  const int lane = lane_id();
-  unsigned char* own = s_own + (threadIdx.x & ~31);
+  constexpr int PER = kFlatItems / kFlatThreads;
   const int64_t cnt = c.scal[kRevCount];
-  // spread the moves over all warps (few per warp): their incidence chains
-  // then run side by side instead of one after another inside a warp
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int64_t want = (cnt + nwarps - 1) / nwarps;
-  const int per = want < 1 ? 1 : (want > 32 ? 32 : (int)want);
-  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t want = (cnt + gridDim.x - 1) / gridDim.x;
+  const int per = want < 32 ? 32 : (want > kFlatItems ? kFlatItems : (int)want);
   int64_t att = 0, undone = 0;
-  for (int64_t base = gw * per; base < cnt; base += nwarps * per) {
-    const int64_t i = base + lane;
-    const bool sel = lane < per && i < cnt;
-    int64_t v = 0;
-    int2 r = make_int2(0, 0);  // (to, from), global blocks
-    int bo = 0;
-    if (sel) {
-      const int4 rv = c.rec[c.revl[i]];
-      v = rv.z;
-      r = make_int2(rv.x, rv.w);
-      bo = block_offset(c, v);
+  for (int64_t r0 = (int64_t)blockIdx.x * per; r0 < cnt; r0 += (int64_t)gridDim.x * per) {
+    if (threadIdx.x == 0) f.n = 0;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int off = q * kFlatThreads + threadIdx.x;
+      const bool sel = off < per && r0 + off < cnt;
+      int4 rv = make_int4(0, 0, 0, 0);
+      int64_t o0 = 0, o1 = 0;
+      if (sel) {
+        rv = c.rec[c.revl[r0 + off]];
+        o0 = c.vtx_off[rv.z];
+        o1 = c.vtx_off[rv.z + 1];
+      }
+      const int slot = flat_append(f, sel);
+      if (sel) {
+        flat_undo_item(c, f, slot, rv.z, rv.x, rv.w, o0, o1, dw, batched);
+        ++undone;
+      }
     }
-    att += undo_tile(c, sel, v, r, bo, own, dw, c.batched != 0);
-    undone += sel ? 1 : 0;
+    __syncthreads();
+    const int n = f.n;
+    const int total = flat_scan(f, n);
+    att += flat_commit(c, f, n, total, batched);
+    __syncthreads();
+    if (batched)
+      for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (f.att[i]) atomicAdd(reinterpret_cast<ull*>(&c.inst_delta[f.inst[i]]), (ull)(int64_t)f.att[i]);
   }
   undo_epilogue(c, round, att, undone, kDeltaSub, s_dw, kdw);
   if (last && last_cta(&c.scal[kDone])) close_subround(c, round);
@@ -2354,44 +2418,46 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_undo_reverts(RoundCtx c, in
 // Rollback: when the sub-round's delta is positive, undo of every move still
 // marked 1 (status 3); decided per instance when batched (kDeltaSub and
 // inst_delta are not written here). Closes the sub-round.
-__global__ void __launch_bounds__(kPackThreads, 4) k_rollback(RoundCtx c, int round, int sub) {
+__global__ void __launch_bounds__(kFlatThreads) k_rollback(RoundCtx c, int round, int sub) {
   const bool roll = c.batched || c.scal[kDeltaSub] > 0;
   extern __shared__ ull s_dw[];
-  __shared__ unsigned char s_own[kPackThreads];
-  ull* dw = c.batched ? reinterpret_cast<ull*>(c.bw) : s_dw;
-  const int kdw = c.batched ? 0 : c.k;
+  __shared__ FlatSmem f;
+  const bool batched = c.batched != 0;
+  ull* dw = batched ? reinterpret_cast<ull*>(c.bw) : s_dw;
+  const int kdw = batched ? 0 : c.k;
   for (int b = threadIdx.x; b < kdw; b += blockDim.x) s_dw[b] = 0;
-  __syncthreads();
-  const int lane = lane_id();
-  unsigned char* own = s_own + (threadIdx.x & ~31);
+  constexpr int PER = kFlatItems / kFlatThreads;
   const int64_t beg = c.sub_off[sub], end = roll ? c.sub_off[sub + 1] : beg;
   int64_t att = 0, undone = 0;
-  for (int64_t base = beg + blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < end;
-       base += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t pos = base + lane;
-    const uint8_t st = pos < end ? c.status[pos] : 0;
-    int64_t v = 0;
-    int bo = 0;
-    bool sel = false;
-    if (st == 1) {
-      v = c.list[pos];
-      sel = true;
-      if (c.batched) {
-        const int i = c.vinst[v];
-        bo = c.inst_boff[i];
-        sel = c.inst_delta[i] > 0;  // rollback is decided per instance
+  for (int64_t r0 = beg + (int64_t)blockIdx.x * kFlatItems; r0 < end; r0 += (int64_t)gridDim.x * kFlatItems) {
+    if (threadIdx.x == 0) f.n = 0;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int64_t pos = r0 + q * kFlatThreads + threadIdx.x;
+      bool sel = pos < end && c.status[pos] == 1;
+      int4 rv = make_int4(0, 0, 0, 0);
+      int64_t o0 = 0, o1 = 0;
+      if (sel) {
+        rv = c.rec[pos];
+        if (batched) sel = c.inst_delta[c.vinst[rv.z]] > 0;  // rollback is decided per instance
+      }
+      if (sel) {
+        o0 = c.vtx_off[rv.z];
+        o1 = c.vtx_off[rv.z + 1];
+      }
+      const int slot = flat_append(f, sel);
+      if (sel) {
+        flat_undo_item(c, f, slot, rv.z, rv.x, rv.w, o0, o1, dw, false);
+        c.status[pos] = 3;
+        ++undone;
       }
     }
-    int2 r = make_int2(0, 0);
-    if (sel) {
-      const int4 rv = c.rec[pos];
-      r = make_int2(rv.x, rv.w);
-    }
-    att += undo_tile(c, sel, v, r, bo, own, dw, false);
-    if (sel) {
-      c.status[pos] = 3;
-      ++undone;
-    }
+    __syncthreads();
+    const int n = f.n;
+    const int total = flat_scan(f, n);
+    att += flat_commit(c, f, n, total, false);
+    __syncthreads();
   }
   undo_epilogue(c, round, att, undone, kDeltaRb, s_dw, kdw);
   if (last_cta(&c.scal[kDone])) close_subround(c, round);
@@ -2401,8 +2467,8 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_rollback(RoundCtx c, int ro
 // pins of its incident nets with |e| <= activation threshold become active in
 // the next round (moveVertex, label_propagation_refiner.h:112-128). Nets are
 // stamped with the round's epoch and expanded by k_expand_nets.
-__global__ void __launch_bounds__(kPackThreads, 4) k_activate_round(RoundCtx c, int S) {
-  __shared__ unsigned char s_own[kPackThreads];
+__global__ void __launch_bounds__(256) k_activate_round(RoundCtx c, int S) {
+  __shared__ unsigned char s_own[256];
   const int lane = lane_id();
   unsigned char* own = s_own + (threadIdx.x & ~31);
   const int epoch = (int)c.scal[kEpoch];
@@ -2425,6 +2491,7 @@ __global__ void __launch_bounds__(kPackThreads, 4) k_activate_round(RoundCtx c, 
     });
   }
 }
+
 
 // End of a round: the pins of every net stamped with the round's epoch
 // become active for the next round. A warp takes 32 nets and walks the pins
@@ -2454,8 +2521,8 @@ __global__ void __launch_bounds__(256) k_expand_nets(RoundCtx c) {
 cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, int S, PhaseTimer* timer) {
   {
     Scope sc(timer, "activate");
-    k_activate_round<<<grid_for(L, c.n, kPackThreads, occupancy((const void*)k_activate_round, kPackThreads, 0)),
-                       kPackThreads, 0, L.st>>>(c, S);
+    k_activate_round<<<grid_for(L, c.n, 256, occupancy((const void*)k_activate_round, 256, 0)), 256, 0,
+                       L.st>>>(c, S);
     LAUNCHED("k_activate_round");
   }
   if (c.m == 0) return cudaSuccess;
@@ -2477,8 +2544,10 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
   const int g = grid_for(L, n, 256, 8);
   // incidence kernels: one wave of resident CTAs striding over the sub-round
   const int g_commit = grid_for(L, n, kFlatItems, occupancy((const void*)k_commit, kFlatThreads, dw_smem));
-  const int g_eval = grid_for(L, n, kPackThreads, occupancy((const void*)k_revert_eval, kPackThreads, 0));
-  const int g_undo = grid_for(L, n, kPackThreads, occupancy((const void*)k_rollback, kPackThreads, dw_smem));
+  const int g_eval = grid_for(L, n, kFlatItems, occupancy((const void*)k_revert_eval, kFlatThreads, 0));
+  const int g_undo = grid_for(L, n, kFlatItems, occupancy((const void*)k_rollback, kFlatThreads, dw_smem));
+  const int g_unrev = (int)std::max<int64_t>(1, std::min<int64_t>((n + 31) / 32, (int64_t)L.num_sms *
+      occupancy((const void*)k_undo_reverts, kFlatThreads, dw_smem)));
   const int g_bin = grid_for(L, n, 256, occupancy((const void*)k_bin_moves, 256, 0));
   {
     Scope sc(timer, "select");
@@ -2499,14 +2568,14 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
   }
   if (c.revert) {
     Scope sc(timer, "revert");
-    k_revert_eval<<<g_eval, kPackThreads, 0, L.st>>>(c, sub);
+    k_revert_eval<<<g_eval, kFlatThreads, 0, L.st>>>(c, sub);
     LAUNCHED("k_revert_eval");
-    k_undo_reverts<<<g_undo, kPackThreads, dw_smem, L.st>>>(c, round, !c.rollback);
+    k_undo_reverts<<<g_unrev, kFlatThreads, dw_smem, L.st>>>(c, round, !c.rollback);
     LAUNCHED("k_undo_reverts");
   }
   if (c.rollback) {
     Scope sc(timer, "rollback");
-    k_rollback<<<g_undo, kPackThreads, dw_smem, L.st>>>(c, round, sub);
+    k_rollback<<<g_undo, kFlatThreads, dw_smem, L.st>>>(c, round, sub);
     LAUNCHED("k_rollback");
   }
   return cudaSuccess;

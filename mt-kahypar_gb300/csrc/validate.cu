@@ -87,8 +87,9 @@ __global__ void k_check_nets(int64_t m, int64_t P, const int64_t* __restrict__ n
   }
 }
 
-// Thread per vertex: w(v) >= 0, the vertex's instance (batched), Σ w(v) per
-// instance (warp sums when the warp's vertices share an instance).
+// Thread per vertex: w(v) >= 0, the vertex's instance (written to vinst when
+// given, i.e. for every batched session), Σ w(v) per instance (warp sums when
+// the warp's vertices share an instance).
 __global__ void k_check_vertices(int64_t n, const int32_t* __restrict__ w_v, int I,
                                  const int64_t* __restrict__ inst_voff, int32_t* __restrict__ vinst,
                                  int64_t* out) {
@@ -102,8 +103,8 @@ __global__ void k_check_vertices(int64_t n, const int32_t* __restrict__ w_v, int
     if (ok) {
       w = w_v ? w_v[v] : 1;
       if (w < 0) fail(out, kVNegVertexWeight);
-      if (I > 1) {
-        inst = find_instance(inst_voff, I, v);
+      if (vinst) {  // batched session (also with a single instance)
+        inst = I > 1 ? find_instance(inst_voff, I, v) : 0;
         vinst[v] = inst;
       }
     }

@@ -113,3 +113,23 @@ def test_instance_buffers_are_checked(lp):
         s.set_partition_instances([x.k for x in insts], [x.part for x in insts])
         bw = s.block_weights()
         assert bw.sum() == sum(x.hg.n for x in insts)
+
+
+@pytest.mark.parametrize("api", ["union", "instances"])
+def test_single_instance_batch(lp, orc, api):
+    """A batch of one instance (every vertex belongs to instance 0) behaves like
+    a plain session."""
+    x = _instances(6, 1)[0]
+    cfg = lp.default_config(rounds=4, subrounds=4)
+    with lp.Session(0) as s:
+        if api == "union":
+            s.upload_batch([x.hg])
+            s.set_partition_batch([x.k], [x.part], eps=0.03)
+        else:
+            s.upload_instances([x.hg])
+            s.set_partition_instances([x.k], [x.part], eps=0.03)
+        s.refine(cfg)
+        got = s.partition()
+    ref, _ = orc.lp_sync(x.hg, x.k, x.lmax, x.part, perfect=x.perfect, rounds=4, subrounds=4,
+                         revert=1, rollback=1, zero_gain=1)
+    assert np.array_equal(got, ref)
