@@ -1714,12 +1714,65 @@ __device__ void plan_to(const RoundCtx& c) {
 }
 
 // Places the candidates of overflowing target blocks into per-block segments.
-__global__ void k_bin_moves(RoundCtx c, int sub) {
+// One instance (k <= kBinSmemBlocks): a CTA counts its candidates per block in
+// shared memory and reserves each block's range with one global atomic, so the
+// per-block cursors see one atomic per CTA instead of one per warp. Batches
+// (many blocks) use warp-aggregated atomics.
+constexpr int kBinThreads = 256;
+constexpr int kBinPer = 8;  // list positions per thread
+constexpr int kBinSmemBlocks = 2048;
+
+__global__ void __launch_bounds__(kBinThreads) k_bin_moves(RoundCtx c, int sub) {
   if (c.scal[kAnyOverTo] == 0) return;
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
-  for (int64_t base = beg + (blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane_id());
-       base < end; base += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t pos = base + lane_id();
+  const bool cta = !c.batched && c.k <= kBinSmemBlocks;
+  __shared__ unsigned s_cnt[kBinSmemBlocks];
+  __shared__ unsigned long long s_base[kBinSmemBlocks];
+  const int lane = lane_id();
+  if (cta) {
+    const int k = c.k;
+    for (int64_t r0 = beg + (int64_t)blockIdx.x * kBinThreads * kBinPer; r0 < end;
+         r0 += (int64_t)gridDim.x * kBinThreads * kBinPer) {
+      for (int b = threadIdx.x; b < k; b += blockDim.x) s_cnt[b] = 0;
+      __syncthreads();
+      int grp[kBinPer];
+      unsigned rank[kBinPer];
+      uint64_t key[kBinPer];
+      int w[kBinPer];
+      int4 rv[kBinPer];
+#pragma unroll
+      for (int q = 0; q < kBinPer; ++q) {
+        const int64_t pos = r0 + q * kBinThreads + threadIdx.x;
+        rv[q] = pos < end ? c.rec[pos] : make_int4(-1, 0, 0, 0);
+      }
+#pragma unroll
+      for (int q = 0; q < kBinPer; ++q) {
+        grp[q] = -1;
+        if (rv[q].x >= 0 && c.over_to[rv[q].x]) {
+          grp[q] = rv[q].x;
+          key[q] = move_key(rv[q].y, rv[q].z);
+          w[q] = c.w_v[rv[q].z];
+          rank[q] = atomicAdd(&s_cnt[grp[q]], 1u);
+        }
+      }
+      __syncthreads();
+      for (int b = threadIdx.x; b < k; b += blockDim.x)
+        if (s_cnt[b]) s_base[b] = atomicAdd(reinterpret_cast<ull*>(&c.cursor[b]), (ull)s_cnt[b]);
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < kBinPer; ++q)
+        if (grp[q] >= 0) {
+          const int64_t slot = (int64_t)s_base[grp[q]] + rank[q];
+          c.seg_key[slot] = key[q];
+          c.seg_w[slot] = w[q];
+        }
+      __syncthreads();
+    }
+    return;
+  }
+  for (int64_t base = beg + (blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane); base < end;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pos = base + lane;
     int grp = -1;
     uint64_t key = 0;
     int w = 0;
@@ -1737,8 +1790,7 @@ __global__ void k_bin_moves(RoundCtx c, int sub) {
       const unsigned peers = __match_any_sync(active, grp);
       const int leader = __ffs(peers) - 1;
       int64_t slot0 = 0;
-      if (lane_id() == leader)
-        slot0 = (int64_t)atomicAdd(reinterpret_cast<ull*>(&c.cursor[grp]), (ull)__popc(peers));
+      if (lane == leader) slot0 = (int64_t)atomicAdd(reinterpret_cast<ull*>(&c.cursor[grp]), (ull)__popc(peers));
       slot0 = __shfl_sync(peers, slot0, leader);
       const int64_t slot = slot0 + __popc(peers & lanemask_lt());
       c.seg_key[slot] = key;
@@ -2545,13 +2597,14 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
   // incidence kernels: one wave of resident CTAs striding over the sub-round
   const int g_commit = grid_for(L, n, kFlatItems, occupancy((const void*)k_commit, kFlatThreads, dw_smem));
   const int g_eval = grid_for(L, n, kFlatItems, occupancy((const void*)k_revert_eval, kFlatThreads, 0));
-  const int g_undo = grid_for(L, n, kFlatItems, occupancy((const void*)k_rollback, kFlatThreads, dw_smem));
-  const int g_unrev = (int)std::max<int64_t>(1, std::min<int64_t>((n + 31) / 32, (int64_t)L.num_sms *
-      occupancy((const void*)k_undo_reverts, kFlatThreads, dw_smem)));
-  const int g_bin = grid_for(L, n, 256, occupancy((const void*)k_bin_moves, 256, 0));
+  // undo kernels usually have little to do: one CTA per SM
+  const int g_undo = (int)std::max<int64_t>(1, std::min<int64_t>((n + kFlatItems - 1) / kFlatItems, L.num_sms));
+  const int g_unrev = (int)std::max<int64_t>(1, std::min<int64_t>((n + 31) / 32, L.num_sms));
+  const int g_bin = grid_for(L, n, kBinThreads * (c.batched ? 1 : kBinPer),
+                             occupancy((const void*)k_bin_moves, kBinThreads, 0));
   {
     Scope sc(timer, "select");
-    k_bin_moves<<<g_bin, 256, 0, L.st>>>(c, sub);
+    k_bin_moves<<<g_bin, kBinThreads, 0, L.st>>>(c, sub);
     LAUNCHED("k_bin_moves");
     cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
     cudaFuncSetAttribute(k_from_side, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);

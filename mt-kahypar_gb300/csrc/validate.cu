@@ -87,6 +87,49 @@ __global__ void k_check_nets(int64_t m, int64_t P, const int64_t* __restrict__ n
   }
 }
 
+// One instance: thread per net (offsets, weights, Σ |e|·w(e)) ...
+__global__ void k_check_nets_flat(int64_t m, int64_t P, const int64_t* __restrict__ net_off,
+                                  const int32_t* __restrict__ w_e, int64_t* out) {
+  int64_t gsum = 0;
+  int maxw = 0, nonunit = 0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = net_off[e], b = net_off[e + 1];
+    if (a < 0 || b < a || b > P) {
+      fail(out, kVBadOffsets);
+      continue;
+    }
+    const int we = w_e ? w_e[e] : 1;
+    if (we < 0) {
+      fail(out, kVNegNetWeight);
+      continue;
+    }
+    maxw = max(maxw, we);
+    nonunit |= we != 1;
+    gsum += (b - a) * (int64_t)we;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    gsum += __shfl_xor_sync(FULL, gsum, o);
+    maxw = max(maxw, __shfl_xor_sync(FULL, maxw, o));
+    nonunit |= __shfl_xor_sync(FULL, nonunit, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (gsum) atomicAdd(reinterpret_cast<ull*>(&out[kVSums]), (ull)gsum);
+    if (maxw) atomicMax(reinterpret_cast<unsigned long long*>(&out[kVMaxWe]), (ull)maxw);
+    if (nonunit) atomicOr(reinterpret_cast<ull*>(&out[kVNonUnit]), 1ull);
+  }
+}
+
+// ... and thread per pin (id in [0, n)): no pin read depends on the offsets.
+__global__ void k_check_pins_flat(int64_t P, const int32_t* __restrict__ pins, int64_t n, int64_t* out) {
+  bool bad = false;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < P; q += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t p = pins[q];
+    bad |= p < 0 || p >= n;
+  }
+  if (bad) fail(out, kVPinRange);
+}
+
 // Thread per vertex: w(v) >= 0, the vertex's instance (written to vinst when
 // given, i.e. for every batched session), Σ w(v) per instance (warp sums when
 // the warp's vertices share an instance).
@@ -182,10 +225,15 @@ cudaError_t launch_validate_csr(const Launch& L, int64_t n, int64_t m, int64_t P
                                 int64_t* out) {
   cudaError_t e = cudaMemsetAsync(out, 0, sizeof(int64_t) * (kVSums + 2 * (int64_t)I), L.st);
   if (e != cudaSuccess) return e;
-  if (m > 0) k_check_nets<<<grid(L, m * 32, 256), 256, 0, L.st>>>(m, P, net_off, pins, w_e, I, inst_voff,
-                                                                    inst_noff, n, out);
+  if (I > 1) {
+    if (m > 0) k_check_nets<<<grid(L, m * 32, 256), 256, 0, L.st>>>(m, P, net_off, pins, w_e, I, inst_voff,
+                                                                      inst_noff, n, out);
+  } else {
+    if (m > 0) k_check_nets_flat<<<grid(L, m, 256), 256, 0, L.st>>>(m, P, net_off, w_e, out);
+    if (P > 0) k_check_pins_flat<<<grid(L, P, 256), 256, 0, L.st>>>(P, pins, n, out);
+  }
   if (n > 0) k_check_vertices<<<grid(L, n, 256), 256, 0, L.st>>>(n, w_v, I, inst_voff, vinst, out);
-  add_kernel_launches((m > 0) + (n > 0));
+  add_kernel_launches((m > 0) + (n > 0) + (I == 1 && P > 0));
   return cudaGetLastError();
 }
 
