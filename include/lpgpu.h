@@ -208,6 +208,26 @@ LPGPU_API lpgpu_status lpgpu_session_set_partition_instances(lpgpu_session* s, c
 /* Instance-local blocks of every instance, one output array per instance. */
 LPGPU_API lpgpu_status lpgpu_session_get_partition_instances(lpgpu_session* s, int32_t* const* partitions);
 
+/* ------------------------------------------------------------ files
+ *
+ * hMetis hypergraph files, read as io::readHypergraphFile does
+ * (mt-kahypar/io/hypergraph_io.cpp:95-333; mt_kahypar_read_hypergraph_from_file,
+ * include/libkahypar.h:74-78): '%' comment lines, header "num_nets
+ * num_vertices [type]" (type 1: net weights, 10: vertex weights, 11: both),
+ * one net per line (weight first when present, pins 1-based), nets with fewer
+ * than two pins dropped, then one weight per vertex when present. Returns
+ * 0-based CSR arrays allocated with malloc (release with lpgpu_free) that
+ * lpgpu_session_upload takes as they are; num_removed_single_pin_nets may be NULL. */
+LPGPU_API lpgpu_status lpgpu_read_hgr(const char* path, int64_t* num_vertices, int64_t* num_nets,
+                                      int64_t** net_offsets, int32_t** pins, int32_t** vertex_weights,
+                                      int32_t** net_weights, int64_t* num_removed_single_pin_nets);
+LPGPU_API void lpgpu_free(void* p);
+
+/* Partition files: one block id per line (io::readPartitionFile /
+ * io::writePartitionFile, hypergraph_io.cpp:336-365). */
+LPGPU_API lpgpu_status lpgpu_read_partition(const char* path, int64_t num_vertices, int32_t* partition);
+LPGPU_API lpgpu_status lpgpu_write_partition(const char* path, int64_t num_vertices, const int32_t* partition);
+
 /* Runs the LP refinement on the device-resident state. Replaces
  * IRefiner::refine of LabelPropagationRefiner<Km1Policy>
  * (label_propagation_refiner.cpp:34-68). refinement_nodes (may be NULL with

@@ -79,7 +79,8 @@ SYMBOLS = [
     "lpgpu_host_free", "lpgpu_session_event_record", "lpgpu_session_event_elapsed",
     "lpgpu_session_synchronize", "lpgpu_session_upload_batch", "lpgpu_session_set_partition_batch",
     "lpgpu_session_instance_km1", "lpgpu_partition_metrics_noalloc", "lpgpu_session_upload_instances",
-    "lpgpu_session_set_partition_instances", "lpgpu_session_get_partition_instances",
+    "lpgpu_session_set_partition_instances", "lpgpu_session_get_partition_instances", "lpgpu_read_hgr",
+    "lpgpu_free", "lpgpu_read_partition", "lpgpu_write_partition",
 ]
 
 
@@ -380,6 +381,39 @@ def pinned_copy(a):
     p = PinnedArray(a.shape, a.dtype)
     p.array[...] = a
     return p
+
+
+def read_hgr(path):
+    """Reads an hMetis .hgr file (lpgpu_read_hgr: the reference reader's rules,
+    single-pin nets dropped). Returns (Hypergraph, number of dropped nets)."""
+    from .gen import Hypergraph
+    L = lib()
+    n, m, removed = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    off, pins, vw, ew = I64P(), I32P(), I32P(), I32P()
+    _check(L.lpgpu_read_hgr(os.fsencode(path), ctypes.byref(n), ctypes.byref(m), ctypes.byref(off),
+                            ctypes.byref(pins), ctypes.byref(vw), ctypes.byref(ew), ctypes.byref(removed)))
+    try:
+        nn, mm = n.value, m.value
+        P = off[mm] if mm > 0 else 0
+        hg = Hypergraph(nn, mm, np.ctypeslib.as_array(off, (mm + 1,)).copy(),
+                        np.ctypeslib.as_array(pins, (max(P, 1),))[:P].copy(),
+                        np.ctypeslib.as_array(vw, (max(nn, 1),))[:nn].copy(),
+                        np.ctypeslib.as_array(ew, (max(mm, 1),))[:mm].copy())
+    finally:
+        for ptr in (off, pins, vw, ew):
+            L.lpgpu_free(ptr)
+    return hg, removed.value
+
+
+def read_partition(path, n):
+    out = np.empty(n, np.int32)
+    _check(lib().lpgpu_read_partition(os.fsencode(path), ctypes.c_int64(n), _p(out, I32P)))
+    return out
+
+
+def write_partition(path, part):
+    p = np.ascontiguousarray(part, np.int32)
+    _check(lib().lpgpu_write_partition(os.fsencode(path), ctypes.c_int64(len(p)), _p(p, I32P)))
 
 
 def kernel_launches():
