@@ -281,6 +281,18 @@ LPGPU_API lpgpu_status lpgpu_session_best_moves(lpgpu_session* s, int32_t* to, i
 LPGPU_API lpgpu_status lpgpu_session_gain_cache(lpgpu_session* s, int32_t* benefit,
                                                 int32_t* penalty);
 
+/* Device-resident gain cache (initializeGainCache, partitioned_hypergraph.h:707-809)
+ * kept up to date by lpgpu_session_apply_moves with the transition rules of
+ * gainCacheUpdate (h:1017-1047, as in changeNodePartWithGainCacheUpdate,
+ * h:574-590): moveToPenalty of every pin changes when Φ(e, b) reaches or leaves
+ * 0, moveFromBenefit of the non-moving pins in b when it reaches or leaves 1,
+ * and the moved vertices' benefits are recounted on the final state. The
+ * maintained cache equals a recomputation from scratch whatever the order of
+ * the concurrent moves. lpgpu_session_gain_cache then copies it out; refine,
+ * set_partition, restore_partition and upload drop it. */
+LPGPU_API lpgpu_status lpgpu_session_init_gain_cache(lpgpu_session* s);
+LPGPU_API lpgpu_status lpgpu_session_drop_gain_cache(lpgpu_session* s);
+
 /* Applies `count` moves concurrently on the device without balance checks,
  * the curried PartitionedHypergraph::changeNodePart (h:566-572) with its
  * updatePinCountOfHyperedge / km1Delta attribution (h:1133-1167,

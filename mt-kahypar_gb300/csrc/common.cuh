@@ -170,8 +170,14 @@ cudaError_t launch_best_moves(const Launch& L, const RoundCtx& c, int32_t* to, i
                               uint8_t* border);
 cudaError_t launch_gain_cache(const Launch& L, const RoundCtx& c, int32_t* benefit,
                               int32_t* penalty);
+// Device-resident gain cache maintained by apply_moves (all null: none).
+struct GainCache {
+  int32_t* benefit;  // n: moveFromBenefit
+  int32_t* penalty;  // n x k: moveToPenalty
+  uint8_t* moved;    // n: zero outside apply_moves
+};
 cudaError_t launch_apply_moves(const Launch& L, const RoundCtx& c, int64_t count,
-                               const int32_t* v, const int32_t* from, const int32_t* to);
+                               const int32_t* v, const int32_t* from, const int32_t* to, const GainCache& g);
 
 // Device-side input checks (validate.cu). `out` holds kVSums + 2 I words;
 // `inst_voff`, `inst_noff` are read when I > 1; `vinst` (batched sessions,

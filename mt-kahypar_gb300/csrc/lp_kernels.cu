@@ -1372,7 +1372,24 @@ cudaError_t launch_gain_cache(const Launch& L, const RoundCtx& c, int32_t* benef
 // hypergraph_common.h:133-140): -w(e) when Φ(e,f) drops to 0, +w(e) when
 // Φ(e,t) rises to 1. The per-move split depends on interleaving; the sum over
 // all concurrent moves is exactly the km1 change.
-__device__ __forceinline__ int64_t warp_commit_vertex(const RoundCtx& c, int64_t v, int f, int t) {
+// Gain-cache maintenance for one flip of net e in block b (gainCacheUpdate,
+// partitioned_hypergraph.h:1017-1047, stated on the transitions an atomic
+// observed): `one` = +1 / -1 when Φ(e, b) reaches / leaves 1, `zero` = +1 / -1
+// when Φ(e, b) reaches / leaves 0. moveToPenalty(u, b) (the weight of u's nets
+// without b) changes with `zero` for every pin; moveFromBenefit(u) changes with
+// `one` for the pins in block b that are not moving in this batch (moving
+// vertices are recomputed afterwards).
+__device__ __forceinline__ void gc_flip(const RoundCtx& c, const GainCache& g, int64_t e, int b, int one, int zero,
+                                        int we) {
+  if (!one && !zero) return;
+  for (int64_t q = c.net_off[e]; q < c.net_off[e + 1]; ++q) {
+    const int u = c.pins[q];
+    if (zero) atomicAdd(&g.penalty[(int64_t)u * c.k + b], zero * we);
+    if (one && !g.moved[u] && c.part[u] == b) atomicAdd(&g.benefit[u], one * we);
+  }
+}
+
+__device__ __forceinline__ int64_t warp_commit_vertex(const RoundCtx& c, int64_t v, int f, int t, const GainCache& g) {
   int64_t att = 0;
   const int k = c.kmax, W = c.W;
   const uint32_t fbit = 1u << (f & 31), tbit = 1u << (t & 31);
@@ -1392,19 +1409,24 @@ __device__ __forceinline__ int64_t warp_commit_vertex(const RoundCtx& c, int64_t
       att += we;
     }
     if (ot == 0 || ot == 1) atomicXor(&rec[W + (t >> 5)], tbit);
+    if (g.benefit) {
+      // f: of -> of - 1; t: ot -> ot + 1
+      gc_flip(c, g, e, f, of == 2 ? 1 : (of == 1 ? -1 : 0), of == 1 ? 1 : 0, we);
+      gc_flip(c, g, e, t, ot == 0 ? 1 : (ot == 1 ? -1 : 0), ot == 0 ? -1 : 0, we);
+    }
   }
   return att;
 }
 
 // Concurrent application of an explicit move list (lpgpu_session_apply_moves).
 __global__ void k_apply_moves(RoundCtx c, int64_t count, const int32_t* __restrict__ vs,
-                              const int32_t* __restrict__ fs, const int32_t* __restrict__ ts) {
+                              const int32_t* __restrict__ fs, const int32_t* __restrict__ ts, GainCache g) {
   int64_t att = 0;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < count; i += warps) {
     const int64_t v = vs[i];
     const int f = fs[i], t = ts[i];
-    att += warp_commit_vertex(c, v, f, t);
+    att += warp_commit_vertex(c, v, f, t, g);
     if (lane_id() == 0) {
       c.part[v] = t;
       const int64_t wv = c.w_v[v];
@@ -1416,13 +1438,46 @@ __global__ void k_apply_moves(RoundCtx c, int64_t count, const int32_t* __restri
   if (threadIdx.x == 0) atomicAdd(reinterpret_cast<ull*>(&c.scal[kApplyDelta]), (ull)att);
 }
 
+__global__ void k_mark_moved(int64_t count, const int32_t* __restrict__ vs, uint8_t* moved, uint8_t value) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    moved[vs[i]] = value;
+}
+
+// moveFromBenefit of the moved vertices on the final state: Σ w(e) over
+// their nets with Φ(e, part(v)) = 1 (warp per vertex).
+__global__ void k_gc_moved_benefit(RoundCtx c, int64_t count, const int32_t* __restrict__ vs, int32_t* benefit) {
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < count; i += warps) {
+    const int64_t v = vs[i];
+    const int pv = c.part[v];
+    int ben = 0;
+    for (int64_t j = c.vtx_off[v] + lane_id(); j < c.vtx_off[v + 1]; j += 32) {
+      const int64_t e = c.inets[j];
+      if (c.phi[e * c.kmax + pv] == 1) ben += c.w_e[e];
+    }
+    ben = warp_sum(ben);
+    if (lane_id() == 0) benefit[v] = ben;
+  }
+}
+
 cudaError_t launch_apply_moves(const Launch& L, const RoundCtx& c, int64_t count, const int32_t* v,
-                               const int32_t* from, const int32_t* to) {
+                               const int32_t* from, const int32_t* to, const GainCache& g) {
   cudaError_t e = cudaMemsetAsync(c.scal + kApplyDelta, 0, sizeof(int64_t), L.st);
   if (e != cudaSuccess) return e;
   if (count > 0) {
-    k_apply_moves<<<grid_for(L, count * 32, 256), 256, 0, L.st>>>(c, count, v, from, to);
+    const int gm = grid_for(L, count, 256);
+    if (g.benefit) {
+      k_mark_moved<<<gm, 256, 0, L.st>>>(count, v, g.moved, 1);
+      LAUNCHED("k_mark_moved");
+    }
+    k_apply_moves<<<grid_for(L, count * 32, 256), 256, 0, L.st>>>(c, count, v, from, to, g);
     LAUNCHED("k_apply_moves");
+    if (g.benefit) {
+      k_gc_moved_benefit<<<grid_for(L, count * 32, 256), 256, 0, L.st>>>(c, count, v, g.benefit);
+      LAUNCHED("k_gc_moved_benefit");
+      k_mark_moved<<<gm, 256, 0, L.st>>>(count, v, g.moved, 0);
+      LAUNCHED("k_mark_moved");
+    }
   }
   return cudaGetLastError();
 }

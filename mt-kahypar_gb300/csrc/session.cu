@@ -102,6 +102,16 @@ struct lpgpu_session_s {
   DevBuf<int4> rec;
   DevBuf<uint64_t> seg_key, thr;
   DevBuf<int32_t> saved_part;
+  // gain cache kept by apply_moves (lpgpu_session_init_gain_cache)
+  bool gc_valid = false;
+  DevBuf<int32_t> gc_benefit, gc_penalty;
+  DevBuf<uint8_t> gc_moved;
+  void drop_gain_cache() {
+    gc_valid = false;
+    gc_benefit.release(&footprint);
+    gc_penalty.release(&footprint);
+    gc_moved.release(&footprint);
+  }
   int64_t scan_tmp_n = 0;
   // batched sessions (lpgpu_session_upload_batch): instance ranges and blocks
   bool batched = false;
@@ -195,6 +205,7 @@ struct lpgpu_session_s {
   }
 
   void release_partition() {
+    drop_gain_cache();
     part.release(&footprint);
     phi.release(&footprint);
     conn.release(&footprint);
@@ -364,6 +375,7 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
   // buffers of the same size are reused; the partition must be set again
   s->has_part = false;
   s->has_hg = false;
+  s->drop_gain_cache();
   s->n = n;
   s->m = m;
   s->P = P;
@@ -546,6 +558,7 @@ static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax
   DeviceGuard g(s->device);
   CK(cudaStreamSynchronize(s->st));
   s->has_part = false;
+  s->drop_gain_cache();
   s->k = K;
   s->kmax = kmax;
   s->W = word_class_of(kmax);
@@ -716,6 +729,7 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
   for (int64_t i = 0; i < num_nodes; ++i)
     if (nodes[i] < 0 || nodes[i] >= s->n) return invalid("refinement node out of range");
   DeviceGuard g(s->device);
+  s->gc_valid = false;  // refinement moves without gain-cache maintenance
   const int R = cfg.rounds, S = cfg.subrounds;
   int64_t* fp = &s->footprint;
   CK(s->stats.alloc(std::max(1, R) * kStats, fp));
@@ -1018,17 +1032,50 @@ lpgpu_status lpgpu_session_gain_cache(lpgpu_session* s, int32_t* benefit, int32_
   DeviceGuard g(s->device);
   int64_t fp = 0;
   DevBuf<int32_t> db, dp;
-  CK(db.alloc(s->n, &fp));
-  CK(dp.alloc((size_t)s->n * s->k, &fp));
-  RoundCtx c = s->ctx();
-  CK(launch_gain_cache(s->launch(), c, db.p, dp.p));
+  const int32_t *sb = s->gc_benefit.p, *sp = s->gc_penalty.p;
+  if (!s->gc_valid) {  // computed for this call
+    CK(db.alloc(s->n, &fp));
+    CK(dp.alloc((size_t)s->n * s->k, &fp));
+    RoundCtx c = s->ctx();
+    CK(launch_gain_cache(s->launch(), c, db.p, dp.p));
+    sb = db.p;
+    sp = dp.p;
+  }
   if (s->n > 0) {
-    if (benefit) CK(cudaMemcpyAsync(benefit, db.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
-    if (penalty) CK(cudaMemcpyAsync(penalty, dp.p, sizeof(int32_t) * s->n * s->k, cudaMemcpyDeviceToHost, s->st));
+    if (benefit) CK(cudaMemcpyAsync(benefit, sb, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
+    if (penalty) CK(cudaMemcpyAsync(penalty, sp, sizeof(int32_t) * s->n * s->k, cudaMemcpyDeviceToHost, s->st));
   }
   CK(cudaStreamSynchronize(s->st));
   db.release(&fp);
   dp.release(&fp);
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_init_gain_cache(lpgpu_session* s) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  if (s->batched) {
+    set_error("this call needs a single-instance session");
+    return LPGPU_ERR_STATE;
+  }
+  DeviceGuard g(s->device);
+  int64_t* fp = &s->footprint;
+  CK(s->gc_benefit.alloc(s->n, fp));
+  CK(s->gc_penalty.alloc((size_t)s->n * s->k, fp));
+  CK(s->gc_moved.alloc(s->n, fp));
+  if (s->n > 0) CK(cudaMemsetAsync(s->gc_moved.p, 0, s->n, s->st));
+  RoundCtx c = s->ctx();
+  CK(launch_gain_cache(s->launch(), c, s->gc_benefit.p, s->gc_penalty.p));
+  CK(cudaStreamSynchronize(s->st));
+  s->gc_valid = true;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_drop_gain_cache(lpgpu_session* s) {
+  if (!s) return invalid("null session");
+  DeviceGuard g(s->device);
+  CK(cudaStreamSynchronize(s->st));
+  s->drop_gain_cache();
   return LPGPU_OK;
 }
 
@@ -1067,7 +1114,9 @@ lpgpu_status lpgpu_session_apply_moves(lpgpu_session* s, int64_t count, const in
     CK(cudaMemcpyAsync(dt.p, ts, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s->st));
   }
   RoundCtx c = s->ctx();
-  CK(launch_apply_moves(s->launch(), c, count, dv.p, df.p, dt.p));
+  GainCache gc{nullptr, nullptr, nullptr};
+  if (s->gc_valid) gc = GainCache{s->gc_benefit.p, s->gc_penalty.p, s->gc_moved.p};
+  CK(launch_apply_moves(s->launch(), c, count, dv.p, df.p, dt.p, gc));
   int64_t d = 0;
   CK(cudaMemcpyAsync(&d, s->scal.p + kApplyDelta, sizeof(int64_t), cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
@@ -1117,6 +1166,7 @@ lpgpu_status lpgpu_session_restore_partition(lpgpu_session* s) {
     return LPGPU_ERR_STATE;
   }
   DeviceGuard g(s->device);
+  s->gc_valid = false;
   if (s->n > 0)
     CK(cudaMemcpyAsync(s->part.p, s->saved_part.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToDevice, s->st));
   RoundCtx c = s->ctx();

@@ -80,7 +80,8 @@ SYMBOLS = [
     "lpgpu_session_synchronize", "lpgpu_session_upload_batch", "lpgpu_session_set_partition_batch",
     "lpgpu_session_instance_km1", "lpgpu_partition_metrics_noalloc", "lpgpu_session_upload_instances",
     "lpgpu_session_set_partition_instances", "lpgpu_session_get_partition_instances", "lpgpu_read_hgr",
-    "lpgpu_free", "lpgpu_read_partition", "lpgpu_write_partition",
+    "lpgpu_free", "lpgpu_read_partition", "lpgpu_write_partition", "lpgpu_session_init_gain_cache",
+    "lpgpu_session_drop_gain_cache",
 ]
 
 
@@ -299,6 +300,15 @@ class Session:
         p = np.empty(self.n * self.k, np.int32)
         _check(lib().lpgpu_session_gain_cache(self._h, _p(b, I32P), _p(p, I32P)))
         return b, p.reshape(self.n, self.k)
+
+    def init_gain_cache(self):
+        """Keeps a device gain cache that apply_moves maintains."""
+        _check(lib().lpgpu_session_init_gain_cache(self._h))
+        return self
+
+    def drop_gain_cache(self):
+        _check(lib().lpgpu_session_drop_gain_cache(self._h))
+        return self
 
     def apply_moves(self, vertices, from_, to):
         v = np.ascontiguousarray(vertices, np.int32)

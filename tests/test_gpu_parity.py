@@ -340,3 +340,32 @@ def test_one_shot_entry_point(lp, orc):
                           subrounds=8, revert=1, rollback=1, zero_gain=1)
     assert np.array_equal(p, ep)
     assert r.km1_after == r.km1_before + r.delta and r.km1_after < r.km1_before
+
+
+@pytest.mark.parametrize("seed", range(3))
+@pytest.mark.parametrize("k,weighted", [(2, True), (7, False), (33, True), (128, True)])
+def test_maintained_gain_cache_equals_recomputation(lp, orc, seed, k, weighted):
+    """The device gain cache kept by apply_moves (gainCacheUpdate rules, many
+    concurrent moves per batch) equals initializeGainCache on the final state."""
+    from lpgpu import gen
+    inst = gen.random_small(seed, n=400, m=480, k=k, max_size=10, weighted=weighted, hubs=2)
+    hg = inst.hg
+    rng = np.random.default_rng([seed, k])
+    s = session(lp, hg, k, inst.part, lmax=inst.lmax, perfect=inst.perfect)
+    s.init_gain_cache()
+    part = inst.part.copy()
+    for batch in range(4):
+        vs = rng.choice(hg.n, size=int(rng.integers(1, 120)), replace=False).astype(np.int32)
+        to = ((part[vs] + rng.integers(1, k, size=len(vs))) % k).astype(np.int32) if k > 1 else part[vs]
+        s.apply_moves(vs, part[vs], to)
+        part[vs] = to
+        ben, pen = s.gain_cache()
+        eben, epen = orc.gain_cache(hg, k, part)
+        assert np.array_equal(ben, eben), f"benefit, batch {batch}"
+        assert np.array_equal(pen, epen), f"penalty, batch {batch}"
+    check_state(orc, s, hg, k, part)
+    s.refine(lp.default_config(rounds=2, subrounds=2))  # drops the maintained cache
+    ben, pen = s.gain_cache()
+    eben, epen = orc.gain_cache(hg, k, s.partition())
+    assert np.array_equal(ben, eben) and np.array_equal(pen, epen)
+    s.close()
