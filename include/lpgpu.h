@@ -281,6 +281,16 @@ LPGPU_API lpgpu_status lpgpu_session_best_moves(lpgpu_session* s, int32_t* to, i
 LPGPU_API lpgpu_status lpgpu_session_gain_cache(lpgpu_session* s, int32_t* benefit,
                                                 int32_t* penalty);
 
+/* Uncoarsening step (uncoarsening.cpp:111-122: setOnlyNodePart of every fine
+ * vertex from its coarse representative, then initializePartition,
+ * partitioned_hypergraph.h:522-526, 693-698), device to device: the partition
+ * of `fine` becomes part[v] = part_coarse[fine_to_coarse[v]] with the coarse
+ * session's k and block bounds, and its Φ, Λ and block weights are built. Both
+ * sessions are single-instance and on the same device; `fine` holds the fine
+ * hypergraph, `coarse` a partition. */
+LPGPU_API lpgpu_status lpgpu_session_project_partition(lpgpu_session* fine, const lpgpu_session* coarse,
+                                                       const int32_t* fine_to_coarse);
+
 /* Device-resident gain cache (initializeGainCache, partitioned_hypergraph.h:707-809)
  * kept up to date by lpgpu_session_apply_moves with the transition rules of
  * gainCacheUpdate (h:1017-1047, as in changeNodePartWithGainCacheUpdate,

@@ -554,7 +554,7 @@ lpgpu_status lpgpu_session_upload_batch(lpgpu_session* s, int32_t num_instances,
 // local ids per instance for a batch (turned into global ids on the device).
 static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax, const int32_t* part,
                                        const std::vector<int64_t>& hl, const std::vector<int64_t>& hp,
-                                       const int32_t* const* parts = nullptr) {
+                                       const int32_t* const* parts = nullptr, const int32_t* part_dev = nullptr) {
   DeviceGuard g(s->device);
   CK(cudaStreamSynchronize(s->st));
   s->has_part = false;
@@ -583,7 +583,9 @@ static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax
     CK(cudaMemcpyAsync(s->inst_k.p, s->h_inst_k.data(), sizeof(int32_t) * s->num_inst, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(s->inst_delta.p, 0, sizeof(int64_t) * s->num_inst, st));
   }
-  if (parts) {
+  if (part_dev) {
+    if (s->n > 0) CK(cudaMemcpyAsync(s->part.p, part_dev, sizeof(int32_t) * s->n, cudaMemcpyDeviceToDevice, st));
+  } else if (parts) {
     for (int32_t i = 0; i < s->num_inst; ++i) {
       const int64_t v0 = s->h_inst_voff[i], ni = s->h_inst_voff[i + 1] - v0;
       if (ni > 0) CK(cudaMemcpyAsync(s->part.p + v0, parts[i], sizeof(int32_t) * ni, cudaMemcpyHostToDevice, st));
@@ -684,6 +686,44 @@ lpgpu_status lpgpu_session_set_partition(lpgpu_session* s, int32_t k, double eps
     if (hp[b] < 1) hp[b] = 1;
   }
   return set_partition_impl(s, k, k, partition, hl, hp);
+}
+
+lpgpu_status lpgpu_session_project_partition(lpgpu_session* fine, const lpgpu_session* coarse,
+                                             const int32_t* fine_to_coarse) {
+  if (!fine || !coarse) return invalid("null session");
+  if (!fine->has_hg || fine->batched) {
+    set_error("project_partition needs a single-instance fine session with a hypergraph");
+    return LPGPU_ERR_STATE;
+  }
+  if (!coarse->has_part || coarse->batched) {
+    set_error("project_partition needs a single-instance coarse session with a partition");
+    return LPGPU_ERR_STATE;
+  }
+  if (coarse->device != fine->device) return invalid("both sessions must live on the same device");
+  if (fine->n > 0 && !fine_to_coarse) return invalid("null fine-to-coarse map");
+  DeviceGuard g(fine->device);
+  CK(cudaStreamSynchronize(coarse->st));
+  int64_t fp = 0;
+  DevBuf<int32_t> map, proj;
+  DevBuf<int64_t> verdict;
+  CK(map.alloc(fine->n, &fp));
+  CK(proj.alloc(fine->n, &fp));
+  CK(verdict.alloc(1, &fp));
+  if (fine->n > 0)
+    CK(cudaMemcpyAsync(map.p, fine_to_coarse, sizeof(int32_t) * fine->n, cudaMemcpyHostToDevice, fine->st));
+  CK(launch_project(fine->launch(), fine->n, map.p, coarse->part.p, coarse->n, proj.p, verdict.p));
+  int64_t bad = 0;
+  std::vector<int64_t> hl(coarse->k);
+  CK(cudaMemcpyAsync(&bad, verdict.p, sizeof(int64_t), cudaMemcpyDeviceToHost, fine->st));
+  CK(cudaMemcpyAsync(hl.data(), coarse->lmax.p, sizeof(int64_t) * coarse->k, cudaMemcpyDeviceToHost, fine->st));
+  CK(cudaStreamSynchronize(fine->st));
+  if (bad) return invalid("fine-to-coarse map entry outside the coarse vertices");
+  const std::vector<int64_t> hp = coarse->h_perfect;
+  const lpgpu_status st = set_partition_impl(fine, coarse->k, coarse->k, nullptr, hl, hp, nullptr, proj.p);
+  map.release(&fp);
+  proj.release(&fp);
+  verdict.release(&fp);
+  return st;
 }
 
 static lpgpu_status read_metrics(lpgpu_session* s, int64_t* km1, int64_t* cut) {

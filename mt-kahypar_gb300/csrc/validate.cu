@@ -212,6 +212,20 @@ __global__ void k_local_blocks(int64_t n, const int32_t* __restrict__ part, cons
     out[v] = part[v] - inst_boff[vinst[v]];
 }
 
+// part[v] = coarse_part[map[v]]; map entries outside [0, nc) set the verdict.
+__global__ void k_project(int64_t n, const int32_t* __restrict__ map, const int32_t* __restrict__ coarse_part,
+                          int64_t nc, int32_t* __restrict__ part, int64_t* verdict) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t u = map[v];
+    if (u < 0 || u >= nc) {
+      atomicCAS(reinterpret_cast<ull*>(verdict), 0ull, 1ull);
+      part[v] = 0;
+    } else {
+      part[v] = coarse_part[u];
+    }
+  }
+}
+
 int grid(const Launch& L, int64_t items, int threads) {
   const int64_t need = (items + threads - 1) / threads;
   return (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)L.num_sms * 8));
@@ -269,6 +283,17 @@ cudaError_t launch_local_blocks(const Launch& L, int64_t n, const int32_t* part,
                                 const int32_t* inst_boff, int32_t* out) {
   if (n > 0) {
     k_local_blocks<<<grid(L, n, 256), 256, 0, L.st>>>(n, part, vinst, inst_boff, out);
+    add_kernel_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_project(const Launch& L, int64_t n, const int32_t* map, const int32_t* coarse_part, int64_t nc,
+                           int32_t* part, int64_t* verdict) {
+  cudaError_t e = cudaMemsetAsync(verdict, 0, sizeof(int64_t), L.st);
+  if (e != cudaSuccess) return e;
+  if (n > 0) {
+    k_project<<<grid(L, n, 256), 256, 0, L.st>>>(n, map, coarse_part, nc, part, verdict);
     add_kernel_launches(1);
   }
   return cudaGetLastError();

@@ -369,3 +369,61 @@ def test_maintained_gain_cache_equals_recomputation(lp, orc, seed, k, weighted):
     eben, epen = orc.gain_cache(hg, k, s.partition())
     assert np.array_equal(ben, eben) and np.array_equal(pen, epen)
     s.close()
+
+
+def _contract_pairs(hg, rng):
+    """A coarse hypergraph from a random matching of vertex pairs: coarse nets are
+    the fine nets with pins mapped and duplicates removed; nets left with one pin
+    are dropped, parallel nets kept (weights as in the fine nets)."""
+    from lpgpu import gen
+    perm = rng.permutation(hg.n)
+    cmap = np.empty(hg.n, np.int32)
+    cmap[perm] = np.arange(hg.n) // 2
+    nc = (hg.n + 1) // 2
+    off, pins, we = [0], [], []
+    for e in range(hg.m):
+        p = np.unique(cmap[hg.pins[hg.net_off[e]:hg.net_off[e + 1]]])
+        if len(p) < 2:
+            continue
+        pins.extend(p.tolist())
+        off.append(len(pins))
+        we.append(hg.w_e[e])
+    w_v = np.zeros(nc, np.int32)
+    np.add.at(w_v, cmap, hg.w_v)
+    coarse = gen.Hypergraph(nc, len(we), np.array(off, np.int64), np.array(pins, np.int32), w_v,
+                            np.array(we, np.int32)).with_incidence()
+    return coarse, cmap
+
+
+@pytest.mark.parametrize("seed", range(3))
+@pytest.mark.parametrize("k", [2, 8, 64])
+def test_projection_between_levels(lp, orc, seed, k):
+    """Coarse refine, then device-to-device projection to the fine level: the fine
+    partition is coarse_part[map], with the coarse bounds and a fresh state."""
+    from lpgpu import gen
+    rng = np.random.default_rng([seed, k, 5])
+    inst = gen.random_small(seed, n=600, m=700, k=k, max_size=8)
+    coarse, cmap = _contract_pairs(inst.hg, rng)
+    cpart = gen.random_balanced_partition(coarse.n, k, rng)
+    perfect, lmax = gen.part_weights(int(coarse.w_v.sum()), k, 0.1)
+    with lp.Session(0) as c, lp.Session(0) as f:
+        c.upload(coarse)
+        c.set_partition(k, cpart, lmax=lmax, perfect=perfect)
+        c.refine(lp.default_config(rounds=3, subrounds=4))
+        cp = c.partition()
+        f.upload(inst.hg)
+        f.project_partition(c, cmap)
+        fp = f.partition()
+        assert np.array_equal(fp, cp[cmap])
+        check_state(orc, f, inst.hg, k, fp)
+        # the fine level refines from there as usual (against the oracle)
+        r = f.refine(lp.default_config(rounds=3, subrounds=4))
+        ref, _ = orc.lp_sync(inst.hg, k, lmax, fp, perfect=perfect, rounds=3, subrounds=4, revert=1,
+                             rollback=1, zero_gain=1)
+        assert np.array_equal(f.partition(), ref)
+        assert r.km1_after == r.km1_before + r.delta
+        bad = cmap.copy()
+        bad[5] = coarse.n
+        with pytest.raises(lp.LpgpuError) as e:
+            f.project_partition(c, bad)
+        assert e.value.status == lp.ERR_INVALID_ARG
