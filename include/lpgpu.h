@@ -291,6 +291,20 @@ LPGPU_API lpgpu_status lpgpu_session_gain_cache(lpgpu_session* s, int32_t* benef
 LPGPU_API lpgpu_status lpgpu_session_project_partition(lpgpu_session* fine, const lpgpu_session* coarse,
                                                        const int32_t* fine_to_coarse);
 
+/* Rebalancer (Rebalancer::rebalance, rebalancing/rebalancer.cpp:34-171) in a
+ * deterministic synchronous form. Per round, while some block is above its max
+ * weight: every border vertex of an overloaded block takes its Km1Policy best
+ * move with rebalance = true (the feasible block of minimum score, any sign,
+ * lowest id on ties); per overloaded block all non-worsening candidates are
+ * taken and worsening ones, in (score, vertex id) order, only while the weight
+ * taken is below the block's excess; the taken moves then go through the LP
+ * selection (target-side prefix within L_max, source blocks kept non-empty)
+ * and are committed. Stops when balanced, after max_rounds, or when a round
+ * moves nothing; lpgpu_session_round_stats gives the rounds (active =
+ * vertices in overloaded blocks). The reference's empty-block repair
+ * (repairEmptyBlocks) is not part of it. */
+LPGPU_API lpgpu_status lpgpu_session_rebalance(lpgpu_session* s, int32_t max_rounds, lpgpu_result* result);
+
 /* Device-resident gain cache (initializeGainCache, partitioned_hypergraph.h:707-809)
  * kept up to date by lpgpu_session_apply_moves with the transition rules of
  * gainCacheUpdate (h:1017-1047, as in changeNodePartWithGainCacheUpdate,

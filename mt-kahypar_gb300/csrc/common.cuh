@@ -218,6 +218,12 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
 // stamped nets into the next round's active set.
 cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, int S, PhaseTimer* timer);
 
+// One round of the deterministic rebalancer on a single-instance session
+// whose list is the identity over all vertices (sub_off = {0, n}). rb_to /
+// rb_score: n-entry scratch; rb: 5k + 1 int64 scratch.
+cudaError_t launch_rebalance_round(const Launch& L, const RoundCtx& c, int round, int32_t* rb_to,
+                                   int32_t* rb_score, int64_t* rb);
+
 // Optional per-phase CUDA-event timing.
 struct PhaseTimer {
   struct Rec {

@@ -2639,6 +2639,219 @@ cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, int S, PhaseT
   return cudaSuccess;
 }
 
+// ============================================================= rebalancer
+//
+// One round of the deterministic rebalancer (lpgpu_session_rebalance, the
+// synchronous restatement of Rebalancer::rebalance,
+// rebalancing/rebalancer.cpp:34-171). The list is the identity over all
+// vertices and the LP selection and commit run unchanged after it.
+// Per-block scratch rb: W0 [0, k) (weight of non-worsening candidates), count
+// of worsening ones [k, 2k), need [2k, 3k), segment offsets [3k, 4k + 1),
+// thresholds [4k + 1, 5k + 1).
+
+// Best move with rebalance = true of every border vertex of an overloaded
+// block (Km1Policy::computeMaxGainMoveImpl, gain_policy.h:108-167): minimum
+// score over feasible blocks, any sign, lowest id on ties. Warp per vertex,
+// penalties summed per block in shared memory.
+__global__ void __launch_bounds__(256) k_rb_candidates(RoundCtx c, int round, int32_t* __restrict__ rb_to,
+                                                       int32_t* __restrict__ rb_score, int64_t* __restrict__ rb) {
+  extern __shared__ int s_rbagg[];
+  const int k = c.k, W = c.W, lane = lane_id();
+  int* agg = s_rbagg + (threadIdx.x >> 5) * k;
+  for (int b = lane; b < k; b += 32) agg[b] = 0;
+  __syncwarp();
+  int64_t active = 0, pins = 0, cands = 0;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; v < c.n; v += warps) {
+    const int from = c.part[v];
+    if (c.bw[from] <= c.lmax[from]) {
+      if (lane == 0) rb_to[v] = -1;
+      continue;
+    }
+    const int64_t o0 = c.vtx_off[v], o1 = c.vtx_off[v + 1];
+    ++active;
+    pins += o1 - o0;
+    int internal = 0;
+    bool border = false;
+    if (o1 - o0 <= kHighDegree) {  // isBorderNode is false above the threshold
+      for (int64_t j = o0 + lane; j < o1; j += 32) {
+        const int64_t e = c.inets[j];
+        const int we = c.w_e[e];
+        const uint32_t* rec = c.conn + e * 2 * W;
+        if (!((rec[W + (from >> 5)] >> (from & 31)) & 1u)) internal += we;  // Φ(e, from) > 1
+        int lam = 0;
+        for (int w = 0; w < W; ++w) {
+          uint32_t bits = rec[w];
+          lam += __popc(bits);
+          while (bits) {
+            const int b = 32 * w + __ffs(bits) - 1;
+            bits &= bits - 1;
+            if (b != from) atomicAdd(&agg[b], we);
+          }
+        }
+        border = border || lam > 1;
+      }
+    }
+    internal = warp_sum(internal);
+    border = __any_sync(FULLMASK, border);
+    __syncwarp();
+    const int64_t wv = c.w_v[v];
+    unsigned long long best = ~0ull;
+    for (int b = lane; b < k; b += 32) {
+      if (border && b != from && c.bw[b] + wv <= c.lmax[b]) {
+        const int sc = internal - agg[b];
+        const unsigned long long key = ((unsigned long long)((uint32_t)sc ^ 0x80000000u) << 32) | (uint32_t)b;
+        best = key < best ? key : best;
+      }
+      agg[b] = 0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long y = __shfl_xor_sync(FULLMASK, best, o);
+      best = y < best ? y : best;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      if (best == ~0ull) {
+        rb_to[v] = -1;
+      } else {
+        const int sc = (int)((uint32_t)(best >> 32) ^ 0x80000000u);
+        rb_to[v] = (int)(best & 0xffffffffu);
+        rb_score[v] = sc;
+        if (sc <= 0)
+          atomicAdd(reinterpret_cast<ull*>(&rb[from]), (ull)wv);
+        else
+          atomicAdd(reinterpret_cast<ull*>(&rb[k + from]), 1ull);
+        ++cands;
+      }
+    }
+  }
+  if (lane == 0) {
+    int64_t* st = c.stats + (int64_t)round * kStats;
+    if (active) atomicAdd(reinterpret_cast<ull*>(&st[kStActive]), (ull)active);
+    if (pins) atomicAdd(reinterpret_cast<ull*>(&st[kStPins]), (ull)pins);
+    if (cands) atomicAdd(reinterpret_cast<ull*>(&st[kStCands]), (ull)cands);
+  }
+}
+
+// Need of every overloaded block beyond its non-worsening candidates, and
+// segments for its worsening candidates (one CTA).
+__global__ void k_rb_src_plan(RoundCtx c, int64_t* rb) {
+  const int k = c.k;
+  __shared__ int64_t s_run;
+  if (threadIdx.x == 0) s_run = 0;
+  __syncthreads();
+  for (int b0 = 0; b0 < k; b0 += blockDim.x) {
+    const int b = b0 + threadIdx.x;
+    int64_t cnt = 0;
+    if (b < k) {
+      const int64_t x = c.bw[b] - c.lmax[b];
+      const int64_t need = x > 0 ? x - rb[b] : 0;
+      rb[2 * k + b] = need;
+      cnt = need > 0 ? rb[k + b] : 0;
+    }
+    int64_t total;
+    const int64_t off = block_scan_excl_i64(cnt, &total) + s_run;
+    if (b < k) {
+      rb[3 * k + b] = off;
+      c.cursor[b] = off;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_run += total;
+    __syncthreads();
+  }
+}
+
+__global__ void k_rb_src_bin(RoundCtx c, const int32_t* __restrict__ rb_to, const int32_t* __restrict__ rb_score,
+                             const int64_t* __restrict__ rb) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < c.n; v += (int64_t)gridDim.x * blockDim.x) {
+    if (rb_to[v] < 0 || rb_score[v] <= 0) continue;
+    const int from = c.part[v];
+    if (rb[2 * c.k + from] <= 0) continue;
+    const ull slot = atomicAdd(reinterpret_cast<ull*>(&c.cursor[from]), 1ull);
+    c.seg_key[slot] = move_key(rb_score[v], (int32_t)v);
+    c.seg_w[slot] = c.w_v[v];
+  }
+}
+
+// Per block with a need: the first worsening key whose weighted prefix
+// reaches the need (keys up to it are taken).
+__global__ void __launch_bounds__(kSelThreads) k_rb_src_select(RoundCtx c, int64_t* rb) {
+  const int k = c.k;
+  uint64_t* thr = reinterpret_cast<uint64_t*>(rb + 4 * k + 1);
+  for (int b = blockIdx.x; b < k; b += gridDim.x) {
+    const int64_t need = rb[2 * k + b], cnt = need > 0 ? rb[k + b] : 0;
+    uint64_t t = 0;
+    if (cnt > 0) t = cta_radix_select(c.seg_key + rb[3 * k + b], c.seg_w + rb[3 * k + b], cnt, need - 1);
+    if (threadIdx.x == 0) thr[b] = t;
+    __syncthreads();
+  }
+}
+
+// Candidates the source side takes become the LP candidates (rec, per-block
+// totals); the last CTA plans the target-side selection.
+__global__ void k_rb_emit(RoundCtx c, const int32_t* __restrict__ rb_to, const int32_t* __restrict__ rb_score,
+                          const int64_t* __restrict__ rb) {
+  const int k = c.k;
+  const uint64_t* thr = reinterpret_cast<const uint64_t*>(rb + 4 * k + 1);
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < c.n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int from = c.part[v];
+    int4 r = make_int4(-1, 0, (int)v, from);
+    const int to = rb_to[v];
+    if (to >= 0) {
+      const int sc = rb_score[v];
+      const bool take = sc <= 0 || (rb[2 * k + from] > 0 && rb[k + from] > 0 &&
+                                    move_key(sc, (int32_t)v) <= thr[from]);
+      if (take) {
+        r.x = to;
+        r.y = sc;
+        const int64_t wv = c.w_v[v];
+        atomicAdd(reinterpret_cast<ull*>(&c.in_w[to]), (ull)wv);
+        atomicAdd(reinterpret_cast<ull*>(&c.in_cnt[to]), 1ull);
+        atomicAdd(reinterpret_cast<ull*>(&c.cand_out[from]), (ull)wv);
+      }
+    }
+    c.rec[v] = r;
+  }
+  if (last_cta(&c.scal[kDone])) plan_to(c);
+}
+
+cudaError_t launch_rebalance_round(const Launch& L, const RoundCtx& c, int round, int32_t* rb_to,
+                                   int32_t* rb_score, int64_t* rb) {
+  if (c.n == 0) return cudaSuccess;
+  const int k = c.k;
+  cudaError_t e = cudaMemsetAsync(rb, 0, sizeof(int64_t) * 2 * k, L.st);
+  if (e != cudaSuccess) return e;
+  const size_t smem = sizeof(int) * k * 8;
+  cudaFuncSetAttribute(k_rb_candidates, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_rb_candidates<<<grid_for(L, c.n * 32, 256), 256, smem, L.st>>>(c, round, rb_to, rb_score, rb);
+  LAUNCHED("k_rb_candidates");
+  k_rb_src_plan<<<1, 1024, 0, L.st>>>(c, rb);
+  LAUNCHED("k_rb_src_plan");
+  const int g = grid_for(L, c.n, 256);
+  k_rb_src_bin<<<g, 256, 0, L.st>>>(c, rb_to, rb_score, rb);
+  LAUNCHED("k_rb_src_bin");
+  cudaFuncSetAttribute(k_rb_src_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
+  k_rb_src_select<<<(unsigned)std::min<int64_t>(k, 4 * (int64_t)L.num_sms), kSelThreads, kSelSmem, L.st>>>(c, rb);
+  LAUNCHED("k_rb_src_select");
+  k_rb_emit<<<g, 256, 0, L.st>>>(c, rb_to, rb_score, rb);
+  LAUNCHED("k_rb_emit");
+  // the LP target-side selection, source floor and commit of one sub-round
+  k_bin_moves<<<grid_for(L, c.n, kBinThreads), kBinThreads, 0, L.st>>>(c, 0);
+  LAUNCHED("k_bin_moves");
+  cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
+  cudaFuncSetAttribute(k_from_side, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
+  k_select<<<(unsigned)std::min<int64_t>(k, 4 * (int64_t)L.num_sms), kSelThreads, kSelSmem, L.st>>>(c);
+  LAUNCHED("k_select");
+  k_from_side<<<1, kSelThreads, kSelSmem, L.st>>>(c, 0);
+  LAUNCHED("k_from_side");
+  const size_t dw_smem = sizeof(ull) * k;
+  k_commit<<<grid_for(L, c.n, kFlatItems, occupancy((const void*)k_commit, kFlatThreads, dw_smem)), kFlatThreads,
+             dw_smem, L.st>>>(c, round, 0, 1);
+  LAUNCHED("k_commit");
+  return cudaGetLastError();
+}
+
 cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int sub, PhaseTimer* timer) {
   const int k = c.k;
   const size_t dw_smem = c.batched ? 0 : sizeof(ull) * k;  // shared block-weight deltas

@@ -726,6 +726,9 @@ lpgpu_status lpgpu_session_project_partition(lpgpu_session* fine, const lpgpu_se
   return st;
 }
 
+static lpgpu_status read_metrics(lpgpu_session* s, int64_t* km1, int64_t* cut);
+static lpgpu_status read_imbalance(lpgpu_session* s, double* imb);
+
 static lpgpu_status read_metrics(lpgpu_session* s, int64_t* km1, int64_t* cut) {
   RoundCtx c = s->ctx();
   CK(launch_metrics(s->launch(), c));
@@ -1211,6 +1214,75 @@ lpgpu_status lpgpu_session_restore_partition(lpgpu_session* s) {
     CK(cudaMemcpyAsync(s->part.p, s->saved_part.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToDevice, s->st));
   RoundCtx c = s->ctx();
   CK(launch_init_partition(s->launch(), c));
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_rebalance(lpgpu_session* s, int32_t max_rounds, lpgpu_result* result) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  if (s->batched) {
+    set_error("this call needs a single-instance session");
+    return LPGPU_ERR_STATE;
+  }
+  if (max_rounds < 0) return invalid("max_rounds must be >= 0");
+  DeviceGuard g(s->device);
+  s->gc_valid = false;
+  const int R = max_rounds, k = s->k;
+  cudaStream_t st = s->st;
+  int64_t* fp = &s->footprint;
+  CK(s->stats.alloc(std::max(1, R) * kStats, fp));
+  CK(cudaMemsetAsync(s->stats.p, 0, sizeof(int64_t) * std::max(1, R) * kStats, st));
+  int64_t tmpfp = 0;
+  DevBuf<int64_t> rb;
+  CK(rb.alloc(5 * (size_t)k + 1, &tmpfp));
+  int64_t km1_before = 0;
+  ps = read_metrics(s, &km1_before, nullptr);
+  if (ps != LPGPU_OK) return ps;
+  std::vector<int64_t> hl(k), hb(k), hs(kStats);
+  CK(cudaMemcpyAsync(hl.data(), s->lmax.p, sizeof(int64_t) * k, cudaMemcpyDeviceToHost, st));
+  const int64_t sub[2] = {0, s->n};
+  RoundCtx c = s->ctx();
+  c.revert = 0;
+  c.rollback = 0;
+  s->last_stats.clear();
+  int64_t delta = 0, moves = 0, pins = 0;
+  for (int r = 0; r < R; ++r) {
+    CK(cudaMemcpyAsync(hb.data(), s->bw.p, sizeof(int64_t) * k, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    bool over = false;
+    for (int b = 0; b < k; ++b) over = over || hb[b] > hl[b];
+    if (!over) break;
+    // one sub-round over all vertices (rec and status per vertex id)
+    CK(cudaMemcpyAsync(s->sub_off.p, sub, sizeof(sub), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(s->blk64.p, 0, sizeof(int64_t) * 3 * k, st));  // in_w, in_cnt, cand_out
+    CK(launch_rebalance_round(s->launch(), c, r, s->heavy.p, s->revl.p, rb.p));
+    CK(cudaMemcpyAsync(hs.data(), s->stats.p + (int64_t)r * kStats, sizeof(int64_t) * kStats,
+                       cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    lpgpu_round_stats rs{hs[kStActive], hs[kStPins], hs[kStCands], hs[kStMoved], hs[kStReverted], hs[kStDelta]};
+    s->last_stats.push_back(rs);
+    delta += rs.delta;
+    moves += rs.moved;
+    pins += rs.pins;
+    if (rs.moved == 0) break;
+  }
+  rb.release(&tmpfp);
+  if (result) {
+    int64_t km1_after = 0;
+    ps = read_metrics(s, &km1_after, nullptr);
+    if (ps != LPGPU_OK) return ps;
+    double imb = 0;
+    ps = read_imbalance(s, &imb);
+    if (ps != LPGPU_OK) return ps;
+    result->km1_before = km1_before;
+    result->km1_after = km1_after;
+    result->delta = delta;
+    result->moves = moves;
+    result->pins_processed = pins;
+    result->rounds = (int32_t)s->last_stats.size();
+    result->improved = delta < 0;
+    result->imbalance = imb;
+  }
   return LPGPU_OK;
 }
 

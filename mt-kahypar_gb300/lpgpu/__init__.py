@@ -81,7 +81,7 @@ SYMBOLS = [
     "lpgpu_session_instance_km1", "lpgpu_partition_metrics_noalloc", "lpgpu_session_upload_instances",
     "lpgpu_session_set_partition_instances", "lpgpu_session_get_partition_instances", "lpgpu_read_hgr",
     "lpgpu_free", "lpgpu_read_partition", "lpgpu_write_partition", "lpgpu_session_init_gain_cache",
-    "lpgpu_session_drop_gain_cache", "lpgpu_session_project_partition",
+    "lpgpu_session_drop_gain_cache", "lpgpu_session_project_partition", "lpgpu_session_rebalance",
 ]
 
 
@@ -300,6 +300,12 @@ class Session:
         p = np.empty(self.n * self.k, np.int32)
         _check(lib().lpgpu_session_gain_cache(self._h, _p(b, I32P), _p(p, I32P)))
         return b, p.reshape(self.n, self.k)
+
+    def rebalance(self, max_rounds=16) -> Result:
+        """Deterministic rebalancer (lpgpu_session_rebalance)."""
+        r = Result()
+        _check(lib().lpgpu_session_rebalance(self._h, ctypes.c_int32(max_rounds), ctypes.byref(r)))
+        return r
 
     def project_partition(self, coarse, fine_to_coarse):
         """This (fine) session's partition from `coarse`'s through the vertex map."""

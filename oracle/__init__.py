@@ -121,6 +121,16 @@ def lp_sync(hg, k, lmax, part, perfect=None, **cfg):
     return p, [_stat_dict(stats[i]) for i in range(r)]
 
 
+def rebalance(hg, k, lmax, part, max_rounds=16):
+    """Deterministic rebalancer (orc_rebalance): partition and per-round stats."""
+    p = np.array(part, np.int32, copy=True)
+    stats = (RoundStats * max(1, max_rounds))()
+    lm = np.ascontiguousarray(lmax, np.int64)
+    r = lib().orc_rebalance(*_hg_args(hg), ctypes.c_int32(k), _p(lm, I64P), _p(p, I32P),
+                            ctypes.c_int32(max_rounds), stats)
+    return p, [_stat_dict(stats[i]) for i in range(r)]
+
+
 def lp_async(hg, k, lmax, perfect, part, **cfg):
     c = _cfg(**cfg)
     p = np.array(part, np.int32, copy=True)

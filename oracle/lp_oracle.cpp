@@ -460,6 +460,125 @@ int32_t orc_lp_sync(int64_t n, int64_t m, const int64_t* net_off, const int32_t*
   return r;
 }
 
+// Deterministic rebalancer (the device's lpgpu_session_rebalance), a
+// synchronous restatement of Rebalancer::rebalance (rebalancing/rebalancer.cpp:34-171,
+// whose thread-local priority queues make the reference order-dependent).
+// Per round, while some block is above its max weight:
+//   * every border vertex of an overloaded block computes its Km1Policy best
+//     move with rebalance = true (gain_policy.h:108-167): the feasible block
+//     (c(b) + w(v) <= L_max(b), b != from) of minimum score, any sign, lowest id
+//     on ties; vertices without a feasible block are no candidates;
+//   * per overloaded source block b with excess X = c(b) - L_max(b): every
+//     candidate with score <= 0 is taken (the reference's first pass moves all
+//     non-worsening moves); candidates with score > 0, ordered by (score,
+//     vertex id), are taken while the weight taken so far is below X (the
+//     second pass moves worsening moves only while the block is overloaded);
+//   * the taken moves go through the LP selection: per target block the
+//     longest (score, vertex id) prefix within L_max, then per source block the
+//     longest prefix that leaves it non-empty; they are committed with km1Delta
+//     attribution.
+// Stops when no block is overloaded, after max_rounds, or when a round moves
+// nothing. Returns the rounds executed; stats[r] gets candidates, moved, delta.
+int32_t orc_rebalance(int64_t n, int64_t m, const int64_t* net_off, const int32_t* pins,
+                      const int64_t* vtx_off, const int32_t* inets, const int32_t* w_v,
+                      const int32_t* w_e, int32_t k, const int64_t* lmax, int32_t* part_inout,
+                      int32_t max_rounds, orc_round_stats* stats) {
+  Hg hg = make_hg(n, m, net_off, pins, vtx_off, inets, w_v, w_e);
+  State s{&hg, k, words_for(k), {}, {}, {}, {}};
+  s.init(part_inout);
+  std::vector<int64_t> scores(k, 0);
+  struct Cand { int32_t v, from, to; int64_t gain; int64_t w; };
+  auto key_less = [](const Cand& a, const Cand& b) { return a.gain != b.gain ? a.gain < b.gain : a.v < b.v; };
+  int32_t r = 0;
+  for (; r < max_rounds; ++r) {
+    bool over = false;
+    for (int b = 0; b < k; ++b) over = over || s.bw[b] > lmax[b];
+    if (!over) break;
+    orc_round_stats st{};
+    std::vector<Cand> cands;
+    for (int64_t v = 0; v < n; ++v) {
+      const int from = s.part[v];
+      if (s.bw[from] <= lmax[from]) continue;
+      st.active++;
+      st.pins += vtx_off[v + 1] - vtx_off[v];
+      if (!s.is_border(v)) continue;
+      // rebalance best move: minimum score over feasible blocks, any sign
+      int64_t internal = 0;
+      for (int64_t i = vtx_off[v]; i < vtx_off[v + 1]; ++i) {
+        const int64_t e = inets[i];
+        if (s.phi[e * k + from] > 1) internal += w_e[e];
+        for (int b = 0; b < k; ++b)
+          if (b != from && bit_of(s.conn.data(), s.W, e, b)) scores[b] -= w_e[e];
+      }
+      int to = from;
+      int64_t best = 0;
+      for (int b = 0; b < k; ++b) {
+        if (b != from && s.bw[b] + w_v[v] <= lmax[b]) {
+          const int64_t sc = scores[b] + internal;
+          if (to == from || sc < best) {
+            to = b;
+            best = sc;
+          }
+        }
+        scores[b] = 0;
+      }
+      if (to != from) cands.push_back({(int32_t)v, from, to, best, w_v[v]});
+    }
+    st.candidates = (int64_t)cands.size();
+    std::sort(cands.begin(), cands.end(), key_less);
+    // source side: non-worsening moves always, worsening ones while needed
+    std::vector<int64_t> taken(k, 0);
+    for (const Cand& c : cands)
+      if (c.gain <= 0) taken[c.from] += c.w;
+    std::vector<Cand> src;
+    for (const Cand& c : cands) {
+      if (c.gain <= 0) {
+        src.push_back(c);
+      } else if (taken[c.from] < s.bw[c.from] - lmax[c.from]) {
+        taken[c.from] += c.w;
+        src.push_back(c);
+      }
+    }
+    // LP selection: target-side prefix, then source-side prefix keeping blocks non-empty
+    std::vector<int64_t> in(k, 0), out(k, 0);
+    std::vector<uint8_t> stop_in(k, 0), stop_out(k, 0), ok(src.size(), 0);
+    for (size_t i = 0; i < src.size(); ++i) {
+      const Cand& c = src[i];
+      if (stop_in[c.to]) continue;
+      if (s.bw[c.to] + in[c.to] + c.w <= lmax[c.to]) {
+        in[c.to] += c.w;
+        ok[i] = 1;
+      } else {
+        stop_in[c.to] = 1;
+      }
+    }
+    for (size_t i = 0; i < src.size(); ++i) {
+      if (!ok[i]) continue;
+      const Cand& c = src[i];
+      if (stop_out[c.from]) { ok[i] = 0; continue; }
+      if (s.bw[c.from] - out[c.from] - c.w >= 1) {
+        out[c.from] += c.w;
+      } else {
+        stop_out[c.from] = 1;
+        ok[i] = 0;
+      }
+    }
+    for (size_t i = 0; i < src.size(); ++i) {
+      if (!ok[i]) continue;
+      st.delta += s.apply_move(src[i].v, src[i].from, src[i].to);
+      st.moved++;
+    }
+    st.km1_after = s.km1();
+    if (stats) stats[r] = st;
+    if (st.moved == 0) {
+      ++r;
+      break;
+    }
+  }
+  std::memcpy(part_inout, s.part.data(), sizeof(int32_t) * n);
+  return r;
+}
+
 // Reference-style asynchronous LP (label_propagation_refiner.{h,cpp}):
 // std::threads, shuffled active set, per-net spinlocks around pin-count
 // updates, atomic block weights with rollback, per-thread precomputed coin
