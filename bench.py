@@ -207,6 +207,10 @@ def reference_arm(args):
     rank, _, world = dist_info()
     if rank != 0:
         return 0
+    if args.workload in ("batch", "served"):
+        print(json.dumps({"impl": "reference", "unavailable": "the batched and served workloads are measured "
+                          "against the plain GPU loop in the gpu arm's own line (plain_loop)"}), flush=True)
+        return 0
     inst = make_instance(args.workload, args.seed)
     threads = os.cpu_count() or 1
     values, times = [], []

@@ -62,3 +62,51 @@ def test_no_device_is_an_error_not_a_fallback(lp):
     assert st == lp.ERR_NO_DEVICE
     with pytest.raises(lp.LpgpuError):
         lp.Session(0)
+
+
+C_PROGRAM = r"""
+#include <stdio.h>
+#include <string.h>
+#include "lpgpu.h"
+int main(int argc, char** argv) {
+  lpgpu_config c;
+  lpgpu_config_default(&c);
+  if (c.rounds != 5 || c.activation_threshold != 100) return 2;
+  int64_t n, m, removed; int64_t* off; int32_t *pins, *vw, *ew;
+  if (lpgpu_read_hgr(argv[1], &n, &m, &off, &pins, &vw, &ew, &removed) != LPGPU_OK) {
+    fprintf(stderr, "%s\n", lpgpu_last_error());
+    return 3;
+  }
+  printf("%lld %lld %lld %lld %d\n", (long long)n, (long long)m, (long long)off[m], (long long)removed, pins[0]);
+  lpgpu_free(off); lpgpu_free(pins); lpgpu_free(vw); lpgpu_free(ew);
+  lpgpu_session* s = 0;
+  lpgpu_status st = lpgpu_session_create(0, &s);  /* no device here: an error, never a fallback */
+  if (st == LPGPU_OK) lpgpu_session_destroy(s);
+  printf("%s\n", lpgpu_status_string(st));
+  return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("compiler,ext", [("gcc", "c"), ("g++", "cpp")])
+def test_header_compiles_and_links_from_c_and_cpp(lp, tmp_path, compiler, ext):
+    """include/lpgpu.h is plain C and C++: a program built with the host
+    compiler links liblpgpu.so and calls it (file reader, no GPU needed)."""
+    import shutil
+    import subprocess
+    if not shutil.which(compiler):
+        pytest.skip(compiler + " not found")
+    src = tmp_path / f"prog.{ext}"
+    src.write_text(C_PROGRAM)
+    hgr = tmp_path / "t.hgr"
+    hgr.write_text("% tiny\n3 4\n1 2\n3\n2 3 4\n")
+    libdir = os.path.dirname(lp.LIB_PATH)
+    exe = tmp_path / "prog"
+    r = subprocess.run([compiler, str(src), "-I", os.path.join(ROOT, "include"), "-L", libdir, "-llpgpu",
+                        "-Wl,-rpath," + libdir, "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe), str(hgr)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    first, second = r.stdout.strip().split("\n")
+    assert first == "4 2 5 1 0"
+    assert second  # status text of session_create (ok on a GPU box, an error here)
