@@ -55,6 +55,8 @@ def parse_args():
                     help="batch: instances (default 4096); served: requests (default 256)")
     ap.add_argument("--rate", type=float, default=2000.0, help="served: Poisson arrival rate (req/s)")
     ap.add_argument("--slots", type=int, default=2, help="served: concurrent batched sessions")
+    ap.add_argument("--batch-pins", type=float, default=None,
+                    help="served: a batch stops growing at this many pins (default: memory budget only)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--subrounds", type=int, default=8)
     ap.add_argument("--no-baseline", action="store_true", help="skip the CPU baseline leg")
@@ -492,7 +494,8 @@ def served_arm(args):
     serve.replay(serve.RefineServer(slots=args.slots), warm)
     serve.plain_loop(warm)
     rs = requests()
-    st_s = serve.replay(serve.RefineServer(slots=args.slots, subrounds=args.subrounds), rs)
+    cap = None if args.batch_pins is None else int(args.batch_pins)
+    st_s = serve.replay(serve.RefineServer(slots=args.slots, subrounds=args.subrounds, max_batch_pins=cap), rs)
     rp = requests()
     st_p = serve.plain_loop(rp, subrounds=args.subrounds)
     same = all(a.km1 == b.km1 and np.array_equal(a.result, b.result) for a, b in zip(rs, rp))
@@ -502,7 +505,8 @@ def served_arm(args):
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",
             "config": {"workload": f"{len(insts)} requests at {args.rate:.0f} req/s, "
                                    f"{sum(x.hg.num_pins for x in insts)} pins in total, 8 rounds each",
-                       "slots": args.slots, "budget_gb": 150, "subrounds": args.subrounds},
+                       "slots": args.slots, "budget_gb": 150, "subrounds": args.subrounds,
+                       "batch_pins": cap},
             "server": ss, "plain_loop": sp, "identical_results": same}
     print(json.dumps(line), flush=True)
     return 0 if same else 1

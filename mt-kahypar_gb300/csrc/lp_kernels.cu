@@ -2007,7 +2007,10 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const i
 }
 
 // Target-side selection: CTAs stride over the overflowing blocks.
-__global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c) {
+__device__ void from_side(const RoundCtx& c, int sub);
+
+// Its last CTA then runs the source-side selection (from_side).
+__global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c, int sub) {
   const int64_t nover = c.scal[kOverCount];
   for (int64_t i = blockIdx.x; i < nover; i += gridDim.x) {
     const int b = c.over_ids[i];
@@ -2017,6 +2020,7 @@ __global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c) {
     if (threadIdx.x == 0) c.thr_to[b] = thr;
     __syncthreads();
   }
+  if (last_cta(&c.scal[kDone])) from_side(c, sub);
 }
 
 // Source-side selection (changeNodePart's from_weight_after > 0,
@@ -2024,7 +2028,7 @@ __global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c) {
 // the target-accepted weight leaving each block; blocks that would become
 // empty get their accepted moves ordered the same way and keep the longest
 // prefix that leaves weight >= 1.
-__global__ void __launch_bounds__(kSelThreads) k_from_side(RoundCtx c, int sub) {
+__device__ void from_side(const RoundCtx& c, int sub) {
   if (c.scal[kAnyOverFrom] == 0) return;
   const int k = c.k;
   __shared__ int s_any;
@@ -2477,7 +2481,13 @@ __device__ __forceinline__ void undo_epilogue(const RoundCtx& c, int round, int6
 // Undo of the moves the hindsight check marked (status 2), from the compact
 // list k_revert_eval wrote, spread over all CTAs (each takes a short range and
 // walks its moves' incidences flat). With `last` the sub-round is closed.
-__global__ void __launch_bounds__(kFlatThreads) k_undo_reverts(RoundCtx c, int round, int last) {
+__device__ void rollback_ranges(const RoundCtx& c, int round, int sub, bool roll, FlatSmem& f, ull* s_dw,
+                                int64_t first, int64_t stride);
+
+// With `roll_tail` (one instance), the last CTA also performs the sub-round's
+// rollback when its delta is positive (rare), so no rollback kernel runs.
+__global__ void __launch_bounds__(kFlatThreads) k_undo_reverts(RoundCtx c, int round, int sub, int last,
+                                                                int roll_tail) {
   extern __shared__ ull s_dw[];
   __shared__ FlatSmem f;
   const bool batched = c.batched != 0;
@@ -2519,16 +2529,24 @@ __global__ void __launch_bounds__(kFlatThreads) k_undo_reverts(RoundCtx c, int r
         if (f.att[i]) atomicAdd(reinterpret_cast<ull*>(&c.inst_delta[f.inst[i]]), (ull)(int64_t)f.att[i]);
   }
   undo_epilogue(c, round, att, undone, kDeltaSub, s_dw, kdw);
-  if (last && last_cta(&c.scal[kDone])) close_subround(c, round);
+  if ((last || roll_tail) && last_cta(&c.scal[kDone])) {
+    if (roll_tail) {
+      const bool roll = *(volatile int64_t*)&c.scal[kDeltaSub] > 0;
+      __syncthreads();
+      rollback_ranges(c, round, sub, roll, f, s_dw, 0, 1);
+    }
+    close_subround(c, round);
+  }
 }
 
 // Rollback: when the sub-round's delta is positive, undo of every move still
 // marked 1 (status 3); decided per instance when batched (kDeltaSub and
 // inst_delta are not written here). Closes the sub-round.
-__global__ void __launch_bounds__(kFlatThreads) k_rollback(RoundCtx c, int round, int sub) {
-  const bool roll = c.batched || c.scal[kDeltaSub] > 0;
-  extern __shared__ ull s_dw[];
-  __shared__ FlatSmem f;
+// Rollback of the sub-round's moves still marked 1 (status 3) over the list
+// ranges first, first + stride, ... (CTA-flat); returns nothing, books into
+// kDeltaRb and the statistics.
+__device__ void rollback_ranges(const RoundCtx& c, int round, int sub, bool roll, FlatSmem& f, ull* s_dw,
+                                int64_t first, int64_t stride) {
   const bool batched = c.batched != 0;
   ull* dw = batched ? reinterpret_cast<ull*>(c.bw) : s_dw;
   const int kdw = batched ? 0 : c.k;
@@ -2536,7 +2554,7 @@ __global__ void __launch_bounds__(kFlatThreads) k_rollback(RoundCtx c, int round
   constexpr int PER = kFlatItems / kFlatThreads;
   const int64_t beg = c.sub_off[sub], end = roll ? c.sub_off[sub + 1] : beg;
   int64_t att = 0, undone = 0;
-  for (int64_t r0 = beg + (int64_t)blockIdx.x * kFlatItems; r0 < end; r0 += (int64_t)gridDim.x * kFlatItems) {
+  for (int64_t r0 = beg + first * kFlatItems; r0 < end; r0 += stride * kFlatItems) {
     if (threadIdx.x == 0) f.n = 0;
     __syncthreads();
 #pragma unroll
@@ -2567,6 +2585,12 @@ __global__ void __launch_bounds__(kFlatThreads) k_rollback(RoundCtx c, int round
     __syncthreads();
   }
   undo_epilogue(c, round, att, undone, kDeltaRb, s_dw, kdw);
+}
+
+__global__ void __launch_bounds__(kFlatThreads) k_rollback(RoundCtx c, int round, int sub) {
+  extern __shared__ ull s_dw[];
+  __shared__ FlatSmem f;
+  rollback_ranges(c, round, sub, c.batched || c.scal[kDeltaSub] > 0, f, s_dw, blockIdx.x, gridDim.x);
   if (last_cta(&c.scal[kDone])) close_subround(c, round);
 }
 
@@ -2840,11 +2864,8 @@ cudaError_t launch_rebalance_round(const Launch& L, const RoundCtx& c, int round
   k_bin_moves<<<grid_for(L, c.n, kBinThreads), kBinThreads, 0, L.st>>>(c, 0);
   LAUNCHED("k_bin_moves");
   cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
-  cudaFuncSetAttribute(k_from_side, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
-  k_select<<<(unsigned)std::min<int64_t>(k, 4 * (int64_t)L.num_sms), kSelThreads, kSelSmem, L.st>>>(c);
+  k_select<<<(unsigned)std::min<int64_t>(k, 4 * (int64_t)L.num_sms), kSelThreads, kSelSmem, L.st>>>(c, 0);
   LAUNCHED("k_select");
-  k_from_side<<<1, kSelThreads, kSelSmem, L.st>>>(c, 0);
-  LAUNCHED("k_from_side");
   const size_t dw_smem = sizeof(ull) * k;
   k_commit<<<grid_for(L, c.n, kFlatItems, occupancy((const void*)k_commit, kFlatThreads, dw_smem)), kFlatThreads,
              dw_smem, L.st>>>(c, round, 0, 1);
@@ -2875,11 +2896,8 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
     k_bin_moves<<<g_bin, kBinThreads, 0, L.st>>>(c, sub);
     LAUNCHED("k_bin_moves");
     cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
-    cudaFuncSetAttribute(k_from_side, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
-    k_select<<<(unsigned)std::min<int64_t>(k, 4 * (int64_t)L.num_sms), kSelThreads, kSelSmem, L.st>>>(c);
+    k_select<<<(unsigned)std::min<int64_t>(k, 4 * (int64_t)L.num_sms), kSelThreads, kSelSmem, L.st>>>(c, sub);
     LAUNCHED("k_select");
-    k_from_side<<<1, kSelThreads, kSelSmem, L.st>>>(c, sub);
-    LAUNCHED("k_from_side");
   }
   const int last_commit = !c.revert && !c.rollback;
   {
@@ -2887,14 +2905,16 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
     k_commit<<<g_commit, kFlatThreads, dw_smem, L.st>>>(c, round, sub, last_commit);
     LAUNCHED("k_commit");
   }
+  // one instance with reverts: the rollback check runs in the undo kernel's last CTA
+  const int roll_tail = c.revert && c.rollback && !c.batched;
   if (c.revert) {
     Scope sc(timer, "revert");
     k_revert_eval<<<g_eval, kFlatThreads, 0, L.st>>>(c, sub);
     LAUNCHED("k_revert_eval");
-    k_undo_reverts<<<g_unrev, kFlatThreads, dw_smem, L.st>>>(c, round, !c.rollback);
+    k_undo_reverts<<<g_unrev, kFlatThreads, dw_smem, L.st>>>(c, round, sub, !c.rollback, roll_tail);
     LAUNCHED("k_undo_reverts");
   }
-  if (c.rollback) {
+  if (c.rollback && !roll_tail) {
     Scope sc(timer, "rollback");
     k_rollback<<<g_undo, kFlatThreads, dw_smem, L.st>>>(c, round, sub);
     LAUNCHED("k_rollback");

@@ -94,12 +94,15 @@ class RefineServer:
     """
 
     def __init__(self, device=0, slots=2, budget_bytes=150 << 30, subrounds=8, max_batch=4096,
-                 session_factory=Session, runner=_run_batch, footprint=None):
+                 session_factory=Session, runner=_run_batch, footprint=None, max_batch_pins=None):
         self.device = device
         self.slots = slots
         self.budget = budget_bytes
         self.subrounds = subrounds
         self.max_batch = max_batch
+        # a batch stops growing once it holds this many pins (None: memory budget only);
+        # smaller batches finish their first requests sooner at some cost in throughput
+        self.max_batch_pins = max_batch_pins
         self._runner = runner
         self._footprint = footprint or (lambda r, s: r.footprint(s))
         self._cv = threading.Condition()
@@ -144,7 +147,7 @@ class RefineServer:
     def _admit(self, slot):
         """Takes waiting requests in arrival order while they fit the memory left."""
         free = self.budget - sum(h for i, h in enumerate(self._held) if i != slot)
-        take, used = [], 0
+        take, used, pins = [], 0, 0
         rounds = self._queue[0].rounds if self._queue else 0
         for r in list(self._queue):
             if r.rounds != rounds:  # a batch runs one round count for all its requests
@@ -152,8 +155,11 @@ class RefineServer:
             f = self._footprint(r, self.subrounds)
             if len(take) >= self.max_batch or used + f > free:
                 break
+            if take and self.max_batch_pins is not None and pins + r.hg.num_pins > self.max_batch_pins:
+                break
             take.append(r)
             used += f
+            pins += r.hg.num_pins
         for r in take:
             self._queue.remove(r)
         self._held[slot] = used

@@ -427,3 +427,19 @@ def test_projection_between_levels(lp, orc, seed, k):
         with pytest.raises(lp.LpgpuError) as e:
             f.project_partition(c, bad)
         assert e.value.status == lp.ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("seed,n,m,k", [(116, 60, 120, 2), (149, 60, 120, 2), (11, 100, 300, 3), (128, 100, 300, 3)])
+def test_rollback_path(lp, orc, seed, n, m, k):
+    """Instances where a whole sub-round is rolled back (one sub-round, no
+    revert): the oracle's result differs with and without rollback, and the
+    device follows the oracle."""
+    from lpgpu import gen
+    inst = gen.random_small(seed, n=n, m=m, k=k, max_size=3)
+    kw = dict(perfect=inst.perfect, rounds=4, subrounds=1, revert=0, zero_gain=1)
+    with_rb, _ = orc.lp_sync(inst.hg, k, inst.lmax, inst.part, rollback=1, **kw)
+    without, _ = orc.lp_sync(inst.hg, k, inst.lmax, inst.part, rollback=0, **kw)
+    assert not np.array_equal(with_rb, without)  # the rollback path is taken
+    out = run_both(lp, orc, inst, 4, dict(subrounds=1, revert=0, rollback=1, rebalancing=1))
+    assert_same_run(*out, orc, inst)
+    out[0].close()

@@ -120,3 +120,15 @@ def test_poisson_arrivals_rate():
     a = serve.poisson_arrivals(20000, 2000.0, 1)
     assert np.all(np.diff(a) > 0)
     assert abs(20000 / a[-1] - 2000.0) < 60.0
+
+
+def test_pin_cap_limits_batches():
+    reqs = _requests(100, 11)
+    for r in reqs:
+        r.hg.num_pins = 10
+    rec = Recorder(10 ** 6)
+    srv = serve.RefineServer(slots=1, budget_bytes=10 ** 6, session_factory=FakeSession, runner=rec,
+                             footprint=lambda r, s: r.hg.n, max_batch_pins=35)
+    serve.replay(srv, reqs)
+    assert max(len(b) for b in rec.batches) <= 3
+    assert sorted(i for b in rec.batches for i in b) == list(range(100))
