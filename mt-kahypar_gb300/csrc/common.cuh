@@ -196,10 +196,10 @@ cudaError_t launch_check_partition(const Launch& L, int64_t n, int32_t* part, in
 cudaError_t launch_rebase_instances(const Launch& L, int I, const int64_t* inst_voff, const int64_t* inst_noff,
                                     const int64_t* inst_poff, int64_t* net_off, int32_t* pins);
 cudaError_t launch_fill_ones(const Launch& L, int32_t* p, int64_t count);
-// Multilevel projection: part[v] = coarse_part[map[v]]; *verdict != 0 when a
+// Multilevel projection: part[v] = coarse_part[map[v]]; *check != 0 when a
 // map entry lies outside [0, nc).
 cudaError_t launch_project(const Launch& L, int64_t n, const int32_t* map, const int32_t* coarse_part, int64_t nc,
-                           int32_t* part, int64_t* verdict);
+                           int32_t* part, int64_t* check);
 // Global block ids of a batch back to instance-local ids.
 cudaError_t launch_local_blocks(const Launch& L, int64_t n, const int32_t* part, const int32_t* vinst,
                                 const int32_t* inst_boff, int32_t* out);

@@ -121,7 +121,7 @@ struct lpgpu_session_s {
   std::vector<int32_t> h_inst_boff, h_inst_k;
   DevBuf<int32_t> vinst, inst_boff, inst_k, over_ids;
   DevBuf<int64_t> inst_voff, inst_noff, inst_delta;
-  DevBuf<int64_t> vout;  // verdict words of the device-side input checks
+  DevBuf<int64_t> vout;  // result words of the device-side input checks
   // results of the last refine
   std::vector<lpgpu_round_stats> last_stats;
   // timing
@@ -469,7 +469,7 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
     s->inst_voff.release(fp);
     s->inst_noff.release(fp);
   }
-  // device-side checks; one copy back of the verdict and the per-instance sums
+  // device-side checks; one copy back of the result words and the per-instance sums
   CK(launch_validate_csr(s->launch(), n, m, P, s->net_off.p, s->pins.p, s->w_v.p, s->w_e.p, I,
                          s->inst_voff.p, s->inst_noff.p, s->vinst.p, s->vout.p));
   std::vector<int64_t> h(kVSums + 2 * (size_t)I);
@@ -595,12 +595,12 @@ static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax
   }
   CK(launch_check_partition(s->launch(), s->n, s->part.p, K, s->batched ? s->vinst.p : nullptr,
                             s->inst_boff.p, s->inst_k.p, s->vout.p));
-  int64_t verdict = 0;
-  CK(cudaMemcpyAsync(&verdict, s->vout.p + kVErr, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  int64_t check = 0;
+  CK(cudaMemcpyAsync(&check, s->vout.p + kVErr, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(s->lmax.p, hl.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(s->perfect.p, hp.data(), sizeof(int64_t) * K, cudaMemcpyHostToDevice, st));
   CK(cudaStreamSynchronize(st));
-  if (verdict != kVOk) return invalid("block id out of range");
+  if (check != kVOk) return invalid("block id out of range");
   CK(cudaMemsetAsync(s->blk64.p, 0, sizeof(int64_t) * (7 * (size_t)K + 1), st));
   RoundCtx c = s->ctx();
   CK(launch_init_partition(s->launch(), c));
@@ -705,16 +705,16 @@ lpgpu_status lpgpu_session_project_partition(lpgpu_session* fine, const lpgpu_se
   CK(cudaStreamSynchronize(coarse->st));
   int64_t fp = 0;
   DevBuf<int32_t> map, proj;
-  DevBuf<int64_t> verdict;
+  DevBuf<int64_t> check;
   CK(map.alloc(fine->n, &fp));
   CK(proj.alloc(fine->n, &fp));
-  CK(verdict.alloc(1, &fp));
+  CK(check.alloc(1, &fp));
   if (fine->n > 0)
     CK(cudaMemcpyAsync(map.p, fine_to_coarse, sizeof(int32_t) * fine->n, cudaMemcpyHostToDevice, fine->st));
-  CK(launch_project(fine->launch(), fine->n, map.p, coarse->part.p, coarse->n, proj.p, verdict.p));
+  CK(launch_project(fine->launch(), fine->n, map.p, coarse->part.p, coarse->n, proj.p, check.p));
   int64_t bad = 0;
   std::vector<int64_t> hl(coarse->k);
-  CK(cudaMemcpyAsync(&bad, verdict.p, sizeof(int64_t), cudaMemcpyDeviceToHost, fine->st));
+  CK(cudaMemcpyAsync(&bad, check.p, sizeof(int64_t), cudaMemcpyDeviceToHost, fine->st));
   CK(cudaMemcpyAsync(hl.data(), coarse->lmax.p, sizeof(int64_t) * coarse->k, cudaMemcpyDeviceToHost, fine->st));
   CK(cudaStreamSynchronize(fine->st));
   if (bad) return invalid("fine-to-coarse map entry outside the coarse vertices");
@@ -722,7 +722,7 @@ lpgpu_status lpgpu_session_project_partition(lpgpu_session* fine, const lpgpu_se
   const lpgpu_status st = set_partition_impl(fine, coarse->k, coarse->k, nullptr, hl, hp, nullptr, proj.p);
   map.release(&fp);
   proj.release(&fp);
-  verdict.release(&fp);
+  check.release(&fp);
   return st;
 }
 

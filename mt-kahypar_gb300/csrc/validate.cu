@@ -212,13 +212,13 @@ __global__ void k_local_blocks(int64_t n, const int32_t* __restrict__ part, cons
     out[v] = part[v] - inst_boff[vinst[v]];
 }
 
-// part[v] = coarse_part[map[v]]; map entries outside [0, nc) set the verdict.
+// part[v] = coarse_part[map[v]]; map entries outside [0, nc) set the check.
 __global__ void k_project(int64_t n, const int32_t* __restrict__ map, const int32_t* __restrict__ coarse_part,
-                          int64_t nc, int32_t* __restrict__ part, int64_t* verdict) {
+                          int64_t nc, int32_t* __restrict__ part, int64_t* check) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
     const int32_t u = map[v];
     if (u < 0 || u >= nc) {
-      atomicCAS(reinterpret_cast<ull*>(verdict), 0ull, 1ull);
+      atomicCAS(reinterpret_cast<ull*>(check), 0ull, 1ull);
       part[v] = 0;
     } else {
       part[v] = coarse_part[u];
@@ -289,11 +289,11 @@ cudaError_t launch_local_blocks(const Launch& L, int64_t n, const int32_t* part,
 }
 
 cudaError_t launch_project(const Launch& L, int64_t n, const int32_t* map, const int32_t* coarse_part, int64_t nc,
-                           int32_t* part, int64_t* verdict) {
-  cudaError_t e = cudaMemsetAsync(verdict, 0, sizeof(int64_t), L.st);
+                           int32_t* part, int64_t* check) {
+  cudaError_t e = cudaMemsetAsync(check, 0, sizeof(int64_t), L.st);
   if (e != cudaSuccess) return e;
   if (n > 0) {
-    k_project<<<grid(L, n, 256), 256, 0, L.st>>>(n, map, coarse_part, nc, part, verdict);
+    k_project<<<grid(L, n, 256), 256, 0, L.st>>>(n, map, coarse_part, nc, part, check);
     add_kernel_launches(1);
   }
   return cudaGetLastError();
