@@ -21,6 +21,22 @@ constexpr int64_t kHighDegree = 100000;
 // Sub-rounds are assigned per aligned chunk of 32 consecutive vertex ids.
 constexpr int kChunkShift = 5;
 constexpr int kMaxSubrounds = 64;
+// Classes inside a sub-round's active list (see k_bin_count): heavy
+// vertices, then four degree classes.
+constexpr int kDegClasses = 5;
+// Log2 buckets of the upload-time degree histogram.
+constexpr int kDegBuckets = 32;
+// Above this degree the warp windows of the k > 128 sweep hand a vertex to a whole CTA.
+constexpr int kHeavyDegree = 1024;
+
+// Whether the sweep evaluates a vertex of degree d with a whole CTA (heavy)
+// instead of its own lane (k <= 128: summed net weight reaches the 2^planes
+// of the lane counters) or a warp window (k > 128). Vertices above
+// kHighDegree are never border vertices and are not evaluated at all.
+__host__ __device__ inline bool sweep_heavy(int64_t d, int W, int unit_nets, int max_we) {
+  if (d <= 0 || d > kHighDegree) return false;
+  return W <= 4 ? d * max_we >= (int64_t(1) << (unit_nets ? 6 : 8)) : d > kHeavyDegree;
+}
 
 // Sub-round of vertex v in round r: mix32((v >> 5) ^ (0x9E3779B9 * (r + 1))) % S.
 __host__ __device__ inline uint32_t mix32(uint32_t x) {
@@ -96,7 +112,7 @@ struct RoundCtx {
   const int64_t* perfect;
   // active lists
   int32_t* list;
-  int64_t* sub_off;      // S + 1 offsets into list
+  int64_t* sub_off;      // S + 1 offsets into list, then per sub-round the end of its heavy vertices
   uint8_t* next_flag;    // n
   int32_t* net_epoch;    // m: round stamp of nets to expand
   // per list position
@@ -123,6 +139,7 @@ struct RoundCtx {
   int32_t unit_nets;     // every net weight is 1
   int32_t max_we;        // largest net weight (0 without nets)
   int64_t act_threshold;
+  int32_t heavy_share;   // per mille of the sweep's work in heavy vertices (0: none can exist)
   // batched sessions: many independent instances in one union hypergraph.
   // part[] holds global block ids (instance block offset + local id); Φ and
   // Λ are indexed by local ids. One instance: batched = 0, kmax = k.
@@ -162,7 +179,8 @@ int64_t scan_tmp_elems(int64_t count);
 
 cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const int64_t* net_off,
                                    const int32_t* pins, int64_t* vtx_off, int32_t* inets,
-                                   int64_t* cursor, int64_t* scan_tmp, int64_t scan_tmp_elems);
+                                   int64_t* cursor, int64_t* scan_tmp, int64_t scan_tmp_elems,
+                                   int64_t* deg_hist);
 cudaError_t launch_init_partition(const Launch& L, const RoundCtx& c);
 cudaError_t launch_metrics(const Launch& L, const RoundCtx& c);
 cudaError_t launch_instance_metrics(const Launch& L, const RoundCtx& c, int64_t* km1_inst);

@@ -169,6 +169,21 @@ __global__ void k_count_pins(const int32_t* __restrict__ pins, int64_t P, int64_
     atomicAdd(reinterpret_cast<ull*>(&cnt[pins[i]]), 1ull);
 }
 
+// Incidences per log2 degree bucket (bucket j: degree in [2^j, 2^(j+1))),
+// from the per-vertex counts before the scan; sizes the sweep's heavy share.
+__global__ void k_degree_hist(int64_t n, const int64_t* __restrict__ cnt, int64_t* __restrict__ hist) {
+  __shared__ ull s_h[kDegBuckets];
+  if (threadIdx.x < kDegBuckets) s_h[threadIdx.x] = 0;
+  __syncthreads();
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t d = cnt[v];
+    if (d > 0) atomicAdd(&s_h[min(63 - __clzll(d), kDegBuckets - 1)], (ull)d);
+  }
+  __syncthreads();
+  if (threadIdx.x < kDegBuckets && s_h[threadIdx.x])
+    atomicAdd(reinterpret_cast<ull*>(&hist[threadIdx.x]), s_h[threadIdx.x]);
+}
+
 // Warp per net: every pin appends the net id to its vertex's incident-net list.
 __global__ void k_scatter_incidence(int64_t m, const int64_t* __restrict__ net_off,
                                     const int32_t* __restrict__ pins, int64_t* __restrict__ cursor,
@@ -185,7 +200,8 @@ __global__ void k_scatter_incidence(int64_t m, const int64_t* __restrict__ net_o
 
 cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const int64_t* net_off,
                                    const int32_t* pins, int64_t* vtx_off, int32_t* inets,
-                                   int64_t* cursor, int64_t* scan_tmp, int64_t scan_tmp_elems) {
+                                   int64_t* cursor, int64_t* scan_tmp, int64_t scan_tmp_elems,
+                                   int64_t* deg_hist) {
   int64_t P = 0;
   cudaError_t e = cudaMemcpyAsync(&P, net_off + m, sizeof(int64_t), cudaMemcpyDeviceToHost, L.st);
   if (e != cudaSuccess) return e;
@@ -194,6 +210,13 @@ cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const 
   if (P > 0) {
     k_count_pins<<<grid_for(L, P, 256, 8), 256, 0, L.st>>>(pins, P, vtx_off);
     LAUNCHED("k_count_pins");
+  }
+  if (deg_hist) {
+    if ((e = cudaMemsetAsync(deg_hist, 0, sizeof(int64_t) * kDegBuckets, L.st)) != cudaSuccess) return e;
+    if (n > 0) {
+      k_degree_hist<<<grid_for(L, n, 256, 4), 256, 0, L.st>>>(n, vtx_off, deg_hist);
+      LAUNCHED("k_degree_hist");
+    }
   }
   if ((e = scan_exclusive_i64(vtx_off, vtx_off, n + 1, scan_tmp, scan_tmp_elems, L.st)) != cudaSuccess)
     return e;
@@ -598,8 +621,6 @@ __device__ __forceinline__ void decide(int k, int from, int wv, int internal, in
 }
 
 constexpr int kSweepThreads = 256;
-// Above this degree the tile windows of k_sweep (k > 128) defer a vertex to k_sweep_heavy.
-constexpr int kHeavyDegree = 1024;
 
 __device__ bool last_cta(int64_t* counter);
 __device__ void plan_to(const RoundCtx& c);
@@ -806,6 +827,126 @@ __device__ __forceinline__ void lv_vertex(const RoundCtx& c, int64_t o0, int d, 
 }
 
 
+// One heavy vertex (sweep_heavy: summed net weight too large for the lane
+// counters, or more than kHeavyDegree incidences) evaluated by the whole CTA:
+// its warps split the incidence windows (lane = incidence, Λ words transposed
+// so that lane l counts block l + 32 t), sum their per-block penalties in
+// shared memory, and warp 0 decides. Query mode (dbg_to != null) writes
+// to / gain / border of v; otherwise rec[pos] and the per-block candidate
+// totals, counting the candidate in `cands` (thread 0 of warp 0).
+template <int W, bool UNIT>
+__device__ void heavy_vertex(const RoundCtx& c, int64_t pos, int64_t v, int zero_gain, int32_t* dbg_to,
+                             int32_t* dbg_gain, uint8_t* dbg_border, int64_t& cands) {
+  constexpr int B = W <= 4 ? 4 : (W <= 8 ? 2 : 1);  // windows per warp whose gathers are issued together
+  constexpr int W2 = 2 * W;
+  __shared__ int s_pen[32 * W];
+  __shared__ ull s_int;
+  __shared__ int s_border;
+  const bool query = dbg_to != nullptr;
+  const bool batched = c.batched != 0;
+  const int lane = lane_id(), wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int64_t o0 = c.vtx_off[v];
+  const int d = (int)(c.vtx_off[v + 1] - o0);  // 0 < d <= kHighDegree for heavy vertices
+  const int inst = batched ? c.vinst[v] : 0;
+  const int bo = batched ? c.inst_boff[inst] : 0;
+  const int kk = batched ? c.inst_k[inst] : c.k;
+  const int from = c.part[v] - bo;
+  const int wv = c.w_v[v];
+  for (int b = threadIdx.x; b < 32 * W; b += blockDim.x) s_pen[b] = 0;
+  if (threadIdx.x == 0) {
+    s_int = 0;
+    s_border = 0;
+  }
+  __syncthreads();
+  int pen[W];
+#pragma unroll
+  for (int t = 0; t < W; ++t) pen[t] = 0;
+  long long internal = 0;
+  bool border = false;
+  for (int wb0 = 32 * B * wid; wb0 < d; wb0 += 32 * B * nw) {
+    uint32_t wd[B][W];
+    int we[B], lam[B];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const int j = wb0 + 32 * u + lane;
+#pragma unroll
+      for (int t = 0; t < W; ++t) wd[u][t] = 0;
+      we[u] = 0;
+      lam[u] = 0;
+      if (j < d) {
+        const int64_t e = c.inets[o0 + j];
+        const int w = UNIT ? 1 : __ldg(&c.w_e[e]);
+        const uint32_t* rec = c.conn + e * W2;
+        load_words<W>(rec, wd[u]);
+        const uint32_t l1 = __ldg(rec + W + (from >> 5));
+        internal += ((l1 >> (from & 31)) & 1u) ? 0 : w;  // Φ(e, from) > 1
+        we[u] = w;
+#pragma unroll
+        for (int t = 0; t < W; ++t) lam[u] += __popc(wd[u][t]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      if (wb0 + 32 * u >= d) break;  // warp-uniform
+      border = border || __ballot_sync(FULLMASK, lam[u] > 1) != 0;
+      if constexpr (UNIT) {
+#pragma unroll
+        for (int t = 0; t < W; ++t) pen[t] += __popc(transpose32(wd[u][t]));
+      } else {
+        const int np = 32 - __clz(__reduce_or_sync(FULLMASK, (unsigned)we[u]));
+        const Planes wp = make_planes(we[u], np);
+#pragma unroll
+        for (int t = 0; t < W; ++t) pen[t] += plane_sum(wp, transpose32(wd[u][t]), we[u]);
+      }
+    }
+  }
+  internal = warp_sum(internal);
+  if (lane == 0 && internal) atomicAdd(&s_int, (ull)internal);
+  if (lane == 0 && border) s_border = 1;
+#pragma unroll
+  for (int t = 0; t < W; ++t)
+    if (pen[t]) atomicAdd(&s_pen[32 * t + lane], pen[t]);
+  __syncthreads();
+  if (wid == 0) {
+    int to = from, gain = 0;
+    const bool bd = s_border != 0;
+    if (bd) {
+      int p[W], slack[W];
+#pragma unroll
+      for (int t = 0; t < W; ++t) {
+        const int b = 32 * t + lane;
+        p[t] = s_pen[b];
+        int sl = -1;
+        if (b < kk) {
+          const int64_t x = c.lmax[bo + b] - c.bw[bo + b];
+          sl = x < 0 ? -1 : (x > INT_MAX ? INT_MAX : (int)x);
+        }
+        slack[t] = sl;
+      }
+      decide<W, UNIT>(kk, from, wv, (int)s_int, zero_gain, p, slack, c.bw + bo, c.perfect + bo, to, gain);
+    }
+    if (lane == 0) {
+      if (query) {
+        dbg_to[v] = to;
+        if (dbg_gain) dbg_gain[v] = gain;
+        if (dbg_border) dbg_border[v] = bd;
+      } else {
+        int4 r = make_int4(-1, 0, (int)v, from + bo);
+        if (to != from) {
+          r.x = to + bo;
+          r.y = gain;
+          atomicAdd(reinterpret_cast<ull*>(&c.in_w[to + bo]), (ull)(int64_t)wv);
+          atomicAdd(reinterpret_cast<ull*>(&c.in_cnt[to + bo]), 1ull);
+          atomicAdd(reinterpret_cast<ull*>(&c.cand_out[from + bo]), (ull)(int64_t)wv);
+          ++cands;
+        }
+        c.rec[pos] = r;
+      }
+    }
+  }
+  __syncthreads();  // s_pen is cleared for the next vertex
+}
+
 // Sweep: the best move of every active vertex (moveVertex's isBorderNode +
 // computeMaxGainMove, label_propagation_refiner.h:82-95) on the current state.
 //
@@ -827,7 +968,7 @@ __device__ __forceinline__ void lv_vertex(const RoundCtx& c, int64_t o0, int d, 
 // mode (dbg_to != null) writes to / gain / border for every vertex (list =
 // all vertices, no zero-gain moves).
 template <int W, bool UNIT>
-__global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : (W == 4 ? LPGPU_SWEEP_MIN_BLOCKS : 3))) k_sweep(RoundCtx c, int round, int sub,
+__global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : (W == 4 ? LPGPU_SWEEP_MIN_BLOCKS : 3))) k_sweep(RoundCtx c, int round, int sub, int nheavy,
                                                              int32_t* dbg_to, int32_t* dbg_gain,
                                                              uint8_t* dbg_border) {
   constexpr int B = W <= 8 ? 2 : 1;  // windows whose gathers are issued together (k > 128)
@@ -874,12 +1015,26 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : (W == 4 ? LPGPU_S
   for (int t = 0; t < W; ++t) slack[t] = (32 * t + lane < k) ? s_slack[32 * t + lane] : -1;
   int slack_inst = -1;  // batched: instance whose block slack is in `slack`
   const int zero_gain = query ? 0 : c.zero_gain;
-  const int64_t beg = query ? 0 : c.sub_off[sub];
-  const int64_t cnt = query ? c.n : c.sub_off[sub + 1] - beg;
+  const int64_t sbeg = query ? 0 : c.sub_off[sub];
+  const int64_t total = query ? c.n : c.sub_off[sub + 1] - sbeg;
   const int W2 = 2 * W;
   int64_t pins = 0, cands = 0;
-  const int64_t wstride = ((int64_t)gridDim.x * blockDim.x);
-  for (int64_t tile = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; tile < cnt; tile += wstride) {
+  // sub-round mode: the sub-round's heavy vertices lead its list; the first
+  // `nheavy` CTAs take them one at a time while the others walk the rest
+  const int H = query ? 0 : nheavy;
+  const int64_t hcnt = H ? c.sub_off[kMaxSubrounds + 1 + sub] - sbeg : 0;
+  const int lb = (int)blockIdx.x - H;  // index among the lane-per-vertex CTAs (< 0: heavy CTA)
+  if (lb < 0) {
+    for (int64_t i = blockIdx.x; i < hcnt; i += H) {
+      const int64_t v = c.list[sbeg + i];
+      if (threadIdx.x == 0) pins += c.vtx_off[v + 1] - c.vtx_off[v];
+      heavy_vertex<W, UNIT>(c, sbeg + i, v, zero_gain, nullptr, nullptr, nullptr, cands);
+    }
+  }
+  const int64_t beg = sbeg + hcnt;
+  const int64_t cnt = lb < 0 ? 0 : total - hcnt;
+  const int64_t wstride = (int64_t)(gridDim.x - H) * blockDim.x;
+  for (int64_t tile = (int64_t)(lb < 0 ? 0 : lb) * blockDim.x + threadIdx.x - lane; tile < cnt; tile += wstride) {
     // ---- one vertex per lane
     const int64_t pos = beg + tile + lane;
     const bool valid = tile + lane < cnt;
@@ -900,19 +1055,16 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : (W == 4 ? LPGPU_S
     }
     int my_to = from, my_gain = 0;
     bool my_border = false;
-    // light vertices are evaluated here; heavy ones are deferred to k_sweep_heavy
-    bool defer = false;
+    // light vertices are evaluated here; in query mode heavy ones are deferred
+    // to k_sweep_heavy (sub-round lists keep them in the heavy CTAs' range)
+    const bool heavy = sweep_heavy(d, W, UNIT, c.max_we);
+    const bool defer = heavy && query;
     if constexpr (kLv) {
-      if (d > 0) {
-        if ((int64_t)d * c.max_we < (1 << PL))
-          lv_vertex<W, UNIT, PL>(c, o0, d, from, wv, bo, inst, batched, zero_gain, s_fmask, s_slack, s_bw, s_perf,
-                                 my_to, my_gain, my_border);
-        else
-          defer = true;
-        d = 0;
-      }
-    } else if (d > kHeavyDegree) {
-      defer = true;
+      if (d > 0 && !heavy)
+        lv_vertex<W, UNIT, PL>(c, o0, d, from, wv, bo, inst, batched, zero_gain, s_fmask, s_slack, s_bw, s_perf,
+                               my_to, my_gain, my_border);
+      d = 0;
+    } else if (heavy) {
       d = 0;
     }
     const unsigned dm = __ballot_sync(FULLMASK, defer);
@@ -1115,7 +1267,7 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : (W == 4 ? LPGPU_S
     int64_t* st = c.stats + (int64_t)round * kStats;
     atomicAdd(reinterpret_cast<ull*>(&st[kStPins]), (ull)pins);
     atomicAdd(reinterpret_cast<ull*>(&st[kStCands]), (ull)cands);
-    if (blockIdx.x == 0) atomicAdd(reinterpret_cast<ull*>(&st[kStActive]), (ull)cnt);
+    if (blockIdx.x == 0) atomicAdd(reinterpret_cast<ull*>(&st[kStActive]), (ull)total);
   }
   __syncthreads();
   for (int b = threadIdx.x; b < k; b += blockDim.x) {
@@ -1125,141 +1277,22 @@ __global__ void __launch_bounds__(kSweepThreads, (W >= 8 ? 2 : (W == 4 ? LPGPU_S
     }
     if (s_out_w[b]) atomicAdd(reinterpret_cast<ull*>(&c.cand_out[b]), s_out_w[b]);
   }
-  // the plan needs every candidate: with deferred vertices k_sweep_heavy makes it
-  if (last_cta(&c.scal[kDone]) && *(volatile int64_t*)&c.scal[kHeavyCount] == 0) plan_to(c);
+  if (last_cta(&c.scal[kDone])) plan_to(c);
 }
 
-// Heavy vertices deferred by k_sweep (summed net weight too large for the
-// lane counters, or more than kHeavyDegree incidences): one CTA per vertex,
-// whose warps split the incidence windows (lane = incidence, Λ words
-// transposed so that lane l counts block l + 32 t), sum their per-block
-// penalties in shared memory, and warp 0 decides. Its last CTA plans the
-// selection and clears the deferred count.
+// Per-vertex queries: the heavy vertices k_sweep deferred (list = all
+// vertices, positions in c.heavy), one CTA each; clears the deferred count.
 template <int W, bool UNIT>
-__global__ void __launch_bounds__(kSweepThreads) k_sweep_heavy(RoundCtx c, int round, int32_t* dbg_to,
-                                                               int32_t* dbg_gain, uint8_t* dbg_border) {
+__global__ void __launch_bounds__(kSweepThreads) k_sweep_heavy(RoundCtx c, int32_t* dbg_to, int32_t* dbg_gain,
+                                                               uint8_t* dbg_border) {
   const int64_t nh = *(volatile int64_t*)&c.scal[kHeavyCount];
-  if (nh == 0) return;  // the sweep planned already
-  constexpr int B = W <= 4 ? 4 : (W <= 8 ? 2 : 1);  // windows per warp whose gathers are issued together
-  constexpr int W2 = 2 * W;
-  __shared__ int s_pen[32 * W];
-  __shared__ ull s_int;
-  __shared__ int s_border;
-  const bool query = dbg_to != nullptr;
-  const bool batched = c.batched != 0;
-  const int lane = lane_id(), wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int zero_gain = query ? 0 : c.zero_gain;
+  if (nh == 0) return;
   int64_t cands = 0;
   for (int64_t i = blockIdx.x; i < nh; i += gridDim.x) {
-    const int32_t pos = c.heavy[i];
-    const int64_t v = query ? pos : c.list[pos];
-    const int64_t o0 = c.vtx_off[v];
-    const int d = (int)(c.vtx_off[v + 1] - o0);  // 0 < d <= kHighDegree for deferred vertices
-    const int inst = batched ? c.vinst[v] : 0;
-    const int bo = batched ? c.inst_boff[inst] : 0;
-    const int kk = batched ? c.inst_k[inst] : c.k;
-    const int from = c.part[v] - bo;
-    const int wv = c.w_v[v];
-    for (int b = threadIdx.x; b < 32 * W; b += blockDim.x) s_pen[b] = 0;
-    if (threadIdx.x == 0) {
-      s_int = 0;
-      s_border = 0;
-    }
-    __syncthreads();
-    int pen[W];
-#pragma unroll
-    for (int t = 0; t < W; ++t) pen[t] = 0;
-    long long internal = 0;
-    bool border = false;
-    for (int wb0 = 32 * B * wid; wb0 < d; wb0 += 32 * B * nw) {
-      uint32_t wd[B][W];
-      int we[B], lam[B];
-#pragma unroll
-      for (int u = 0; u < B; ++u) {
-        const int j = wb0 + 32 * u + lane;
-#pragma unroll
-        for (int t = 0; t < W; ++t) wd[u][t] = 0;
-        we[u] = 0;
-        lam[u] = 0;
-        if (j < d) {
-          const int64_t e = c.inets[o0 + j];
-          const int w = UNIT ? 1 : __ldg(&c.w_e[e]);
-          const uint32_t* rec = c.conn + e * W2;
-          load_words<W>(rec, wd[u]);
-          const uint32_t l1 = __ldg(rec + W + (from >> 5));
-          internal += ((l1 >> (from & 31)) & 1u) ? 0 : w;  // Φ(e, from) > 1
-          we[u] = w;
-#pragma unroll
-          for (int t = 0; t < W; ++t) lam[u] += __popc(wd[u][t]);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < B; ++u) {
-        if (wb0 + 32 * u >= d) break;  // warp-uniform
-        border = border || __ballot_sync(FULLMASK, lam[u] > 1) != 0;
-        if constexpr (UNIT) {
-#pragma unroll
-          for (int t = 0; t < W; ++t) pen[t] += __popc(transpose32(wd[u][t]));
-        } else {
-          const int np = 32 - __clz(__reduce_or_sync(FULLMASK, (unsigned)we[u]));
-          const Planes wp = make_planes(we[u], np);
-#pragma unroll
-          for (int t = 0; t < W; ++t) pen[t] += plane_sum(wp, transpose32(wd[u][t]), we[u]);
-        }
-      }
-    }
-    internal = warp_sum(internal);
-    if (lane == 0 && internal) atomicAdd(&s_int, (ull)internal);
-    if (lane == 0 && border) s_border = 1;
-#pragma unroll
-    for (int t = 0; t < W; ++t)
-      if (pen[t]) atomicAdd(&s_pen[32 * t + lane], pen[t]);
-    __syncthreads();
-    if (wid == 0) {
-      int to = from, gain = 0;
-      const bool bd = s_border != 0;
-      if (bd) {
-        int p[W], slack[W];
-#pragma unroll
-        for (int t = 0; t < W; ++t) {
-          const int b = 32 * t + lane;
-          p[t] = s_pen[b];
-          int sl = -1;
-          if (b < kk) {
-            const int64_t x = c.lmax[bo + b] - c.bw[bo + b];
-            sl = x < 0 ? -1 : (x > INT_MAX ? INT_MAX : (int)x);
-          }
-          slack[t] = sl;
-        }
-        decide<W, UNIT>(kk, from, wv, (int)s_int, zero_gain, p, slack, c.bw + bo, c.perfect + bo, to, gain);
-      }
-      if (lane == 0) {
-        if (query) {
-          dbg_to[v] = to;
-          if (dbg_gain) dbg_gain[v] = gain;
-          if (dbg_border) dbg_border[v] = bd;
-        } else {
-          int4 r = make_int4(-1, 0, (int)v, from + bo);
-          if (to != from) {
-            r.x = to + bo;
-            r.y = gain;
-            atomicAdd(reinterpret_cast<ull*>(&c.in_w[to + bo]), (ull)(int64_t)wv);
-            atomicAdd(reinterpret_cast<ull*>(&c.in_cnt[to + bo]), 1ull);
-            atomicAdd(reinterpret_cast<ull*>(&c.cand_out[from + bo]), (ull)(int64_t)wv);
-            ++cands;
-          }
-          c.rec[pos] = r;
-        }
-      }
-    }
-    __syncthreads();  // s_pen is cleared for the next vertex
+    const int32_t v = c.heavy[i];
+    heavy_vertex<W, UNIT>(c, v, v, 0, dbg_to, dbg_gain, dbg_border, cands);
   }
-  if (!query && threadIdx.x == 0 && cands)
-    atomicAdd(reinterpret_cast<ull*>(&c.stats[(int64_t)round * kStats + kStCands]), (ull)cands);
-  if (last_cta(&c.scal[kDone])) {
-    if (threadIdx.x == 0) c.scal[kHeavyCount] = 0;
-    if (!query) plan_to(c);
-  }
+  if (last_cta(&c.scal[kDone]) && threadIdx.x == 0) c.scal[kHeavyCount] = 0;
 }
 
 #define LPGPU_DISPATCH_W(W, ...)          \
@@ -1294,11 +1327,21 @@ static cudaError_t launch_sweep(const Launch& L, const RoundCtx& c, int round, i
     auto kern = c.unit_nets ? k_sweep<kW, true> : k_sweep<kW, false>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int per_sm = occupancy((const void*)kern, kSweepThreads, smem);
-    kern<<<grid_for(L, c.n * 4, kSweepThreads, per_sm), kSweepThreads, smem, L.st>>>(c, round, sub, to, gain, border);
+    int grid = grid_for(L, c.n * 4, kSweepThreads, per_sm);
+    // CTAs for the heavy vertices: their share of the work, at least two
+    int H = 0;
+    if (!to && c.heavy_share > 0) {
+      H = std::max(2, (int)((int64_t)grid * c.heavy_share / 1000));
+      H = std::min(H, std::max(1, grid - 1));
+      grid = std::max(grid, H + 1);
+    }
+    kern<<<grid, kSweepThreads, smem, L.st>>>(c, round, sub, H, to, gain, border);
     LAUNCHED("k_sweep");
-    auto heavy = c.unit_nets ? k_sweep_heavy<kW, true> : k_sweep_heavy<kW, false>;
-    heavy<<<grid_for(L, c.n, kSweepThreads, 2), kSweepThreads, 0, L.st>>>(c, round, to, gain, border);
-    LAUNCHED("k_sweep_heavy");
+    if (to) {
+      auto heavy = c.unit_nets ? k_sweep_heavy<kW, true> : k_sweep_heavy<kW, false>;
+      heavy<<<grid_for(L, c.n, kSweepThreads, 2), kSweepThreads, 0, L.st>>>(c, to, gain, border);
+      LAUNCHED("k_sweep_heavy");
+    }
   });
   return cudaSuccess;
 }
@@ -1538,75 +1581,117 @@ cudaError_t launch_mark_list(const Launch& L, const RoundCtx& c, const int32_t* 
   return cudaGetLastError();
 }
 
-// Per tile, flagged vertices per sub-round (tile_cnt[s * tiles + tile]).
-// All 32 vertices of an aligned chunk share one sub-round.
-// Batched sessions hash instance-local ids (so that an instance gets the same
-// sub-rounds alone and in a batch): then a chunk may straddle two instances and
-// every vertex computes its own sub-round.
+// Active-list binning. Each round's active vertices are grouped by sub-round
+// and, inside a sub-round, by class (vertex_class): the heavy vertices first,
+// which the sweep gives to whole CTAs, then four degree classes, since the
+// lane-per-vertex sweep runs a warp until its longest incidence list is done.
+// Bin b = sub-round * kDegClasses + class; tile_cnt[b * tiles + tile] counts
+// the tile's flagged vertices per bin. Which position a vertex takes inside
+// its sub-round changes no result.
+//
+// All 32 vertices of an aligned chunk share one sub-round. Batched sessions
+// hash instance-local ids (so that an instance gets the same sub-rounds alone
+// and in a batch): then a chunk may straddle two instances and every vertex
+// computes its own sub-round.
 __device__ __forceinline__ int vertex_subround(const int32_t* vinst, const int64_t* inst_voff, int64_t v,
                                                int round, int S) {
   return subround_of(vinst ? v - inst_voff[vinst[v]] : v, round, S);
 }
 
+// Heavy vertices (sweep_heavy) -> 0; the others by the groups of four
+// incidences a sweep lane walks: 0-4 incidences -> 1, 5-8 -> 2, 9-12 -> 3,
+// more -> 4.
+struct ClassRule {
+  const int64_t* vtx_off;
+  int W, unit_nets, max_we;
+};
+__device__ __forceinline__ int vertex_class(const ClassRule& r, int64_t v) {
+  const int64_t d = r.vtx_off[v + 1] - r.vtx_off[v];
+  if (sweep_heavy(d, r.W, r.unit_nets, r.max_we)) return 0;
+  const int64_t g = (d + 3) >> 2;
+  return g <= 1 ? 1 : (g >= kDegClasses - 1 ? kDegClasses - 1 : (int)g);
+}
+
 __global__ void __launch_bounds__(1024) k_bin_count(const uint8_t* __restrict__ flag, int64_t n,
                                                     int round, int S, int64_t tiles,
-                                                    int64_t* __restrict__ tile_cnt,
+                                                    int64_t* __restrict__ tile_cnt, ClassRule rule,
                                                     const int32_t* __restrict__ vinst,
                                                     const int64_t* __restrict__ inst_voff) {
-  __shared__ int s_cnt[kMaxSubrounds];
-  if (threadIdx.x < S) s_cnt[threadIdx.x] = 0;
+  __shared__ int s_cnt[kMaxSubrounds * kDegClasses];
+  const int bins = S * kDegClasses;
+  for (int i = threadIdx.x; i < bins; i += blockDim.x) s_cnt[i] = 0;
   __syncthreads();
   const int64_t v = blockIdx.x * (int64_t)kTile + threadIdx.x;
   const bool f = v < n && flag[v];
+  const int cls = f ? vertex_class(rule, v) : 0;
   if (vinst) {
-    if (f) atomicAdd(&s_cnt[vertex_subround(vinst, inst_voff, v, round, S)], 1);
+    if (f) atomicAdd(&s_cnt[vertex_subround(vinst, inst_voff, v, round, S) * kDegClasses + cls], 1);
   } else {
-    const unsigned bal = __ballot_sync(FULLMASK, f);
-    if (lane_id() == 0 && bal) atomicAdd(&s_cnt[subround_of(v, round, S)], __popc(bal));
+    const int sub = subround_of(v, round, S);
+#pragma unroll
+    for (int q = 0; q < kDegClasses; ++q) {
+      const unsigned bal = __ballot_sync(FULLMASK, f && cls == q);
+      if (lane_id() == 0 && bal) atomicAdd(&s_cnt[sub * kDegClasses + q], __popc(bal));
+    }
   }
   __syncthreads();
-  if (threadIdx.x < S) tile_cnt[threadIdx.x * tiles + blockIdx.x] = s_cnt[threadIdx.x];
+  for (int i = threadIdx.x; i < bins; i += blockDim.x) tile_cnt[i * tiles + blockIdx.x] = s_cnt[i];
 }
 
-// Writes each sub-round's flagged vertices in increasing id order and clears
-// the flags. Sub-round s occupies list[tile_off[s * tiles] .. tile_off[(s+1) * tiles]).
+// Writes each bin's flagged vertices (in increasing id order for one
+// instance) and clears the flags. Sub-round s occupies
+// list[tile_off[s * kDegClasses * tiles] .. tile_off[(s + 1) * kDegClasses * tiles]).
 __global__ void __launch_bounds__(1024) k_bin_scatter(uint8_t* __restrict__ flag, int64_t n, int round,
                                                       int S, int64_t tiles,
                                                       const int64_t* __restrict__ tile_off,
-                                                      int32_t* __restrict__ list,
+                                                      int32_t* __restrict__ list, ClassRule rule,
                                                       const int32_t* __restrict__ vinst,
                                                       const int64_t* __restrict__ inst_voff) {
-  __shared__ int s_cnt[32];
+  __shared__ int s_cnt[32][kDegClasses];    // per warp and class: flagged vertices
+  __shared__ int64_t s_base[32][kDegClasses];
   __shared__ int s_sub[32];
-  __shared__ int64_t s_base[32];
-  __shared__ unsigned long long s_cur[kMaxSubrounds];
-  const int w = threadIdx.x >> 5;
+  __shared__ unsigned long long s_cur[kMaxSubrounds * kDegClasses];
+  const int w = threadIdx.x >> 5, lane = lane_id();
   const int64_t v = blockIdx.x * (int64_t)kTile + threadIdx.x;
   const bool f = v < n && flag[v];
+  const int cls = f ? vertex_class(rule, v) : 0;
   if (vinst) {
-    // per-vertex sub-rounds; positions inside a (tile, sub-round) segment are
-    // taken in arrival order (nothing depends on the order inside a list)
-    if (threadIdx.x < S) s_cur[threadIdx.x] = (unsigned long long)tile_off[threadIdx.x * tiles + blockIdx.x];
+    // per-vertex sub-rounds; positions inside a (tile, bin) segment are taken
+    // in arrival order
+    for (int i = threadIdx.x; i < S * kDegClasses; i += blockDim.x) {
+      const int sub = i / kDegClasses, q = i - sub * kDegClasses;
+      s_cur[i] = (unsigned long long)tile_off[(sub * kDegClasses + q) * tiles + blockIdx.x];
+    }
     __syncthreads();
     if (f) {
-      const int sr = vertex_subround(vinst, inst_voff, v, round, S);
-      list[atomicAdd(&s_cur[sr], 1ull)] = (int32_t)v;
+      const int b = vertex_subround(vinst, inst_voff, v, round, S) * kDegClasses + cls;
+      list[atomicAdd(&s_cur[b], 1ull)] = (int32_t)v;
       flag[v] = 0;
     }
     return;
   }
-  const unsigned bal = __ballot_sync(FULLMASK, f);
-  const int sub = subround_of(blockIdx.x * (int64_t)kTile + w * 32, round, S);
-  if (lane_id() == 0) { s_cnt[w] = __popc(bal); s_sub[w] = sub; }
+  unsigned mine = 0;
+#pragma unroll
+  for (int q = 0; q < kDegClasses; ++q) {
+    const unsigned bal = __ballot_sync(FULLMASK, f && cls == q);
+    if (q == cls) mine = bal;
+    if (lane == 0) s_cnt[w][q] = __popc(bal);
+  }
+  if (lane == 0) s_sub[w] = subround_of(blockIdx.x * (int64_t)kTile + w * 32, round, S);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int64_t run[kMaxSubrounds];
-    for (int s = 0; s < S; ++s) run[s] = tile_off[s * tiles + blockIdx.x];
-    for (int i = 0; i < 32; ++i) { s_base[i] = run[s_sub[i]]; run[s_sub[i]] += s_cnt[i]; }
+  if (threadIdx.x < 32 * kDegClasses) {
+    // base of (warp ww, class q): the bin's tile offset plus the class-q
+    // vertices of earlier warps of this tile in the same sub-round
+    const int ww = threadIdx.x & 31, q = threadIdx.x >> 5;
+    const int sub = s_sub[ww];
+    int64_t base = tile_off[(sub * kDegClasses + q) * tiles + blockIdx.x];
+    for (int x = 0; x < ww; ++x)
+      if (s_sub[x] == sub) base += s_cnt[x][q];
+    s_base[ww][q] = base;
   }
   __syncthreads();
   if (f) {
-    list[s_base[w] + __popc(bal & lanemask_lt())] = (int32_t)v;
+    list[s_base[w][cls] + __popc(mine & lanemask_lt())] = (int32_t)v;
     flag[v] = 0;
   }
 }
@@ -1614,9 +1699,12 @@ __global__ void __launch_bounds__(1024) k_bin_scatter(uint8_t* __restrict__ flag
 __global__ void k_sub_offsets(const int64_t* __restrict__ tile_off, const int64_t* __restrict__ tile_cnt,
                               int S, int64_t tiles, int64_t* __restrict__ sub_off, int64_t* scal) {
   const int s = threadIdx.x;
-  if (s < S) sub_off[s] = tile_off[s * tiles];
+  if (s < S) {
+    sub_off[s] = tile_off[(int64_t)s * kDegClasses * tiles];
+    sub_off[kMaxSubrounds + 1 + s] = tile_off[((int64_t)s * kDegClasses + 1) * tiles];  // end of the heavy class
+  }
   if (s == 0) {
-    const int64_t last = (int64_t)S * tiles - 1;
+    const int64_t last = (int64_t)S * kDegClasses * tiles - 1;
     sub_off[S] = tile_off[last] + tile_cnt[last];
     scal[kEpoch] += 1;  // new round: fresh activation stamp
   }
@@ -1673,12 +1761,14 @@ cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int
   Scope sc(timer, "bin_active");
   const int64_t tiles = std::max<int64_t>(1, (c.n + kTile - 1) / kTile);
   const int32_t* vinst = c.batched ? c.vinst : nullptr;
-  k_bin_count<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_cnt, vinst,
+  const ClassRule rule{c.vtx_off, c.W, c.unit_nets, c.max_we};
+  k_bin_count<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_cnt, rule, vinst,
                                                    c.inst_voff);
   LAUNCHED("k_bin_count");
-  cudaError_t e = scan_exclusive_i64(tile_cnt, tile_off, S * tiles, scan_tmp, scan_tmp_elems, L.st);
+  cudaError_t e =
+      scan_exclusive_i64(tile_cnt, tile_off, (int64_t)S * kDegClasses * tiles, scan_tmp, scan_tmp_elems, L.st);
   if (e != cudaSuccess) return e;
-  k_bin_scatter<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_off, c.list,
+  k_bin_scatter<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_off, c.list, rule,
                                                      vinst, c.inst_voff);
   LAUNCHED("k_bin_scatter");
   k_sub_offsets<<<1, 64, 0, L.st>>>(tile_off, tile_cnt, S, tiles, c.sub_off, c.scal);

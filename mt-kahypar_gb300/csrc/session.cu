@@ -84,6 +84,7 @@ struct lpgpu_session_s {
   bool has_hg = false;
   int64_t n = 0, m = 0, P = 0;
   int64_t total_vw = 0;
+  int64_t deg_inc[kDegBuckets] = {};  // incidences per log2 degree bucket
   bool unit_nets = true;
   int32_t max_we = 0;
   DevBuf<int64_t> net_off, vtx_off;
@@ -136,6 +137,23 @@ struct lpgpu_session_s {
 
   Launch launch() const { return Launch{st, num_sms}; }
 
+  // Per mille of the sweep's work in heavy vertices, from the degree
+  // histogram: a bucket counts as heavy when its largest degree is; a heavy
+  // incidence costs about twice a light one. 0 only when no vertex is heavy.
+  int32_t heavy_share() const {
+    double heavy = 0, light = 0;
+    for (int j = 0; j < kDegBuckets; ++j) {
+      const int64_t top = j >= 62 ? INT64_MAX : (int64_t(2) << j) - 1;
+      if (sweep_heavy(top < kHighDegree ? top : kHighDegree, W, unit_nets ? 1 : 0, max_we))
+        heavy += (double)deg_inc[j];
+      else
+        light += (double)deg_inc[j];
+    }
+    if (heavy == 0) return 0;
+    const int x = (int)(1000.0 * 2.0 * heavy / (2.0 * heavy + light));
+    return x < 1 ? 1 : x;
+  }
+
   RoundCtx ctx(const lpgpu_config* cfg = nullptr) {
     RoundCtx c{};
     c.n = n;
@@ -150,6 +168,7 @@ struct lpgpu_session_s {
     c.w_e = w_e.p;
     c.unit_nets = unit_nets ? 1 : 0;
     c.max_we = max_we;
+    c.heavy_share = heavy_share();
     c.part = part.p;
     c.phi = phi.p;
     c.conn = conn.p;
@@ -396,12 +415,13 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
   CK(s->seg_w.alloc(n, fp));
   CK(s->heavy.alloc(n, fp));
   CK(s->revl.alloc(n, fp));
-  CK(s->vout.alloc(kVSums + 2 * (int64_t)I, fp));
-  CK(s->sub_off.alloc(kMaxSubrounds + 1, fp));
+  CK(s->vout.alloc(std::max<int64_t>(kVSums + 2 * (int64_t)I, kDegBuckets), fp));
+  CK(s->sub_off.alloc(2 * kMaxSubrounds + 1, fp));
   const int64_t tiles = tiles_for(n);
-  CK(s->tile_cnt.alloc(kMaxSubrounds * tiles, fp));
-  CK(s->tile_off.alloc(kMaxSubrounds * tiles, fp));
-  s->scan_tmp_n = std::max<int64_t>(1, std::max(scan_tmp_elems(n + 1), scan_tmp_elems(kMaxSubrounds * tiles)));
+  CK(s->tile_cnt.alloc(kMaxSubrounds * kDegClasses * tiles, fp));
+  CK(s->tile_off.alloc(kMaxSubrounds * kDegClasses * tiles, fp));
+  s->scan_tmp_n =
+      std::max<int64_t>(1, std::max(scan_tmp_elems(n + 1), scan_tmp_elems(kMaxSubrounds * kDegClasses * tiles)));
   CK(s->scan_tmp.alloc(s->scan_tmp_n, fp));
   cudaStream_t st = s->st;
   const Launch L = s->launch();
@@ -498,7 +518,9 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
   s->max_we = (int32_t)h[kVMaxWe];
   s->unit_nets = h[kVNonUnit] == 0;
   CK(launch_build_incidence(s->launch(), n, m, s->net_off.p, s->pins.p, s->vtx_off.p, s->inets.p,
-                            reinterpret_cast<int64_t*>(s->seg_key.p), s->scan_tmp.p, s->scan_tmp_n));
+                            reinterpret_cast<int64_t*>(s->seg_key.p), s->scan_tmp.p, s->scan_tmp_n,
+                            s->vout.p));
+  CK(cudaMemcpyAsync(s->deg_inc, s->vout.p, sizeof(s->deg_inc), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   s->has_hg = true;
   return LPGPU_OK;
@@ -1183,8 +1205,8 @@ int64_t lpgpu_estimate_footprint(int64_t n, int64_t m, int64_t P, int32_t k, int
   int64_t b = 0;
   b += 8 * (m + 1) + 8 * (n + 1) + 4 * P * 2 + 4 * n + 4 * m;          // CSR + weights
   b += 4 * m + 4 * n + n + n + 16 * n + 8 * n + 4 * n + 8 * n;         // epoch, list, flags, status, rec, seg, queues
-  b += 8 * (kMaxSubrounds + 1) + 2 * 8 * kMaxSubrounds * tiles;        // sub-round bins
-  b += 8 * (scan_tmp_elems(std::max(n + 1, kMaxSubrounds * tiles)) + 1);
+  b += 8 * (2 * kMaxSubrounds + 1) + 2 * 8 * kMaxSubrounds * kDegClasses * tiles;  // sub-round bins
+  b += 8 * (scan_tmp_elems(std::max(n + 1, kMaxSubrounds * kDegClasses * tiles)) + 1);
   b += 4 * n + 4 * m * (int64_t)k + 8 * m * W;                         // part, Φ, Λ + Λ1
   b += 8 * (3 * k + 7 * k + 1 + 2 * k) + 2 * k + 8 * 64 + 8 * 8;       // per-block, stats, scalars
   return b;

@@ -227,6 +227,21 @@ def test_lp_rounds_bit_exact_plain_small(lp, orc, mode):
     out[0].close()
 
 
+@pytest.mark.parametrize("threshold", [40, 64, 65, 1000])
+@pytest.mark.parametrize("seed", range(2))
+def test_activation_of_large_nets(lp, orc, threshold, seed):
+    """Nets of up to 200 pins (several 32-pin groups in the stamped-net
+    expansion), with activation thresholds below, at and above the 32- and
+    64-pin group boundaries."""
+    from lpgpu import gen
+    inst = gen.random_small(seed, n=1200, m=400, k=[3, 16][seed], max_size=200)
+    assert np.diff(inst.hg.net_off).max() > 65
+    for mode in (LP_MODES[1], LP_MODES[2]):
+        out = run_both(lp, orc, inst, 5, mode, threshold=threshold)
+        assert_same_run(*out, orc, inst)
+        out[0].close()
+
+
 def test_refinement_nodes_and_threshold(lp, orc):
     from lpgpu import gen
     inst = gen.random_small(5, n=500, m=600, k=4)
