@@ -55,8 +55,8 @@ def parse_args():
                     help="batch: instances (default 4096); served: requests (default 256)")
     ap.add_argument("--rate", type=float, default=2000.0, help="served: Poisson arrival rate (req/s)")
     ap.add_argument("--slots", type=int, default=2, help="served: concurrent batched sessions")
-    ap.add_argument("--batch-pins", type=float, default=None,
-                    help="served: a batch stops growing at this many pins (default: memory budget only)")
+    ap.add_argument("--batch-pins", type=float, default=1e8,
+                    help="served: a batch stops growing at this many pins (0: memory budget only)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--subrounds", type=int, default=8)
     ap.add_argument("--no-baseline", action="store_true", help="skip the CPU baseline leg")
@@ -494,7 +494,7 @@ def served_arm(args):
     serve.replay(serve.RefineServer(slots=args.slots), warm)
     serve.plain_loop(warm)
     rs = requests()
-    cap = None if args.batch_pins is None else int(args.batch_pins)
+    cap = int(args.batch_pins) if args.batch_pins and args.batch_pins > 0 else None
     st_s = serve.replay(serve.RefineServer(slots=args.slots, subrounds=args.subrounds, max_batch_pins=cap), rs)
     rp = requests()
     st_p = serve.plain_loop(rp, subrounds=args.subrounds)

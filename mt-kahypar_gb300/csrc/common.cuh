@@ -22,8 +22,12 @@ constexpr int64_t kHighDegree = 100000;
 constexpr int kChunkShift = 5;
 constexpr int kMaxSubrounds = 64;
 // Classes inside a sub-round's active list (see k_bin_count): heavy
-// vertices, then four degree classes.
-constexpr int kDegClasses = 5;
+// vertices, then LPGPU_DEG_CLASSES - 1 degree classes (at least one).
+#ifndef LPGPU_DEG_CLASSES
+#define LPGPU_DEG_CLASSES 3
+#endif
+constexpr int kDegClasses = LPGPU_DEG_CLASSES;
+static_assert(kDegClasses >= 2, "the heavy class and at least one other");
 // Log2 buckets of the upload-time degree histogram.
 constexpr int kDegBuckets = 32;
 // Above this degree the warp windows of the k > 128 sweep hand a vertex to a whole CTA.

@@ -1599,8 +1599,8 @@ __device__ __forceinline__ int vertex_subround(const int32_t* vinst, const int64
 }
 
 // Heavy vertices (sweep_heavy) -> 0; the others by the groups of four
-// incidences a sweep lane walks: 0-4 incidences -> 1, 5-8 -> 2, 9-12 -> 3,
-// more -> 4.
+// incidences a sweep lane walks: 0-4 incidences -> 1, 5-8 -> 2, ..., capped
+// at the last class.
 struct ClassRule {
   const int64_t* vtx_off;
   int W, unit_nets, max_we;
@@ -1609,7 +1609,7 @@ __device__ __forceinline__ int vertex_class(const ClassRule& r, int64_t v) {
   const int64_t d = r.vtx_off[v + 1] - r.vtx_off[v];
   if (sweep_heavy(d, r.W, r.unit_nets, r.max_we)) return 0;
   const int64_t g = (d + 3) >> 2;
-  return g <= 1 ? 1 : (g >= kDegClasses - 1 ? kDegClasses - 1 : (int)g);
+  return g <= 1 ? 1 : (g >= kDegClasses - 1 ? kDegClasses - 1 : (int)g);  // D = 2: always 1
 }
 
 __global__ void __launch_bounds__(1024) k_bin_count(const uint8_t* __restrict__ flag, int64_t n,

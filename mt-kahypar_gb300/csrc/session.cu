@@ -13,31 +13,53 @@ namespace lpgpu {
 static thread_local std::string g_error;
 void set_error(const std::string& msg) { g_error = msg; }
 
+// Device memory of a session: a session-owned pool, allocations and frees
+// ordered on the session's stream (no device-wide synchronisation, as a
+// cudaFree would impose on every other session), and the bytes held by the
+// session's buffers.
+struct Mem {
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t st = nullptr;
+  int64_t bytes = 0;
+};
+
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
   size_t count = 0;
-  cudaError_t alloc(size_t n, int64_t* footprint) {
+  cudaError_t alloc(size_t n, Mem* mem) {
     if (n == count && p) return cudaSuccess;
-    release(footprint);
+    release(mem);
     if (n == 0) return cudaSuccess;
-    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&p), n * sizeof(T), mem->pool, mem->st);
     if (e != cudaSuccess) {
       p = nullptr;
       return e;
     }
     count = n;
-    *footprint += (int64_t)(n * sizeof(T));
+    mem->bytes += (int64_t)(n * sizeof(T));
     return cudaSuccess;
   }
-  void release(int64_t* footprint) {
+  void release(Mem* mem) {
     if (p) {
-      cudaFree(p);
-      *footprint -= (int64_t)(count * sizeof(T));
+      cudaFreeAsync(p, mem->st);
+      mem->bytes -= (int64_t)(count * sizeof(T));
     }
     p = nullptr;
     count = 0;
   }
+};
+
+// A temporary device buffer of one call, freed (stream-ordered) on every
+// return path.
+template <typename T>
+struct TmpBuf {
+  DevBuf<T> b;
+  Mem m;
+  TmpBuf(const Mem& owner) : m{owner.pool, owner.st, 0} {}
+  ~TmpBuf() { b.release(&m); }
+  cudaError_t alloc(size_t n) { return b.alloc(n, &m); }
+  T* p() const { return b.p; }
 };
 
 static int word_count(int k) { return (k + 31) / 32; }
@@ -79,7 +101,7 @@ struct lpgpu_session_s {
   int device = 0;
   cudaStream_t st = nullptr;
   int num_sms = 1;
-  int64_t footprint = 0;
+  Mem mem;
   // hypergraph
   bool has_hg = false;
   int64_t n = 0, m = 0, P = 0;
@@ -109,9 +131,9 @@ struct lpgpu_session_s {
   DevBuf<uint8_t> gc_moved;
   void drop_gain_cache() {
     gc_valid = false;
-    gc_benefit.release(&footprint);
-    gc_penalty.release(&footprint);
-    gc_moved.release(&footprint);
+    gc_benefit.release(&mem);
+    gc_penalty.release(&mem);
+    gc_moved.release(&mem);
   }
   int64_t scan_tmp_n = 0;
   // batched sessions (lpgpu_session_upload_batch): instance ranges and blocks
@@ -225,36 +247,45 @@ struct lpgpu_session_s {
 
   void release_partition() {
     drop_gain_cache();
-    part.release(&footprint);
-    phi.release(&footprint);
-    conn.release(&footprint);
-    bw.release(&footprint);
-    lmax.release(&footprint);
-    perfect.release(&footprint);
-    blk64.release(&footprint);
-    thr.release(&footprint);
-    over.release(&footprint);
-    over_ids.release(&footprint);
-    inst_boff.release(&footprint);
-    inst_k.release(&footprint);
-    inst_delta.release(&footprint);
+    part.release(&mem);
+    phi.release(&mem);
+    conn.release(&mem);
+    bw.release(&mem);
+    lmax.release(&mem);
+    perfect.release(&mem);
+    blk64.release(&mem);
+    thr.release(&mem);
+    over.release(&mem);
+    over_ids.release(&mem);
+    inst_boff.release(&mem);
+    inst_k.release(&mem);
+    inst_delta.release(&mem);
     has_part = false;
   }
+  // Returns pooled memory beyond the buffers in use plus 1 GiB of slack
+  // (call after a synchronisation: pending frees still count as in use).
+  void trim() {
+    uint64_t reserved = 0;
+    if (cudaMemPoolGetAttribute(mem.pool, cudaMemPoolAttrReservedMemCurrent, &reserved) != cudaSuccess) return;
+    const uint64_t keep = (uint64_t)mem.bytes + (1ull << 30);
+    if (reserved > keep) cudaMemPoolTrimTo(mem.pool, keep);
+  }
+
   void release_all() {
     release_partition();
     DevBuf<int64_t>* b64[] = {&net_off, &vtx_off, &sub_off, &stats, &tile_cnt, &tile_off, &scan_tmp};
-    for (auto* b : b64) b->release(&footprint);
+    for (auto* b : b64) b->release(&mem);
     DevBuf<int32_t>* b32[] = {&pins, &inets, &w_v, &w_e, &list, &net_epoch, &seg_w, &heavy, &revl};
-    for (auto* b : b32) b->release(&footprint);
-    next_flag.release(&footprint);
-    saved_part.release(&footprint);
-    vinst.release(&footprint);
-    inst_voff.release(&footprint);
-    inst_noff.release(&footprint);
-    vout.release(&footprint);
-    status.release(&footprint);
-    rec.release(&footprint);
-    seg_key.release(&footprint);
+    for (auto* b : b32) b->release(&mem);
+    next_flag.release(&mem);
+    saved_part.release(&mem);
+    vinst.release(&mem);
+    inst_voff.release(&mem);
+    inst_noff.release(&mem);
+    vout.release(&mem);
+    status.release(&mem);
+    rec.release(&mem);
+    seg_key.release(&mem);
     has_hg = false;
   }
 };
@@ -355,9 +386,25 @@ lpgpu_status lpgpu_session_create(int32_t device, lpgpu_session** out) {
     return cuda_fail(e, "cudaStreamCreate");
   }
   s->timer.st = s->st;
-  if ((e = s->scal.alloc(kScalars, &s->footprint)) != cudaSuccess ||
-      (e = cudaMemset(s->scal.p, 0, sizeof(int64_t) * kScalars)) != cudaSuccess) {
-    s->scal.release(&s->footprint);
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  if ((e = cudaMemPoolCreate(&s->mem.pool, &props)) != cudaSuccess) {
+    cudaStreamDestroy(s->st);
+    delete s;
+    return cuda_fail(e, "cudaMemPoolCreate");
+  }
+  // freed blocks stay in the pool for the next upload; trim() returns them
+  uint64_t keep = UINT64_MAX;
+  cudaMemPoolSetAttribute(s->mem.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  s->mem.st = s->st;
+  if ((e = s->scal.alloc(kScalars, &s->mem)) != cudaSuccess ||
+      (e = cudaMemsetAsync(s->scal.p, 0, sizeof(int64_t) * kScalars, s->st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s->st)) != cudaSuccess) {
+    s->scal.release(&s->mem);
+    cudaStreamSynchronize(s->st);
+    cudaMemPoolDestroy(s->mem.pool);
     cudaStreamDestroy(s->st);
     delete s;
     return cuda_fail(e, "alloc scalars");
@@ -372,10 +419,12 @@ lpgpu_status lpgpu_session_destroy(lpgpu_session* s) {
     DeviceGuard g(s->device);
     cudaStreamSynchronize(s->st);
     s->release_all();
-    s->scal.release(&s->footprint);
+    s->scal.release(&s->mem);
     for (auto& ev : s->slots)
       if (ev) cudaEventDestroy(ev);
     if (s->graph) cudaGraphExecDestroy(s->graph);
+    cudaStreamSynchronize(s->st);
+    cudaMemPoolDestroy(s->mem.pool);
     cudaStreamDestroy(s->st);
   }
   delete s;
@@ -399,7 +448,7 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
   s->m = m;
   s->P = P;
   const int32_t I = inst_voff ? num_inst : 1;
-  int64_t* fp = &s->footprint;
+  Mem* fp = &s->mem;
   CK(s->net_off.alloc(m + 1, fp));
   CK(s->vtx_off.alloc(n + 1, fp));
   CK(s->pins.alloc(P, fp));
@@ -476,13 +525,11 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
     CK(cudaMemcpyAsync(s->inst_voff.p, inst_voff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(s->inst_noff.p, inst_noff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
     if (insts) {  // local ids to union ids
-      DevBuf<int64_t> poff;
-      int64_t tmpfp = 0;
-      CK(poff.alloc(I + 1, &tmpfp));
-      CK(cudaMemcpyAsync(poff.p, inst_poff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
-      CK(launch_rebase_instances(L, I, s->inst_voff.p, s->inst_noff.p, poff.p, s->net_off.p, s->pins.p));
+      TmpBuf<int64_t> poff(s->mem);
+      CK(poff.alloc(I + 1));
+      CK(cudaMemcpyAsync(poff.p(), inst_poff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
+      CK(launch_rebase_instances(L, I, s->inst_voff.p, s->inst_noff.p, poff.p(), s->net_off.p, s->pins.p));
       CK(cudaStreamSynchronize(st));
-      poff.release(&tmpfp);
     }
   } else {
     s->vinst.release(fp);
@@ -523,6 +570,7 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
   CK(cudaMemcpyAsync(s->deg_inc, s->vout.p, sizeof(s->deg_inc), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   s->has_hg = true;
+  s->trim();
   return LPGPU_OK;
 }
 
@@ -584,7 +632,7 @@ static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax
   s->k = K;
   s->kmax = kmax;
   s->W = word_class_of(kmax);
-  int64_t* fp = &s->footprint;
+  Mem* fp = &s->mem;
   // same-size buffers are kept from the previous partition
   CK(s->part.alloc(s->n, fp));
   CK(s->phi.alloc((size_t)s->m * kmax, fp));
@@ -629,6 +677,7 @@ static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax
   CK(cudaStreamSynchronize(st));
   s->h_perfect = hp;
   s->has_part = true;
+  s->trim();
   return LPGPU_OK;
 }
 
@@ -725,27 +774,22 @@ lpgpu_status lpgpu_session_project_partition(lpgpu_session* fine, const lpgpu_se
   if (fine->n > 0 && !fine_to_coarse) return invalid("null fine-to-coarse map");
   DeviceGuard g(fine->device);
   CK(cudaStreamSynchronize(coarse->st));
-  int64_t fp = 0;
-  DevBuf<int32_t> map, proj;
-  DevBuf<int64_t> check;
-  CK(map.alloc(fine->n, &fp));
-  CK(proj.alloc(fine->n, &fp));
-  CK(check.alloc(1, &fp));
+  TmpBuf<int32_t> map(fine->mem), proj(fine->mem);
+  TmpBuf<int64_t> check(fine->mem);
+  CK(map.alloc(fine->n));
+  CK(proj.alloc(fine->n));
+  CK(check.alloc(1));
   if (fine->n > 0)
-    CK(cudaMemcpyAsync(map.p, fine_to_coarse, sizeof(int32_t) * fine->n, cudaMemcpyHostToDevice, fine->st));
-  CK(launch_project(fine->launch(), fine->n, map.p, coarse->part.p, coarse->n, proj.p, check.p));
+    CK(cudaMemcpyAsync(map.p(), fine_to_coarse, sizeof(int32_t) * fine->n, cudaMemcpyHostToDevice, fine->st));
+  CK(launch_project(fine->launch(), fine->n, map.p(), coarse->part.p, coarse->n, proj.p(), check.p()));
   int64_t bad = 0;
   std::vector<int64_t> hl(coarse->k);
-  CK(cudaMemcpyAsync(&bad, check.p, sizeof(int64_t), cudaMemcpyDeviceToHost, fine->st));
+  CK(cudaMemcpyAsync(&bad, check.p(), sizeof(int64_t), cudaMemcpyDeviceToHost, fine->st));
   CK(cudaMemcpyAsync(hl.data(), coarse->lmax.p, sizeof(int64_t) * coarse->k, cudaMemcpyDeviceToHost, fine->st));
   CK(cudaStreamSynchronize(fine->st));
   if (bad) return invalid("fine-to-coarse map entry outside the coarse vertices");
   const std::vector<int64_t> hp = coarse->h_perfect;
-  const lpgpu_status st = set_partition_impl(fine, coarse->k, coarse->k, nullptr, hl, hp, nullptr, proj.p);
-  map.release(&fp);
-  proj.release(&fp);
-  check.release(&fp);
-  return st;
+  return set_partition_impl(fine, coarse->k, coarse->k, nullptr, hl, hp, nullptr, proj.p());
 }
 
 static lpgpu_status read_metrics(lpgpu_session* s, int64_t* km1, int64_t* cut);
@@ -796,7 +840,7 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
   DeviceGuard g(s->device);
   s->gc_valid = false;  // refinement moves without gain-cache maintenance
   const int R = cfg.rounds, S = cfg.subrounds;
-  int64_t* fp = &s->footprint;
+  Mem* fp = &s->mem;
   CK(s->stats.alloc(std::max(1, R) * kStats, fp));
   cudaStream_t st = s->st;
   int64_t km1_before = 0;
@@ -804,11 +848,10 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
   if (ms != LPGPU_OK) return ms;
   RoundCtx c = s->ctx(&cfg);
   const Launch L = s->launch();
-  DevBuf<int32_t> dnodes;
-  int64_t tmpfp = 0;
+  TmpBuf<int32_t> dnodes(s->mem);
   if (num_nodes > 0) {
-    CK(dnodes.alloc(num_nodes, &tmpfp));
-    CK(cudaMemcpyAsync(dnodes.p, nodes, sizeof(int32_t) * num_nodes, cudaMemcpyHostToDevice, st));
+    CK(dnodes.alloc(num_nodes));
+    CK(cudaMemcpyAsync(dnodes.p(), nodes, sizeof(int32_t) * num_nodes, cudaMemcpyHostToDevice, st));
   }
   PhaseTimer* tm = s->timing ? &s->timer : nullptr;
   // The whole refine is a fixed sequence of launches whose element counts live
@@ -822,7 +865,7 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
     if (s->batched && (e = cudaMemsetAsync(s->inst_delta.p, 0, sizeof(int64_t) * s->num_inst, st)) != cudaSuccess)
       return e;
     if (num_nodes > 0) {
-      if ((e = launch_mark_list(L, c, dnodes.p, num_nodes)) != cudaSuccess) return e;
+      if ((e = launch_mark_list(L, c, dnodes.p(), num_nodes)) != cudaSuccess) return e;
     } else {
       if (s->n > 0 && (e = cudaMemsetAsync(s->next_flag.p, 0, s->n, st)) != cudaSuccess) return e;
       if ((e = launch_mark_all(L, c, cfg.rebalancing)) != cudaSuccess) return e;
@@ -889,7 +932,6 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
   std::vector<int64_t> hs(std::max(1, R) * kStats);
   CK(cudaMemcpyAsync(hs.data(), s->stats.p, sizeof(int64_t) * hs.size(), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  dnodes.release(&tmpfp);
   if (tm) {
     std::map<int, lpgpu_phase_time> acc;
     for (auto& rec : tm->recs) {
@@ -992,14 +1034,12 @@ lpgpu_status lpgpu_session_instance_km1(lpgpu_session* s, int64_t* km1) {
   if (!s->batched) {
     return read_metrics(s, km1, nullptr);
   }
-  int64_t fp = 0;
-  DevBuf<int64_t> d;
-  CK(d.alloc(s->num_inst, &fp));
+  TmpBuf<int64_t> d(s->mem);
+  CK(d.alloc(s->num_inst));
   RoundCtx c = s->ctx();
-  CK(launch_instance_metrics(s->launch(), c, d.p));
-  CK(cudaMemcpyAsync(km1, d.p, sizeof(int64_t) * s->num_inst, cudaMemcpyDeviceToHost, s->st));
+  CK(launch_instance_metrics(s->launch(), c, d.p()));
+  CK(cudaMemcpyAsync(km1, d.p(), sizeof(int64_t) * s->num_inst, cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
-  d.release(&fp);
   return LPGPU_OK;
 }
 
@@ -1067,23 +1107,19 @@ lpgpu_status lpgpu_session_best_moves(lpgpu_session* s, int32_t* to, int32_t* ga
     return LPGPU_ERR_STATE;
   }
   DeviceGuard g(s->device);
-  int64_t fp = 0;
-  DevBuf<int32_t> dto, dgain;
-  DevBuf<uint8_t> dborder;
-  CK(dto.alloc(s->n, &fp));
-  CK(dgain.alloc(s->n, &fp));
-  CK(dborder.alloc(s->n, &fp));
+  TmpBuf<int32_t> dto(s->mem), dgain(s->mem);
+  TmpBuf<uint8_t> dborder(s->mem);
+  CK(dto.alloc(s->n));
+  CK(dgain.alloc(s->n));
+  CK(dborder.alloc(s->n));
   RoundCtx c = s->ctx();
-  CK(launch_best_moves(s->launch(), c, dto.p, dgain.p, dborder.p));
+  CK(launch_best_moves(s->launch(), c, dto.p(), dgain.p(), dborder.p()));
   if (s->n > 0) {
-    if (to) CK(cudaMemcpyAsync(to, dto.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
-    if (gain) CK(cudaMemcpyAsync(gain, dgain.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
-    if (border) CK(cudaMemcpyAsync(border, dborder.p, s->n, cudaMemcpyDeviceToHost, s->st));
+    if (to) CK(cudaMemcpyAsync(to, dto.p(), sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
+    if (gain) CK(cudaMemcpyAsync(gain, dgain.p(), sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
+    if (border) CK(cudaMemcpyAsync(border, dborder.p(), s->n, cudaMemcpyDeviceToHost, s->st));
   }
   CK(cudaStreamSynchronize(s->st));
-  dto.release(&fp);
-  dgain.release(&fp);
-  dborder.release(&fp);
   return LPGPU_OK;
 }
 
@@ -1095,24 +1131,21 @@ lpgpu_status lpgpu_session_gain_cache(lpgpu_session* s, int32_t* benefit, int32_
     return LPGPU_ERR_STATE;
   }
   DeviceGuard g(s->device);
-  int64_t fp = 0;
-  DevBuf<int32_t> db, dp;
+  TmpBuf<int32_t> db(s->mem), dp(s->mem);
   const int32_t *sb = s->gc_benefit.p, *sp = s->gc_penalty.p;
   if (!s->gc_valid) {  // computed for this call
-    CK(db.alloc(s->n, &fp));
-    CK(dp.alloc((size_t)s->n * s->k, &fp));
+    CK(db.alloc(s->n));
+    CK(dp.alloc((size_t)s->n * s->k));
     RoundCtx c = s->ctx();
-    CK(launch_gain_cache(s->launch(), c, db.p, dp.p));
-    sb = db.p;
-    sp = dp.p;
+    CK(launch_gain_cache(s->launch(), c, db.p(), dp.p()));
+    sb = db.p();
+    sp = dp.p();
   }
   if (s->n > 0) {
     if (benefit) CK(cudaMemcpyAsync(benefit, sb, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost, s->st));
     if (penalty) CK(cudaMemcpyAsync(penalty, sp, sizeof(int32_t) * s->n * s->k, cudaMemcpyDeviceToHost, s->st));
   }
   CK(cudaStreamSynchronize(s->st));
-  db.release(&fp);
-  dp.release(&fp);
   return LPGPU_OK;
 }
 
@@ -1124,7 +1157,7 @@ lpgpu_status lpgpu_session_init_gain_cache(lpgpu_session* s) {
     return LPGPU_ERR_STATE;
   }
   DeviceGuard g(s->device);
-  int64_t* fp = &s->footprint;
+  Mem* fp = &s->mem;
   CK(s->gc_benefit.alloc(s->n, fp));
   CK(s->gc_penalty.alloc((size_t)s->n * s->k, fp));
   CK(s->gc_moved.alloc(s->n, fp));
@@ -1168,33 +1201,29 @@ lpgpu_status lpgpu_session_apply_moves(lpgpu_session* s, int64_t count, const in
     if (seen[vs[i]]) return invalid("vertex moved twice in one batch");
     seen[vs[i]] = 1;
   }
-  int64_t fp = 0;
-  DevBuf<int32_t> dv, df, dt;
-  CK(dv.alloc(count, &fp));
-  CK(df.alloc(count, &fp));
-  CK(dt.alloc(count, &fp));
+  TmpBuf<int32_t> dv(s->mem), df(s->mem), dt(s->mem);
+  CK(dv.alloc(count));
+  CK(df.alloc(count));
+  CK(dt.alloc(count));
   if (count > 0) {
-    CK(cudaMemcpyAsync(dv.p, vs, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s->st));
-    CK(cudaMemcpyAsync(df.p, fs, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s->st));
-    CK(cudaMemcpyAsync(dt.p, ts, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(dv.p(), vs, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(df.p(), fs, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(dt.p(), ts, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s->st));
   }
   RoundCtx c = s->ctx();
   GainCache gc{nullptr, nullptr, nullptr};
   if (s->gc_valid) gc = GainCache{s->gc_benefit.p, s->gc_penalty.p, s->gc_moved.p};
-  CK(launch_apply_moves(s->launch(), c, count, dv.p, df.p, dt.p, gc));
+  CK(launch_apply_moves(s->launch(), c, count, dv.p(), df.p(), dt.p(), gc));
   int64_t d = 0;
   CK(cudaMemcpyAsync(&d, s->scal.p + kApplyDelta, sizeof(int64_t), cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
-  dv.release(&fp);
-  df.release(&fp);
-  dt.release(&fp);
   if (delta) *delta = d;
   return LPGPU_OK;
 }
 
 lpgpu_status lpgpu_session_footprint(lpgpu_session* s, int64_t* bytes) {
   if (!s || !bytes) return invalid("null pointer");
-  *bytes = s->footprint;
+  *bytes = s->mem.bytes;
   return LPGPU_OK;
 }
 
@@ -1216,7 +1245,7 @@ lpgpu_status lpgpu_session_save_partition(lpgpu_session* s) {
   lpgpu_status ps = need_part(s);
   if (ps != LPGPU_OK) return ps;
   DeviceGuard g(s->device);
-  CK(s->saved_part.alloc(s->n, &s->footprint));
+  CK(s->saved_part.alloc(s->n, &s->mem));
   if (s->n > 0)
     CK(cudaMemcpyAsync(s->saved_part.p, s->part.p, sizeof(int32_t) * s->n, cudaMemcpyDeviceToDevice, s->st));
   CK(cudaStreamSynchronize(s->st));
@@ -1251,12 +1280,11 @@ lpgpu_status lpgpu_session_rebalance(lpgpu_session* s, int32_t max_rounds, lpgpu
   s->gc_valid = false;
   const int R = max_rounds, k = s->k;
   cudaStream_t st = s->st;
-  int64_t* fp = &s->footprint;
+  Mem* fp = &s->mem;
   CK(s->stats.alloc(std::max(1, R) * kStats, fp));
   CK(cudaMemsetAsync(s->stats.p, 0, sizeof(int64_t) * std::max(1, R) * kStats, st));
-  int64_t tmpfp = 0;
-  DevBuf<int64_t> rb;
-  CK(rb.alloc(5 * (size_t)k + 1, &tmpfp));
+  TmpBuf<int64_t> rb(s->mem);
+  CK(rb.alloc(5 * (size_t)k + 1));
   int64_t km1_before = 0;
   ps = read_metrics(s, &km1_before, nullptr);
   if (ps != LPGPU_OK) return ps;
@@ -1277,7 +1305,7 @@ lpgpu_status lpgpu_session_rebalance(lpgpu_session* s, int32_t max_rounds, lpgpu
     // one sub-round over all vertices (rec and status per vertex id)
     CK(cudaMemcpyAsync(s->sub_off.p, sub, sizeof(sub), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(s->blk64.p, 0, sizeof(int64_t) * 3 * k, st));  // in_w, in_cnt, cand_out
-    CK(launch_rebalance_round(s->launch(), c, r, s->heavy.p, s->revl.p, rb.p));
+    CK(launch_rebalance_round(s->launch(), c, r, s->heavy.p, s->revl.p, rb.p()));
     CK(cudaMemcpyAsync(hs.data(), s->stats.p + (int64_t)r * kStats, sizeof(int64_t) * kStats,
                        cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -1288,7 +1316,6 @@ lpgpu_status lpgpu_session_rebalance(lpgpu_session* s, int32_t max_rounds, lpgpu
     pins += rs.pins;
     if (rs.moved == 0) break;
   }
-  rb.release(&tmpfp);
   if (result) {
     int64_t km1_after = 0;
     ps = read_metrics(s, &km1_after, nullptr);
