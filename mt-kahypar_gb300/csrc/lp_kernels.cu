@@ -161,100 +161,6 @@ cudaError_t scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t count, i
   return cudaGetLastError();
 }
 
-// ============================================================ incidence
-
-__global__ void k_count_pins(const int32_t* __restrict__ pins, int64_t P, int64_t* __restrict__ cnt) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P;
-       i += (int64_t)gridDim.x * blockDim.x)
-    atomicAdd(reinterpret_cast<ull*>(&cnt[pins[i]]), 1ull);
-}
-
-// Incidences per log2 degree bucket (bucket j: degree in [2^j, 2^(j+1))),
-// from the per-vertex counts before the scan; sizes the sweep's heavy share.
-__global__ void k_degree_hist(int64_t n, const int64_t* __restrict__ cnt, int64_t* __restrict__ hist) {
-  __shared__ ull s_h[kDegBuckets];
-  if (threadIdx.x < kDegBuckets) s_h[threadIdx.x] = 0;
-  __syncthreads();
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t d = cnt[v];
-    if (d > 0) atomicAdd(&s_h[min(63 - __clzll(d), kDegBuckets - 1)], (ull)d);
-  }
-  __syncthreads();
-  if (threadIdx.x < kDegBuckets && s_h[threadIdx.x])
-    atomicAdd(reinterpret_cast<ull*>(&hist[threadIdx.x]), s_h[threadIdx.x]);
-}
-
-// Warp per net: every pin appends the net id to its vertex's incident-net list.
-__global__ void k_scatter_incidence(int64_t m, const int64_t* __restrict__ net_off,
-                                    const int32_t* __restrict__ pins, int64_t* __restrict__ cursor,
-                                    int32_t* __restrict__ inets) {
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < m; e += warps) {
-    const int64_t b = net_off[e], en = net_off[e + 1];
-    for (int64_t i = b + lane_id(); i < en; i += 32) {
-      const int64_t pos = (int64_t)atomicAdd(reinterpret_cast<ull*>(&cursor[pins[i]]), 1ull);
-      inets[pos] = (int32_t)e;
-    }
-  }
-}
-
-cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const int64_t* net_off,
-                                   const int32_t* pins, int64_t* vtx_off, int32_t* inets,
-                                   int64_t* cursor, int64_t* scan_tmp, int64_t scan_tmp_elems,
-                                   int64_t* deg_hist) {
-  int64_t P = 0;
-  cudaError_t e = cudaMemcpyAsync(&P, net_off + m, sizeof(int64_t), cudaMemcpyDeviceToHost, L.st);
-  if (e != cudaSuccess) return e;
-  if ((e = cudaStreamSynchronize(L.st)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(vtx_off, 0, sizeof(int64_t) * (n + 1), L.st)) != cudaSuccess) return e;
-  if (P > 0) {
-    k_count_pins<<<grid_for(L, P, 256, 8), 256, 0, L.st>>>(pins, P, vtx_off);
-    LAUNCHED("k_count_pins");
-  }
-  if (deg_hist) {
-    if ((e = cudaMemsetAsync(deg_hist, 0, sizeof(int64_t) * kDegBuckets, L.st)) != cudaSuccess) return e;
-    if (n > 0) {
-      k_degree_hist<<<grid_for(L, n, 256, 4), 256, 0, L.st>>>(n, vtx_off, deg_hist);
-      LAUNCHED("k_degree_hist");
-    }
-  }
-  if ((e = scan_exclusive_i64(vtx_off, vtx_off, n + 1, scan_tmp, scan_tmp_elems, L.st)) != cudaSuccess)
-    return e;
-  if ((e = cudaMemcpyAsync(cursor, vtx_off, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, L.st)) !=
-      cudaSuccess)
-    return e;
-  if (m > 0) {
-    k_scatter_incidence<<<grid_for(L, m * 32, 256, 8), 256, 0, L.st>>>(m, net_off, pins, cursor, inets);
-    LAUNCHED("k_scatter_incidence");
-  }
-  return cudaGetLastError();
-}
-
-// ======================================================== partition init
-
-// c(V_b) = sum of w(v) over v in block b (initializeBlockWeights, h:1067-1084).
-// Batched sessions have too many blocks for shared memory: global atomics.
-__global__ void k_block_weights(RoundCtx c) {
-  extern __shared__ ull s_w[];
-  const bool priv = !c.batched;
-  if (priv) {
-    for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_w[b] = 0;
-    __syncthreads();
-  }
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < c.n;
-       v += (int64_t)gridDim.x * blockDim.x) {
-    if (priv)
-      atomicAdd(&s_w[c.part[v]], (ull)(int64_t)c.w_v[v]);
-    else
-      atomicAdd(reinterpret_cast<ull*>(&c.bw[c.part[v]]), (ull)(int64_t)c.w_v[v]);
-  }
-  if (priv) {
-    __syncthreads();
-    for (int b = threadIdx.x; b < c.k; b += blockDim.x)
-      if (s_w[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_w[b]);
-  }
-}
-
 // Incidence packing shared by the kernels that walk the incidences of a set
 // of vertices (one per lane). Vertices of degree 1..32 are packed greedily
 // into groups of <= 32 incidences (lane = incidence, contiguous per vertex);
@@ -322,6 +228,113 @@ __device__ __forceinline__ int packed_incidences(bool sel, int64_t o0, int deg,
   }
   return my_total;
 }
+
+// ============================================================ incidence
+
+__global__ void k_count_pins(const int32_t* __restrict__ pins, int64_t P, int64_t* __restrict__ cnt) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P;
+       i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(reinterpret_cast<ull*>(&cnt[pins[i]]), 1ull);
+}
+
+// Incidences per log2 degree bucket (bucket j: degree in [2^j, 2^(j+1))),
+// from the per-vertex counts before the scan; sizes the sweep's heavy share.
+__global__ void k_degree_hist(int64_t n, const int64_t* __restrict__ cnt, int64_t* __restrict__ hist) {
+  __shared__ ull s_h[kDegBuckets];
+  if (threadIdx.x < kDegBuckets) s_h[threadIdx.x] = 0;
+  __syncthreads();
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t d = cnt[v];
+    if (d > 0) atomicAdd(&s_h[min(63 - __clzll(d), kDegBuckets - 1)], (ull)d);
+  }
+  __syncthreads();
+  if (threadIdx.x < kDegBuckets && s_h[threadIdx.x])
+    atomicAdd(reinterpret_cast<ull*>(&hist[threadIdx.x]), s_h[threadIdx.x]);
+}
+
+// Every pin appends its net id to its vertex's incident-net list. A warp
+// takes 32 nets and walks their pins in packed 32-pin groups (nets of more
+// than 32 pins alone, 32 pins at a time), so small nets keep every lane busy.
+__global__ void __launch_bounds__(256) k_scatter_incidence(int64_t m, const int64_t* __restrict__ net_off,
+                                                           const int32_t* __restrict__ pins,
+                                                           int64_t* __restrict__ cursor,
+                                                           int32_t* __restrict__ inets) {
+  __shared__ unsigned char s_own[256];
+  const int lane = lane_id();
+  unsigned char* own = s_own + (threadIdx.x & ~31);
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < m;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = base + lane;
+    const bool sel = e < m;
+    const int64_t o0 = sel ? net_off[e] : 0;
+    const int deg = sel ? (int)(net_off[e + 1] - o0) : 0;
+    packed_incidences(sel, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
+      if (has) {
+        const int64_t pos = (int64_t)atomicAdd(reinterpret_cast<ull*>(&cursor[pins[j]]), 1ull);
+        inets[pos] = (int32_t)(base + ow);
+      }
+      return 0;
+    });
+  }
+}
+
+cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const int64_t* net_off,
+                                   const int32_t* pins, int64_t* vtx_off, int32_t* inets,
+                                   int64_t* cursor, int64_t* scan_tmp, int64_t scan_tmp_elems,
+                                   int64_t* deg_hist) {
+  int64_t P = 0;
+  cudaError_t e = cudaMemcpyAsync(&P, net_off + m, sizeof(int64_t), cudaMemcpyDeviceToHost, L.st);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(L.st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(vtx_off, 0, sizeof(int64_t) * (n + 1), L.st)) != cudaSuccess) return e;
+  if (P > 0) {
+    k_count_pins<<<grid_for(L, P, 256, 8), 256, 0, L.st>>>(pins, P, vtx_off);
+    LAUNCHED("k_count_pins");
+  }
+  if (deg_hist) {
+    if ((e = cudaMemsetAsync(deg_hist, 0, sizeof(int64_t) * kDegBuckets, L.st)) != cudaSuccess) return e;
+    if (n > 0) {
+      k_degree_hist<<<grid_for(L, n, 256, 4), 256, 0, L.st>>>(n, vtx_off, deg_hist);
+      LAUNCHED("k_degree_hist");
+    }
+  }
+  if ((e = scan_exclusive_i64(vtx_off, vtx_off, n + 1, scan_tmp, scan_tmp_elems, L.st)) != cudaSuccess)
+    return e;
+  if ((e = cudaMemcpyAsync(cursor, vtx_off, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, L.st)) !=
+      cudaSuccess)
+    return e;
+  if (m > 0) {
+    k_scatter_incidence<<<grid_for(L, m, 256, 8), 256, 0, L.st>>>(m, net_off, pins, cursor, inets);
+    LAUNCHED("k_scatter_incidence");
+  }
+  return cudaGetLastError();
+}
+
+// ======================================================== partition init
+
+// c(V_b) = sum of w(v) over v in block b (initializeBlockWeights, h:1067-1084).
+// Batched sessions have too many blocks for shared memory: global atomics.
+__global__ void k_block_weights(RoundCtx c) {
+  extern __shared__ ull s_w[];
+  const bool priv = !c.batched;
+  if (priv) {
+    for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_w[b] = 0;
+    __syncthreads();
+  }
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < c.n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    if (priv)
+      atomicAdd(&s_w[c.part[v]], (ull)(int64_t)c.w_v[v]);
+    else
+      atomicAdd(reinterpret_cast<ull*>(&c.bw[c.part[v]]), (ull)(int64_t)c.w_v[v]);
+  }
+  if (priv) {
+    __syncthreads();
+    for (int b = threadIdx.x; b < c.k; b += blockDim.x)
+      if (s_w[b]) atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), s_w[b]);
+  }
+}
+
 
 // Φ, Λ and Λ1 (blocks holding exactly one pin of the net) from scratch
 // (initializePinCountInPart, h:1086-1110), fused with the km1 / cut sums, on
