@@ -321,12 +321,25 @@ __global__ void k_block_weights(RoundCtx c) {
     for (int b = threadIdx.x; b < c.k; b += blockDim.x) s_w[b] = 0;
     __syncthreads();
   }
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < c.n;
-       v += (int64_t)gridDim.x * blockDim.x) {
-    if (priv)
-      atomicAdd(&s_w[c.part[v]], (ull)(int64_t)c.w_v[v]);
-    else
-      atomicAdd(reinterpret_cast<ull*>(&c.bw[c.part[v]]), (ull)(int64_t)c.w_v[v]);
+  // lanes of a warp whose vertices share a block (contiguous partitions) add once
+  const int lane = lane_id();
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < c.n;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t v = base + lane;
+    const bool has = v < c.n;
+    const int b = has ? c.part[v] : -1;
+    const unsigned wv = has ? (unsigned)c.w_v[v] : 0u;  // vertex weights are >= 0
+    const unsigned peers = __match_any_sync(FULLMASK, b);
+    // sum over the lanes of the same block, in 16-bit halves (no 32-bit overflow)
+    const unsigned lo = __reduce_add_sync(peers, wv & 0xFFFFu);
+    const unsigned hi = __reduce_add_sync(peers, wv >> 16);
+    const ull w = (ull)lo + ((ull)hi << 16);
+    if (has && __ffs(peers) - 1 == lane) {
+      if (priv)
+        atomicAdd(&s_w[b], w);
+      else
+        atomicAdd(reinterpret_cast<ull*>(&c.bw[b]), w);
+    }
   }
   if (priv) {
     __syncthreads();
