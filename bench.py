@@ -485,12 +485,14 @@ def served_arm(args):
     insts = gen.generate_many("served_request", args.seed, args.instances or 256)  # before any CUDA call
     lpgpu.build()
     arr = serve.poisson_arrivals(len(insts), args.rate, args.seed)
+    # requests arrive in page-locked host buffers (both arms read the same ones)
+    hgs, parts, _, arenas = pinned_instances(lpgpu, gen, insts)
 
     def requests():
-        return [serve.Request(i, x.hg, x.k, x.eps, x.part, x.rounds, float(arr[i])) for i, x in enumerate(insts)]
+        return [serve.Request(i, hgs[i], x.k, x.eps, parts[i], x.rounds, float(arr[i])) for i, x in enumerate(insts)]
 
     # warm-up: one small batch through a server and one plain call
-    warm = [serve.Request(0, insts[0].hg, insts[0].k, insts[0].eps, insts[0].part, insts[0].rounds, 0.0)]
+    warm = [serve.Request(0, hgs[0], insts[0].k, insts[0].eps, parts[0], insts[0].rounds, 0.0)]
     serve.replay(serve.RefineServer(slots=args.slots), warm)
     serve.plain_loop(warm)
     rs = requests()
@@ -506,7 +508,7 @@ def served_arm(args):
             "config": {"workload": f"{len(insts)} requests at {args.rate:.0f} req/s, "
                                    f"{sum(x.hg.num_pins for x in insts)} pins in total, 8 rounds each",
                        "slots": args.slots, "budget_gb": 150, "subrounds": args.subrounds,
-                       "batch_pins": cap},
+                       "batch_pins": cap, "inputs": "page-locked host buffers"},
             "server": ss, "plain_loop": sp, "identical_results": same}
     print(json.dumps(line), flush=True)
     return 0 if same else 1

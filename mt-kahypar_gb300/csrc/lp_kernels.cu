@@ -243,9 +243,17 @@ __global__ void k_degree_hist(int64_t n, const int64_t* __restrict__ cnt, int64_
   __shared__ ull s_h[kDegBuckets];
   if (threadIdx.x < kDegBuckets) s_h[threadIdx.x] = 0;
   __syncthreads();
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t d = cnt[v];
-    if (d > 0) atomicAdd(&s_h[min(63 - __clzll(d), kDegBuckets - 1)], (ull)d);
+  // most vertices share a few buckets: lanes of one bucket add once
+  const int lane = lane_id();
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < n;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t v = base + lane;
+    const int64_t d = v < n ? cnt[v] : 0;  // 16-bit halves: exact below 2^43 incidences per vertex
+    const int j = d > 0 ? min(63 - __clzll(d), kDegBuckets - 1) : -1;
+    const unsigned peers = __match_any_sync(FULLMASK, j);
+    const unsigned lo = __reduce_add_sync(peers, (unsigned)d & 0xFFFFu);
+    const unsigned hi = __reduce_add_sync(peers, (unsigned)(d >> 16));
+    if (j >= 0 && __ffs(peers) - 1 == lane) atomicAdd(&s_h[j], (ull)lo + ((ull)hi << 16));
   }
   __syncthreads();
   if (threadIdx.x < kDegBuckets && s_h[threadIdx.x])
