@@ -85,7 +85,7 @@ using ull = unsigned long long;
 // Result words of the device-side input checks (validate.cu): the first
 // failure code, the largest net weight, whether some net weight is not 1,
 // then I per-instance sums of |e|·w(e) and I per-instance vertex weights.
-enum ValidateWord : int { kVErr = 0, kVMaxWe = 1, kVNonUnit = 2, kVSums = 4 };
+enum ValidateWord : int { kVErr = 0, kVMaxWe = 1, kVNonUnit = 2, kVMaxSize = 3, kVSums = 4 };
 enum ValidateCode : int {
   kVOk = 0,
   kVBadOffsets = 1,
@@ -109,7 +109,7 @@ struct RoundCtx {
   const int32_t* w_v;
   const int32_t* w_e;
   int32_t* part;
-  int32_t* phi;
+  int32_t* phi;          // Φ(e, b) at e * kmax + b: 16-bit entries when phi16, else 32-bit (phi_get / phi_add)
   uint32_t* conn;        // m x 2W words: Λ(e) (W words), then Λ1(e) (W words)
   int64_t* bw;
   const int64_t* lmax;
@@ -141,6 +141,7 @@ struct RoundCtx {
   // parameters
   int32_t zero_gain, revert, rollback;
   int32_t unit_nets;     // every net weight is 1
+  int32_t phi16;         // every net has fewer than 2^16 pins: Φ entries are 16 bits
   int32_t max_we;        // largest net weight (0 without nets)
   int64_t act_threshold;
   int32_t heavy_share;   // per mille of the sweep's work in heavy vertices (0: none can exist)
@@ -159,6 +160,29 @@ struct RoundCtx {
   int32_t* heavy;           // list positions deferred by the sweep (count in scal[kHeavyCount])
   int32_t* revl;            // list positions of moves marked for revert (count in scal[kRevCount])
 };
+
+// Φ(e, b) at index i = e * kmax + b. With 16-bit entries two share a 32-bit
+// word; an atomic add of d << 16 * (i & 1) changes one entry only, since an
+// entry never leaves [0, 2^16): the counts stay at most |e| < 2^16 and only
+// counts of at least 1 are decremented.
+__device__ __forceinline__ int phi_get(const RoundCtx& c, int64_t i) {
+  return c.phi16 ? (int)reinterpret_cast<const uint16_t*>(c.phi)[i] : c.phi[i];
+}
+__device__ __forceinline__ void phi_set(const RoundCtx& c, int64_t i, int v) {
+  if (c.phi16)
+    reinterpret_cast<uint16_t*>(c.phi)[i] = (uint16_t)v;
+  else
+    c.phi[i] = v;
+}
+// Adds d (+1 or -1) to Φ at i and returns the count before.
+__device__ __forceinline__ int phi_add(const RoundCtx& c, int64_t i, int d) {
+  if (c.phi16) {
+    const int sh = (int)(i & 1) * 16;
+    const uint32_t old = atomicAdd(reinterpret_cast<uint32_t*>(c.phi) + (i >> 1), (uint32_t)d << sh);
+    return (int)((old >> sh) & 0xFFFFu);
+  }
+  return atomicAdd(&c.phi[i], d);
+}
 
 // Global block offset of vertex v's instance.
 __device__ __forceinline__ int block_offset(const RoundCtx& c, int64_t v) {

@@ -400,7 +400,7 @@ __global__ void __launch_bounds__(256) k_pin_counts(RoundCtx c) {
       const bool leader = has && __ffs(peers) - 1 == lane;
       if (leader) {
         const int cnt = __popc(peers);
-        c.phi[e_ow * k + b] = cnt;
+        phi_set(c, e_ow * k + b, cnt);
         uint32_t* rec = c.conn + e_ow * 2 * W;
         atomicOr(&rec[b >> 5], 1u << (b & 31));
         if (cnt == 1) atomicOr(&rec[W + (b >> 5)], 1u << (b & 31));
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(256) k_pin_counts(RoundCtx c) {
         if (b < k) {
           cnt = hist[b];
           hist[b] = 0;
-          if (cnt) c.phi[eq * k + b] = cnt;
+          if (cnt) phi_set(c, eq * k + b, cnt);
         }
         const unsigned bits = __ballot_sync(FULLMASK, cnt > 0);
         const unsigned ones = __ballot_sync(FULLMASK, cnt == 1);
@@ -464,7 +464,9 @@ cudaError_t launch_init_partition(const Launch& L, const RoundCtx& c) {
     LAUNCHED("k_block_weights");
   }
   if (c.m > 0) {
-    if ((e = cudaMemsetAsync(c.phi, 0, sizeof(int32_t) * (size_t)c.m * c.kmax, L.st)) != cudaSuccess) return e;
+    const size_t entries = (size_t)c.m * c.kmax;
+    const size_t phi_bytes = c.phi16 ? sizeof(uint32_t) * ((entries + 1) / 2) : sizeof(int32_t) * entries;
+    if ((e = cudaMemsetAsync(c.phi, 0, phi_bytes, L.st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(c.conn, 0, sizeof(uint32_t) * (size_t)c.m * 2 * c.W, L.st)) != cudaSuccess) return e;
     const size_t smem = sizeof(int) * c.kmax * 8;
     k_pin_counts<<<grid_for(L, c.m, 256, occupancy((const void*)k_pin_counts, 256, smem)), 256, smem, L.st>>>(c);
@@ -1405,7 +1407,7 @@ __global__ void __launch_bounds__(256) k_gain_cache(RoundCtx c, int32_t* benefit
     for (int64_t j = c.vtx_off[v] + lane; j < c.vtx_off[v + 1]; j += 32) {
       const int e = c.inets[j];
       const int we = c.w_e[e];
-      if (c.phi[(int64_t)e * c.k + pv] == 1) ben += we;
+      if (phi_get(c, (int64_t)e * c.k + pv) == 1) ben += we;
       inc += we;
       for (int w = 0; w < c.W; ++w) {
         uint32_t bits = c.conn[(int64_t)e * 2 * c.W + w];
@@ -1474,13 +1476,13 @@ __device__ __forceinline__ int64_t warp_commit_vertex(const RoundCtx& c, int64_t
     const int64_t e = c.inets[j];
     const int we = c.w_e[e];
     uint32_t* rec = c.conn + e * 2 * W;
-    const int of = atomicSub(&c.phi[e * k + f], 1);
+    const int of = phi_add(c, e * k + f, -1);
     if (of == 1) {
       atomicXor(&rec[f >> 5], fbit);
       att -= we;
     }
     if (of == 1 || of == 2) atomicXor(&rec[W + (f >> 5)], fbit);
-    const int ot = atomicAdd(&c.phi[e * k + t], 1);
+    const int ot = phi_add(c, e * k + t, 1);
     if (ot == 0) {
       atomicXor(&rec[t >> 5], tbit);
       att += we;
@@ -1530,7 +1532,7 @@ __global__ void k_gc_moved_benefit(RoundCtx c, int64_t count, const int32_t* __r
     int ben = 0;
     for (int64_t j = c.vtx_off[v] + lane_id(); j < c.vtx_off[v + 1]; j += 32) {
       const int64_t e = c.inets[j];
-      if (c.phi[e * c.kmax + pv] == 1) ben += c.w_e[e];
+      if (phi_get(c, e * c.kmax + pv) == 1) ben += c.w_e[e];
     }
     ben = warp_sum(ben);
     if (lane_id() == 0) benefit[v] = ben;
@@ -2333,12 +2335,12 @@ __device__ __forceinline__ void commit_pair(const RoundCtx& c, bool h0, int64_t 
   const int64_t k = c.kmax;
   int of0 = 0, ot0 = 0, of1 = 0, ot1 = 0;
   if (h0) {
-    of0 = atomicSub(&c.phi[e0 * k + f0], 1);
-    ot0 = atomicAdd(&c.phi[e0 * k + t0], 1);
+    of0 = phi_add(c, e0 * k + f0, -1);
+    ot0 = phi_add(c, e0 * k + t0, 1);
   }
   if (h1) {
-    of1 = atomicSub(&c.phi[e1 * k + f1], 1);
-    ot1 = atomicAdd(&c.phi[e1 * k + t1], 1);
+    of1 = phi_add(c, e1 * k + f1, -1);
+    ot1 = phi_add(c, e1 * k + t1, 1);
   }
   a0 = a1 = 0;
   if (h0) {

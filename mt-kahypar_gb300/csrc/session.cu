@@ -109,6 +109,7 @@ struct lpgpu_session_s {
   int64_t deg_inc[kDegBuckets] = {};  // incidences per log2 degree bucket
   bool unit_nets = true;
   int32_t max_we = 0;
+  int64_t max_net_size = 0;
   DevBuf<int64_t> net_off, vtx_off;
   DevBuf<int32_t> pins, inets, w_v, w_e;
   // partition
@@ -176,6 +177,13 @@ struct lpgpu_session_s {
     return x < 1 ? 1 : x;
   }
 
+  // Φ entries fit 16 bits when every net has fewer than 2^16 pins.
+  bool phi16() const { return max_net_size < 65536; }
+  size_t phi_words() const {
+    const size_t entries = (size_t)m * kmax;
+    return phi16() ? (entries + 1) / 2 : entries;
+  }
+
   RoundCtx ctx(const lpgpu_config* cfg = nullptr) {
     RoundCtx c{};
     c.n = n;
@@ -189,6 +197,7 @@ struct lpgpu_session_s {
     c.w_v = w_v.p;
     c.w_e = w_e.p;
     c.unit_nets = unit_nets ? 1 : 0;
+    c.phi16 = phi16() ? 1 : 0;
     c.max_we = max_we;
     c.heavy_share = heavy_share();
     c.part = part.p;
@@ -563,6 +572,7 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
   }
   s->total_vw = total;
   s->max_we = (int32_t)h[kVMaxWe];
+  s->max_net_size = h[kVMaxSize];
   s->unit_nets = h[kVNonUnit] == 0;
   CK(launch_build_incidence(s->launch(), n, m, s->net_off.p, s->pins.p, s->vtx_off.p, s->inets.p,
                             reinterpret_cast<int64_t*>(s->seg_key.p), s->scan_tmp.p, s->scan_tmp_n,
@@ -635,7 +645,7 @@ static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax
   Mem* fp = &s->mem;
   // same-size buffers are kept from the previous partition
   CK(s->part.alloc(s->n, fp));
-  CK(s->phi.alloc((size_t)s->m * kmax, fp));
+  CK(s->phi.alloc(s->phi_words(), fp));
   CK(s->conn.alloc((size_t)s->m * 2 * s->W, fp));
   CK(s->bw.alloc(K, fp));
   CK(s->lmax.alloc(K, fp));
@@ -1066,8 +1076,15 @@ lpgpu_status lpgpu_session_get_pin_counts(lpgpu_session* s, int32_t* pc) {
   lpgpu_status ps = need_part(s);
   if (ps != LPGPU_OK) return ps;
   DeviceGuard g(s->device);
-  if (s->m > 0)
-    CK(cudaMemcpyAsync(pc, s->phi.p, sizeof(int32_t) * s->m * s->kmax, cudaMemcpyDeviceToHost, s->st));
+  const size_t entries = (size_t)s->m * s->kmax;
+  if (entries > 0 && !s->phi16()) {
+    CK(cudaMemcpyAsync(pc, s->phi.p, sizeof(int32_t) * entries, cudaMemcpyDeviceToHost, s->st));
+  } else if (entries > 0) {  // 16-bit entries: widened on the host
+    std::vector<uint16_t> h(entries);
+    CK(cudaMemcpyAsync(h.data(), s->phi.p, sizeof(uint16_t) * entries, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    for (size_t i = 0; i < entries; ++i) pc[i] = h[i];
+  }
   CK(cudaStreamSynchronize(s->st));
   return LPGPU_OK;
 }

@@ -30,7 +30,7 @@ __device__ __forceinline__ int find_instance(const int64_t* __restrict__ off, in
 
 // Warp per net: offsets inside [0, P] and non-decreasing, w(e) >= 0, every
 // pin inside its instance's vertex range; Σ |e|·w(e) per instance, the
-// largest net weight and whether some weight differs from 1.
+// largest net weight and size, and whether some weight differs from 1.
 __global__ void k_check_nets(int64_t m, int64_t P, const int64_t* __restrict__ net_off,
                              const int32_t* __restrict__ pins, const int32_t* __restrict__ w_e, int I,
                              const int64_t* __restrict__ inst_voff, const int64_t* __restrict__ inst_noff,
@@ -40,6 +40,7 @@ __global__ void k_check_nets(int64_t m, int64_t P, const int64_t* __restrict__ n
   int64_t gsum = 0;
   int cur = -1;  // instance whose sum is held in gsum
   int maxw = 0, nonunit = 0;
+  int64_t maxs = 0;
   for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < m; e += warps) {
     const int64_t a = net_off[e], b = net_off[e + 1];
     if (a < 0 || b < a || b > P) {
@@ -52,6 +53,7 @@ __global__ void k_check_nets(int64_t m, int64_t P, const int64_t* __restrict__ n
       continue;
     }
     maxw = max(maxw, we);
+    maxs = max(maxs, b - a);
     nonunit |= we != 1;
     int inst = 0;
     int64_t v0 = 0, v1 = n;
@@ -79,10 +81,12 @@ __global__ void k_check_nets(int64_t m, int64_t P, const int64_t* __restrict__ n
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     maxw = max(maxw, __shfl_xor_sync(FULL, maxw, o));
+    maxs = max(maxs, __shfl_xor_sync(FULL, maxs, o));
     nonunit |= __shfl_xor_sync(FULL, nonunit, o);
   }
   if (lane == 0) {
     if (maxw) atomicMax(reinterpret_cast<unsigned long long*>(&out[kVMaxWe]), (ull)maxw);
+    if (maxs) atomicMax(reinterpret_cast<unsigned long long*>(&out[kVMaxSize]), (ull)maxs);
     if (nonunit) atomicOr(reinterpret_cast<ull*>(&out[kVNonUnit]), 1ull);
   }
 }
@@ -90,7 +94,7 @@ __global__ void k_check_nets(int64_t m, int64_t P, const int64_t* __restrict__ n
 // One instance: thread per net (offsets, weights, Σ |e|·w(e)) ...
 __global__ void k_check_nets_flat(int64_t m, int64_t P, const int64_t* __restrict__ net_off,
                                   const int32_t* __restrict__ w_e, int64_t* out) {
-  int64_t gsum = 0;
+  int64_t gsum = 0, maxs = 0;
   int maxw = 0, nonunit = 0;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t a = net_off[e], b = net_off[e + 1];
@@ -104,6 +108,7 @@ __global__ void k_check_nets_flat(int64_t m, int64_t P, const int64_t* __restric
       continue;
     }
     maxw = max(maxw, we);
+    maxs = max(maxs, b - a);
     nonunit |= we != 1;
     gsum += (b - a) * (int64_t)we;
   }
@@ -111,11 +116,13 @@ __global__ void k_check_nets_flat(int64_t m, int64_t P, const int64_t* __restric
   for (int o = 16; o > 0; o >>= 1) {
     gsum += __shfl_xor_sync(FULL, gsum, o);
     maxw = max(maxw, __shfl_xor_sync(FULL, maxw, o));
+    maxs = max(maxs, __shfl_xor_sync(FULL, maxs, o));
     nonunit |= __shfl_xor_sync(FULL, nonunit, o);
   }
   if ((threadIdx.x & 31) == 0) {
     if (gsum) atomicAdd(reinterpret_cast<ull*>(&out[kVSums]), (ull)gsum);
     if (maxw) atomicMax(reinterpret_cast<unsigned long long*>(&out[kVMaxWe]), (ull)maxw);
+    if (maxs) atomicMax(reinterpret_cast<unsigned long long*>(&out[kVMaxSize]), (ull)maxs);
     if (nonunit) atomicOr(reinterpret_cast<ull*>(&out[kVNonUnit]), 1ull);
   }
 }

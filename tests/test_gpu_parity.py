@@ -242,6 +242,34 @@ def test_activation_of_large_nets(lp, orc, threshold, seed):
         out[0].close()
 
 
+@pytest.mark.parametrize("big", [65535, 65536])
+def test_pin_count_width_boundary(lp, orc, big):
+    """A net of 65,535 pins keeps 16-bit pin counts (two per 32-bit word, a count
+    can reach 65,535); one of 65,536 pins switches the session to 32-bit counts.
+    Most of the big net starts in block 0, so moves push its counts up to the
+    width's limit and down again."""
+    from lpgpu import gen
+    rng = np.random.default_rng([big, 3])
+    n, m_small, k = big + 64, 3000, 3
+    sizes = rng.integers(2, 7, size=m_small)
+    small = [rng.choice(n, size=s, replace=False) for s in sizes]
+    nets = [np.arange(big)] + small
+    off = np.zeros(len(nets) + 1, np.int64)
+    np.cumsum([len(x) for x in nets], out=off[1:])
+    pins = np.concatenate(nets).astype(np.int32)
+    hg = gen.Hypergraph(n, len(nets), off, pins, np.ones(n, np.int32), np.ones(len(nets), np.int32)).with_incidence()
+    part = np.where(rng.random(n) < 0.9, 0, rng.integers(1, k, size=n)).astype(np.int32)
+    inst = gen.Instance("bignet", hg, k, 0.03, part, 3)
+    inst.lmax = np.full(k, n, np.int64)  # room for every move, block 0 included
+    s = session(lp, hg, k, part, lmax=inst.lmax, perfect=inst.perfect)
+    check_state(orc, s, hg, k, part)
+    s.close()
+    for mode in (LP_MODES[1], LP_MODES[2]):
+        out = run_both(lp, orc, inst, 3, mode)
+        assert_same_run(*out, orc, inst)
+        out[0].close()
+
+
 def test_refinement_nodes_and_threshold(lp, orc):
     from lpgpu import gen
     inst = gen.random_small(5, n=500, m=600, k=4)
