@@ -2322,63 +2322,70 @@ __device__ __forceinline__ int flat_find(const FlatSmem& f, int n, int x) {
   return lo;
 }
 
-// Φ / Λ / Λ1 update of two incidences at once; the four Φ atomics are issued
-// before any result is used. Per incidence of a move from f to t: atomic
-// decrement of Φ(e, f) and increment of Φ(e, t); Λ toggles when Φ(e, f)
-// reaches 0 or Φ(e, t) leaves 0, Λ1 when either passes through 1. The
-// attributed delta (km1Delta, hypergraph_common.h:133-140) is -w(e) when
-// Φ(e, f) reaches 0 and +w(e) when Φ(e, t) reaches 1; a0 / a1 are each
-// incidence's part.
-__device__ __forceinline__ void commit_pair(const RoundCtx& c, bool h0, int64_t e0, int f0, int t0, bool h1,
-                                            int64_t e1, int f1, int t1, int& a0, int& a1) {
+// Commit of Q incidences (e[q], from f[q], to t[q]; h[q]: present): all 2Q Φ
+// atomics are issued before any result is used, then per incidence the
+// decrement of Φ(e, f) and increment of Φ(e, t) toggle Λ when Φ(e, f) reaches
+// 0 or Φ(e, t) leaves 0, and Λ1 when either passes through 1. The attributed
+// delta (km1Delta, hypergraph_common.h:133-140) is -w(e) when Φ(e, f) reaches
+// 0 and +w(e) when Φ(e, t) reaches 1; a[q] is each incidence's part.
+template <int Q>
+__device__ __forceinline__ void commit_group(const RoundCtx& c, const bool (&h)[Q], const int64_t (&e)[Q],
+                                             const int (&f)[Q], const int (&t)[Q], int (&a)[Q]) {
   const int W = c.W;
   const int64_t k = c.kmax;
-  int of0 = 0, ot0 = 0, of1 = 0, ot1 = 0;
-  if (h0) {
-    of0 = phi_add(c, e0 * k + f0, -1);
-    ot0 = phi_add(c, e0 * k + t0, 1);
+  int of[Q], ot[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    of[q] = ot[q] = 0;
+    if (h[q]) {
+      of[q] = phi_add(c, e[q] * k + f[q], -1);
+      ot[q] = phi_add(c, e[q] * k + t[q], 1);
+    }
   }
-  if (h1) {
-    of1 = phi_add(c, e1 * k + f1, -1);
-    ot1 = phi_add(c, e1 * k + t1, 1);
-  }
-  a0 = a1 = 0;
-  if (h0) {
-    const int we = c.unit_nets ? 1 : c.w_e[e0];
-    uint32_t* rec = c.conn + e0 * 2 * W;
-    if (of0 == 1) { atomicXor(&rec[f0 >> 5], 1u << (f0 & 31)); a0 -= we; }
-    if (of0 == 1 || of0 == 2) atomicXor(&rec[W + (f0 >> 5)], 1u << (f0 & 31));
-    if (ot0 == 0) { atomicXor(&rec[t0 >> 5], 1u << (t0 & 31)); a0 += we; }
-    if (ot0 == 0 || ot0 == 1) atomicXor(&rec[W + (t0 >> 5)], 1u << (t0 & 31));
-  }
-  if (h1) {
-    const int we = c.unit_nets ? 1 : c.w_e[e1];
-    uint32_t* rec = c.conn + e1 * 2 * W;
-    if (of1 == 1) { atomicXor(&rec[f1 >> 5], 1u << (f1 & 31)); a1 -= we; }
-    if (of1 == 1 || of1 == 2) atomicXor(&rec[W + (f1 >> 5)], 1u << (f1 & 31));
-    if (ot1 == 0) { atomicXor(&rec[t1 >> 5], 1u << (t1 & 31)); a1 += we; }
-    if (ot1 == 0 || ot1 == 1) atomicXor(&rec[W + (t1 >> 5)], 1u << (t1 & 31));
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    a[q] = 0;
+    if (!h[q]) continue;
+    const int we = c.unit_nets ? 1 : c.w_e[e[q]];
+    uint32_t* rec = c.conn + e[q] * 2 * W;
+    const uint32_t fb = 1u << (f[q] & 31), tb = 1u << (t[q] & 31);
+    if (of[q] == 1) { atomicXor(&rec[f[q] >> 5], fb); a[q] -= we; }
+    if (of[q] == 1 || of[q] == 2) atomicXor(&rec[W + (f[q] >> 5)], fb);
+    if (ot[q] == 0) { atomicXor(&rec[t[q] >> 5], tb); a[q] += we; }
+    if (ot[q] == 0 || ot[q] == 1) atomicXor(&rec[W + (t[q] >> 5)], tb);
   }
 }
+
+// Incidences a thread of the CTA-flat commit handles per step.
+#ifndef LPGPU_COMMIT_GROUP
+#define LPGPU_COMMIT_GROUP 2  // 4 and 8 measured slower on rownet
+#endif
 
 // Moves every incidence of the CTA's collected vertices from their `from` to
 // their `to` block (flat over the CTA). Returns this thread's summed delta;
 // per-vertex sums go to f.att when `per_item`.
 __device__ __forceinline__ int64_t flat_commit(const RoundCtx& c, FlatSmem& f, int n, int total, bool per_item) {
+  constexpr int Q = LPGPU_COMMIT_GROUP;
   int64_t att = 0;
-  for (int x0 = threadIdx.x; x0 < total; x0 += 2 * kFlatThreads) {
-    const int x1 = x0 + kFlatThreads;
-    const bool h1 = x1 < total;
-    const int i0 = flat_find(f, n, x0), i1 = h1 ? flat_find(f, n, x1) : i0;
-    const int64_t e0 = c.inets[f.o0[i0] + (x0 - f.pre[i0])];
-    const int64_t e1 = h1 ? c.inets[f.o0[i1] + (x1 - f.pre[i1])] : 0;
-    const int ft0 = f.ft[i0], ft1 = f.ft[i1];
-    int a0, a1;
-    commit_pair(c, true, e0, ft0 & 0xffff, ft0 >> 16, h1, e1, ft1 & 0xffff, ft1 >> 16, a0, a1);
-    att += a0 + a1;
-    if (per_item) {
-      if (a0) atomicAdd(&f.att[i0], a0);
-      if (a1) atomicAdd(&f.att[i1], a1);
+  for (int x0 = threadIdx.x; x0 < total; x0 += Q * kFlatThreads) {
+    bool h[Q];
+    int64_t e[Q];
+    int fr[Q], to[Q], it[Q], a[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int x = x0 + q * kFlatThreads;
+      h[q] = x < total;
+      it[q] = h[q] ? flat_find(f, n, x) : 0;
+      e[q] = h[q] ? c.inets[f.o0[it[q]] + (x - f.pre[it[q]])] : 0;
+      const int ft = h[q] ? f.ft[it[q]] : 0;
+      fr[q] = ft & 0xffff;
+      to[q] = ft >> 16;
+    }
+    commit_group<Q>(c, h, e, fr, to, a);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      att += a[q];
+      if (per_item && a[q]) atomicAdd(&f.att[it[q]], a[q]);
     }
   }
   return att;
