@@ -161,6 +161,10 @@ struct RoundCtx {
   int32_t* revl;            // list positions of moves marked for revert (count in scal[kRevCount])
 };
 
+#ifndef LPGPU_PHI16
+#define LPGPU_PHI16 1  // 0: 32-bit Φ entries always
+#endif
+
 // Φ(e, b) at index i = e * kmax + b. With 16-bit entries two share a 32-bit
 // word; an atomic add of d << 16 * (i & 1) changes one entry only, since an
 // entry never leaves [0, 2^16): the counts stay at most |e| < 2^16 and only

@@ -1988,8 +1988,14 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_moves(RoundCtx c, int sub) 
 // histogram (32-bit: vertex weights total at most INT32_MAX) and the whole CTA
 // folds them before one warp scans the bins. Returns the threshold to every
 // thread.
-constexpr int kSelThreads = 512;
-constexpr int kSelStage = 16384;  // keys (8 B) + weights (4 B) staged in shared memory
+#ifndef LPGPU_SEL_THREADS
+#define LPGPU_SEL_THREADS 1024
+#endif
+#ifndef LPGPU_SEL_STAGE
+#define LPGPU_SEL_STAGE 8192
+#endif
+constexpr int kSelThreads = LPGPU_SEL_THREADS;
+constexpr int kSelStage = LPGPU_SEL_STAGE;  // keys (8 B) + weights (4 B) staged in shared memory
 constexpr size_t kSelSmem = (size_t)kSelStage * 12;
 
 // One histogram pass: the weights of the keys matching `prefix` under `mask`,

@@ -178,7 +178,7 @@ struct lpgpu_session_s {
   }
 
   // Φ entries fit 16 bits when every net has fewer than 2^16 pins.
-  bool phi16() const { return max_net_size < 65536; }
+  bool phi16() const { return LPGPU_PHI16 && max_net_size < 65536; }
   size_t phi_words() const {
     const size_t entries = (size_t)m * kmax;
     return phi16() ? (entries + 1) / 2 : entries;
