@@ -2252,8 +2252,12 @@ __device__ __forceinline__ void activate_incidence(const RoundCtx& c, int64_t e,
 // takes incidences t, t + blockDim, ... and finds its vertex by binary search
 // in the scanned degrees. Hub vertices are split across the whole CTA, and the
 // gathers and atomics of different vertices are in flight together.
-constexpr int kFlatThreads = 256;
+#ifndef LPGPU_FLAT_THREADS
+#define LPGPU_FLAT_THREADS 512
+#endif
+constexpr int kFlatThreads = LPGPU_FLAT_THREADS;
 constexpr int kFlatItems = 1024;  // list positions (and so at most this many vertices) per CTA pass
+static_assert(kFlatItems % kFlatThreads == 0, "whole items per thread");
 
 struct FlatSmem {
   int64_t o0[kFlatItems];    // first incidence
