@@ -1899,8 +1899,14 @@ __device__ void plan_to(const RoundCtx& c) {
 // shared memory and reserves each block's range with one global atomic, so the
 // per-block cursors see one atomic per CTA instead of one per warp. Batches
 // (many blocks) use warp-aggregated atomics.
-constexpr int kBinThreads = 256;
-constexpr int kBinPer = 8;  // list positions per thread
+#ifndef LPGPU_BIN_THREADS
+#define LPGPU_BIN_THREADS 512
+#endif
+#ifndef LPGPU_BIN_PER
+#define LPGPU_BIN_PER 4
+#endif
+constexpr int kBinThreads = LPGPU_BIN_THREADS;
+constexpr int kBinPer = LPGPU_BIN_PER;  // list positions per thread
 constexpr int kBinSmemBlocks = 2048;
 
 __global__ void __launch_bounds__(kBinThreads) k_bin_moves(RoundCtx c, int sub) {
@@ -2741,8 +2747,13 @@ __global__ void __launch_bounds__(kFlatThreads) k_rollback(RoundCtx c, int round
 // pins of its incident nets with |e| <= activation threshold become active in
 // the next round (moveVertex, label_propagation_refiner.h:112-128). Nets are
 // stamped with the round's epoch and expanded by k_expand_nets.
-__global__ void __launch_bounds__(256) k_activate_round(RoundCtx c, int S) {
-  __shared__ unsigned char s_own[256];
+#ifndef LPGPU_ACT_THREADS
+#define LPGPU_ACT_THREADS 256
+#endif
+constexpr int kActThreads = LPGPU_ACT_THREADS;  // activation and expansion CTAs
+
+__global__ void __launch_bounds__(kActThreads) k_activate_round(RoundCtx c, int S) {
+  __shared__ unsigned char s_own[kActThreads];
   const int lane = lane_id();
   unsigned char* own = s_own + (threadIdx.x & ~31);
   const int epoch = (int)c.scal[kEpoch];
@@ -2770,8 +2781,8 @@ __global__ void __launch_bounds__(256) k_activate_round(RoundCtx c, int S) {
 // End of a round: the pins of every net stamped with the round's epoch
 // become active for the next round. A warp takes 32 nets and walks the pins
 // of the stamped ones in packed 32-pin groups.
-__global__ void __launch_bounds__(256) k_expand_nets(RoundCtx c) {
-  __shared__ unsigned char s_own[256];
+__global__ void __launch_bounds__(kActThreads) k_expand_nets(RoundCtx c) {
+  __shared__ unsigned char s_own[kActThreads];
   const int epoch = (int)c.scal[kEpoch];
   const int lane = lane_id();
   unsigned char* own = s_own + (threadIdx.x & ~31);
@@ -2795,13 +2806,14 @@ __global__ void __launch_bounds__(256) k_expand_nets(RoundCtx c) {
 cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, int S, PhaseTimer* timer) {
   {
     Scope sc(timer, "activate");
-    k_activate_round<<<grid_for(L, c.n, 256, occupancy((const void*)k_activate_round, 256, 0)), 256, 0,
-                       L.st>>>(c, S);
+    k_activate_round<<<grid_for(L, c.n, kActThreads, occupancy((const void*)k_activate_round, kActThreads, 0)),
+                       kActThreads, 0, L.st>>>(c, S);
     LAUNCHED("k_activate_round");
   }
   if (c.m == 0) return cudaSuccess;
   Scope sc(timer, "expand");
-  k_expand_nets<<<grid_for(L, c.m, 256, occupancy((const void*)k_expand_nets, 256, 0)), 256, 0, L.st>>>(c);
+  k_expand_nets<<<grid_for(L, c.m, kActThreads, occupancy((const void*)k_expand_nets, kActThreads, 0)),
+                  kActThreads, 0, L.st>>>(c);
   LAUNCHED("k_expand_nets");
   return cudaSuccess;
 }
