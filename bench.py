@@ -58,7 +58,7 @@ def parse_args():
     ap.add_argument("--batch-pins", type=float, default=1e8,
                     help="served: a batch stops growing at this many pins (0: memory budget only)")
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--subrounds", type=int, default=8)
+    ap.add_argument("--subrounds", type=int, default=7)
     ap.add_argument("--no-baseline", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     return ap.parse_args()

@@ -64,7 +64,7 @@ typedef struct {
   int32_t activation_threshold; /* hyperedge_size_activation_threshold; <= 0 means no limit */
   int32_t rebalancing;          /* 1: all vertices start active and zero-gain rebalancing
                                    moves are allowed; 0: border vertices start active */
-  int32_t subrounds;            /* sub-rounds per round (>= 1) */
+  int32_t subrounds;            /* sub-rounds per round (>= 1; default 7) */
   int32_t revert;               /* 1: undo moves whose reverse now strictly improves km1 */
   int32_t rollback;             /* 1: undo a sub-round whose summed delta is positive */
   int32_t flags;                /* LPGPU_FLAG_* */

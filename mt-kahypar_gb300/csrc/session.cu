@@ -349,7 +349,7 @@ void lpgpu_config_default(lpgpu_config* cfg) {
   cfg->rounds = 5;
   cfg->activation_threshold = 100;
   cfg->rebalancing = 1;
-  cfg->subrounds = 8;
+  cfg->subrounds = 7;
   cfg->revert = 1;
   cfg->rollback = 1;
   cfg->flags = 0;

@@ -49,7 +49,7 @@ class Request:
     def latency(self):
         return None if self.finish is None else self.finish - self.arrival
 
-    def footprint(self, subrounds=8):
+    def footprint(self, subrounds=7):
         return estimate_footprint(self.hg.n, self.hg.m, self.hg.num_pins, self.k, subrounds)
 
 
@@ -93,7 +93,7 @@ class RefineServer:
     lpgpu_estimate_footprint. Tests replace them to check the scheduling alone.
     """
 
-    def __init__(self, device=0, slots=2, budget_bytes=150 << 30, subrounds=8, max_batch=4096,
+    def __init__(self, device=0, slots=2, budget_bytes=150 << 30, subrounds=7, max_batch=4096,
                  session_factory=Session, runner=_run_batch, footprint=None, max_batch_pins=None):
         self.device = device
         self.slots = slots
@@ -215,7 +215,7 @@ def replay(server: RefineServer, requests):
     return server.stats
 
 
-def plain_loop(requests, device=0, subrounds=8, flags=FLAG_NO_GRAPH):
+def plain_loop(requests, device=0, subrounds=7, flags=FLAG_NO_GRAPH):
     """Baseline: one request at a time in arrival order on one session."""
     stats = ServeStats()
     t0 = time.perf_counter()
