@@ -270,6 +270,25 @@ def test_pin_count_width_boundary(lp, orc, big):
         out[0].close()
 
 
+def test_quality_against_async_lp(lp, orc):
+    """Quality bar: with the default configuration the device's km1 after
+    refinement is at most 0.5 % above the reference-style asynchronous LP's
+    (oracle, 4 threads), mean over seeds of the 16,384-vertex workload."""
+    from lpgpu import gen
+    dev, ref = [], []
+    for seed in range(3):
+        inst = gen.plain_small(seed=seed)
+        s = session(lp, inst.hg, inst.k, inst.part, lmax=inst.lmax, perfect=inst.perfect)
+        r = s.refine(lp.default_config(rounds=inst.rounds))
+        s.close()
+        pa, _ = orc.lp_async(inst.hg, inst.k, inst.lmax, inst.perfect, inst.part, rounds=inst.rounds, threads=4,
+                             seed=seed)
+        _, conn, _ = orc.init_partition(inst.hg, inst.k, pa)
+        dev.append(r.km1_after)
+        ref.append(orc.metrics(inst.hg, inst.k, conn)[0])
+    assert np.mean(dev) <= 1.005 * np.mean(ref), (dev, ref)
+
+
 def test_refinement_nodes_and_threshold(lp, orc):
     from lpgpu import gen
     inst = gen.random_small(5, n=500, m=600, k=4)
