@@ -75,7 +75,7 @@ enum Scalar : int {
   kEpoch = 8,      // activation stamp of the current round
   kDone = 9,       // arrival counter of the last-CTA pattern
   kOverCount = 10, // number of overflowing target blocks
-  kHeavyCount = 11, // vertices the sweep deferred to the heavy-vertex kernel
+  kHeavyCount = 11, // heavy vertices a per-vertex query deferred to k_sweep_heavy
   kRevCount = 12,  // moves marked for revert in the current sub-round
   kScalars = 16
 };
@@ -157,7 +157,7 @@ struct RoundCtx {
   const int32_t* inst_k;    // blocks of each instance
   int64_t* inst_delta;      // per-instance summed delta of the current sub-round
   int32_t* over_ids;        // target blocks that overflow (count in scal[kOverCount])
-  int32_t* heavy;           // list positions deferred by the sweep (count in scal[kHeavyCount])
+  int32_t* heavy;           // vertices a per-vertex query deferred (count in scal[kHeavyCount])
   int32_t* revl;            // list positions of moves marked for revert (count in scal[kRevCount])
 };
 

@@ -986,9 +986,13 @@ __device__ void heavy_vertex(const RoundCtx& c, int64_t pos, int64_t v, int zero
 // Sweep: the best move of every active vertex (moveVertex's isBorderNode +
 // computeMaxGainMove, label_propagation_refiner.h:82-95) on the current state.
 //
-// A warp takes a tile of 32 list entries (lane = vertex) and walks the tile's
-// concatenated incidence lists in windows of 32 incidences (lane =
-// incidence); the gathers of B windows are issued before any is consumed.
+// Heavy vertices (sweep_heavy) lead a sub-round's list; the first `nheavy`
+// CTAs take them one per CTA (heavy_vertex) while the other CTAs walk the
+// rest. For k <= 128 a lane evaluates its own vertex (lv_vertex, bit-sliced
+// counters). For k > 128 a warp takes a tile of 32 list entries (lane =
+// vertex) and walks the tile's concatenated incidence lists in windows of 32
+// incidences (lane = incidence); the gathers of B windows are issued before
+// any is consumed.
 // Each incidence lane loads its net's record {Λ(e), Λ1(e)} (one 32-byte
 // sector for k <= 128) and, for weighted nets, w(e); Λ words are transposed
 // across the warp so that lane l holds, per 32-block word t, the mask of
