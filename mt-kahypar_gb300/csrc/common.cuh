@@ -209,9 +209,9 @@ cudaError_t scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t count, i
                                int64_t tmp_elems, cudaStream_t st);
 int64_t scan_tmp_elems(int64_t count);
 
-cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const int64_t* net_off,
+cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, int64_t P, const int64_t* net_off,
                                    const int32_t* pins, int64_t* vtx_off, int32_t* inets,
-                                   int64_t* cursor, int64_t* scan_tmp, int64_t scan_tmp_elems,
+                                   int32_t* rank, int64_t* scan_tmp, int64_t scan_tmp_elems,
                                    int64_t* deg_hist);
 cudaError_t launch_init_partition(const Launch& L, const RoundCtx& c);
 cudaError_t launch_metrics(const Launch& L, const RoundCtx& c);

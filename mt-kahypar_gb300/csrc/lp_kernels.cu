@@ -231,10 +231,13 @@ __device__ __forceinline__ int packed_incidences(bool sel, int64_t o0, int deg,
 
 // ============================================================ incidence
 
-__global__ void k_count_pins(const int32_t* __restrict__ pins, int64_t P, int64_t* __restrict__ cnt) {
+// Degrees by one atomic per pin; the count returned is the pin's rank among its
+// vertex's incidences, i.e. its slot in the vertex's incident-net list.
+__global__ void k_count_pins(const int32_t* __restrict__ pins, int64_t P, int64_t* __restrict__ cnt,
+                             int32_t* __restrict__ rank) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P;
        i += (int64_t)gridDim.x * blockDim.x)
-    atomicAdd(reinterpret_cast<ull*>(&cnt[pins[i]]), 1ull);
+    rank[i] = (int32_t)atomicAdd(reinterpret_cast<ull*>(&cnt[pins[i]]), 1ull);
 }
 
 // Incidences per log2 degree bucket (bucket j: degree in [2^j, 2^(j+1))),
@@ -260,12 +263,14 @@ __global__ void k_degree_hist(int64_t n, const int64_t* __restrict__ cnt, int64_
     atomicAdd(reinterpret_cast<ull*>(&hist[threadIdx.x]), s_h[threadIdx.x]);
 }
 
-// Every pin appends its net id to its vertex's incident-net list. A warp
-// takes 32 nets and walks their pins in packed 32-pin groups (nets of more
-// than 32 pins alone, 32 pins at a time), so small nets keep every lane busy.
+// Every pin writes its net id into its slot of its vertex's incident-net list
+// (list start + the rank k_count_pins returned). A warp takes 32 nets and
+// walks their pins in packed 32-pin groups (nets of more than 32 pins alone,
+// 32 pins at a time), so small nets keep every lane busy.
 __global__ void __launch_bounds__(256) k_scatter_incidence(int64_t m, const int64_t* __restrict__ net_off,
                                                            const int32_t* __restrict__ pins,
-                                                           int64_t* __restrict__ cursor,
+                                                           const int64_t* __restrict__ vtx_off,
+                                                           const int32_t* __restrict__ rank,
                                                            int32_t* __restrict__ inets) {
   __shared__ unsigned char s_own[256];
   const int lane = lane_id();
@@ -277,26 +282,20 @@ __global__ void __launch_bounds__(256) k_scatter_incidence(int64_t m, const int6
     const int64_t o0 = sel ? net_off[e] : 0;
     const int deg = sel ? (int)(net_off[e + 1] - o0) : 0;
     packed_incidences(sel, o0, deg, own, [&](bool has, int ow, int64_t j) -> int {
-      if (has) {
-        const int64_t pos = (int64_t)atomicAdd(reinterpret_cast<ull*>(&cursor[pins[j]]), 1ull);
-        inets[pos] = (int32_t)(base + ow);
-      }
+      if (has) inets[vtx_off[pins[j]] + rank[j]] = (int32_t)(base + ow);
       return 0;
     });
   }
 }
 
-cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const int64_t* net_off,
+cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, int64_t P, const int64_t* net_off,
                                    const int32_t* pins, int64_t* vtx_off, int32_t* inets,
-                                   int64_t* cursor, int64_t* scan_tmp, int64_t scan_tmp_elems,
+                                   int32_t* rank, int64_t* scan_tmp, int64_t scan_tmp_elems,
                                    int64_t* deg_hist) {
-  int64_t P = 0;
-  cudaError_t e = cudaMemcpyAsync(&P, net_off + m, sizeof(int64_t), cudaMemcpyDeviceToHost, L.st);
+  cudaError_t e = cudaMemsetAsync(vtx_off, 0, sizeof(int64_t) * (n + 1), L.st);
   if (e != cudaSuccess) return e;
-  if ((e = cudaStreamSynchronize(L.st)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(vtx_off, 0, sizeof(int64_t) * (n + 1), L.st)) != cudaSuccess) return e;
   if (P > 0) {
-    k_count_pins<<<grid_for(L, P, 256, 8), 256, 0, L.st>>>(pins, P, vtx_off);
+    k_count_pins<<<grid_for(L, P, 256, 8), 256, 0, L.st>>>(pins, P, vtx_off, rank);
     LAUNCHED("k_count_pins");
   }
   if (deg_hist) {
@@ -308,11 +307,8 @@ cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, const 
   }
   if ((e = scan_exclusive_i64(vtx_off, vtx_off, n + 1, scan_tmp, scan_tmp_elems, L.st)) != cudaSuccess)
     return e;
-  if ((e = cudaMemcpyAsync(cursor, vtx_off, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, L.st)) !=
-      cudaSuccess)
-    return e;
   if (m > 0) {
-    k_scatter_incidence<<<grid_for(L, m, 256, 8), 256, 0, L.st>>>(m, net_off, pins, cursor, inets);
+    k_scatter_incidence<<<grid_for(L, m, 256, 8), 256, 0, L.st>>>(m, net_off, pins, vtx_off, rank, inets);
     LAUNCHED("k_scatter_incidence");
   }
   return cudaGetLastError();

@@ -574,9 +574,10 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
   s->max_we = (int32_t)h[kVMaxWe];
   s->max_net_size = h[kVMaxSize];
   s->unit_nets = h[kVNonUnit] == 0;
-  CK(launch_build_incidence(s->launch(), n, m, s->net_off.p, s->pins.p, s->vtx_off.p, s->inets.p,
-                            reinterpret_cast<int64_t*>(s->seg_key.p), s->scan_tmp.p, s->scan_tmp_n,
-                            s->vout.p));
+  TmpBuf<int32_t> rank(s->mem);  // each pin's slot in its vertex's incident-net list
+  CK(rank.alloc((size_t)P));
+  CK(launch_build_incidence(s->launch(), n, m, P, s->net_off.p, s->pins.p, s->vtx_off.p, s->inets.p, rank.p(),
+                            s->scan_tmp.p, s->scan_tmp_n, s->vout.p));
   CK(cudaMemcpyAsync(s->deg_inc, s->vout.p, sizeof(s->deg_inc), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   s->has_hg = true;
