@@ -2614,6 +2614,7 @@ __device__ __forceinline__ void flat_undo_item(const RoundCtx& c, FlatSmem& f, i
 // the CTA's block-weight deltas.
 __device__ __forceinline__ void undo_epilogue(const RoundCtx& c, int round, int64_t att, int64_t undone,
                                               int slot, ull* s_dw, int kdw) {
+  if (!__syncthreads_or(undone != 0)) return;  // this CTA undid nothing: no sums, no weight deltas
   att = block_sum_i64(att);
   undone = block_sum_i64(undone);
   if (threadIdx.x == 0 && undone) {
@@ -2682,7 +2683,7 @@ __global__ void __launch_bounds__(kFlatThreads) k_undo_reverts(RoundCtx c, int r
     if (roll_tail) {
       const bool roll = *(volatile int64_t*)&c.scal[kDeltaSub] > 0;
       __syncthreads();
-      rollback_ranges(c, round, sub, roll, f, s_dw, 0, 1);
+      if (roll) rollback_ranges(c, round, sub, true, f, s_dw, 0, 1);  // otherwise nothing to undo or book
     }
     close_subround(c, round);
   }
