@@ -243,8 +243,12 @@ cudaError_t launch_check_partition(const Launch& L, int64_t n, int32_t* part, in
 
 // Batches uploaded one instance at a time (validate.cu): instance i's local
 // pins and net offsets, copied into place, are shifted to union ids.
+// Instance-local vertex ids and pin offsets to union ones; with `staged`, the
+// instances' offset arrays (m_i + 1 entries each, back to back) are moved into
+// net_off first.
 cudaError_t launch_rebase_instances(const Launch& L, int I, const int64_t* inst_voff, const int64_t* inst_noff,
-                                    const int64_t* inst_poff, int64_t* net_off, int32_t* pins);
+                                    const int64_t* inst_poff, int64_t* net_off, int32_t* pins,
+                                    const int64_t* staged);
 cudaError_t launch_fill_ones(const Launch& L, int32_t* p, int64_t count);
 // Multilevel projection: part[v] = coarse_part[map[v]]; *check != 0 when a
 // map entry lies outside [0, nc).

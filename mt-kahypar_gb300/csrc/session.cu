@@ -62,6 +62,35 @@ struct TmpBuf {
   T* p() const { return b.p; }
 };
 
+// Copies of consecutive pieces in one direction: a piece whose host and
+// device ranges both continue the previous piece's joins it, so buffers that
+// callers keep back to back (arenas of many instances) go in one call.
+struct CopyRun {
+  cudaStream_t st;
+  cudaMemcpyKind kind;
+  char* dst = nullptr;
+  const char* src = nullptr;
+  size_t bytes = 0;
+  cudaError_t add(void* d, const void* h, size_t b) {
+    if (b == 0) return cudaSuccess;
+    if (bytes && static_cast<char*>(d) == dst + bytes && static_cast<const char*>(h) == src + bytes) {
+      bytes += b;
+      return cudaSuccess;
+    }
+    const cudaError_t e = flush();
+    dst = static_cast<char*>(d);
+    src = static_cast<const char*>(h);
+    bytes = b;
+    return e;
+  }
+  cudaError_t flush() {
+    if (!bytes) return cudaSuccess;
+    const size_t b = bytes;
+    bytes = 0;
+    return cudaMemcpyAsync(dst, src, b, kind, st);
+  }
+};
+
 static int word_count(int k) { return (k + 31) / 32; }
 static int word_class_of(int k) {
   int w = 1;
@@ -458,6 +487,7 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
   s->P = P;
   const int32_t I = inst_voff ? num_inst : 1;
   Mem* fp = &s->mem;
+  TmpBuf<int64_t> staged(s->mem);  // per-instance offsets before the rebase
   CK(s->net_off.alloc(m + 1, fp));
   CK(s->vtx_off.alloc(n + 1, fp));
   CK(s->pins.alloc(P, fp));
@@ -503,17 +533,23 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
     }
     if (unit_v) CK(launch_fill_ones(L, s->w_v.p, n));
     if (unit_e) CK(launch_fill_ones(L, s->w_e.p, m));
+    // offsets with their closing entry (m_i + 1 each) go back to back into a
+    // staging buffer, instance i's at inst_noff[i] + i; the rebase moves them
+    CK(staged.alloc((size_t)(m + I)));
+    CopyRun c_off{st, cudaMemcpyHostToDevice}, c_pin{st, cudaMemcpyHostToDevice},
+        c_wv{st, cudaMemcpyHostToDevice}, c_we{st, cudaMemcpyHostToDevice};
     for (int32_t i = 0; i < I; ++i) {
       const lpgpu_instance& x = insts[i];
       const int64_t ni = x.num_vertices, mi = x.num_nets, pi = inst_poff[i + 1] - inst_poff[i];
-      if (mi > 0)
-        CK(cudaMemcpyAsync(s->net_off.p + inst_noff[i], x.net_offsets, sizeof(int64_t) * mi, cudaMemcpyHostToDevice, st));
-      if (pi > 0) CK(cudaMemcpyAsync(s->pins.p + inst_poff[i], x.pins, sizeof(int32_t) * pi, cudaMemcpyHostToDevice, st));
-      if (ni > 0 && x.vertex_weights)
-        CK(cudaMemcpyAsync(s->w_v.p + inst_voff[i], x.vertex_weights, sizeof(int32_t) * ni, cudaMemcpyHostToDevice, st));
-      if (mi > 0 && x.net_weights)
-        CK(cudaMemcpyAsync(s->w_e.p + inst_noff[i], x.net_weights, sizeof(int32_t) * mi, cudaMemcpyHostToDevice, st));
+      if (mi > 0) CK(c_off.add(staged.p() + inst_noff[i] + i, x.net_offsets, sizeof(int64_t) * (mi + 1)));
+      if (pi > 0) CK(c_pin.add(s->pins.p + inst_poff[i], x.pins, sizeof(int32_t) * pi));
+      if (ni > 0 && x.vertex_weights) CK(c_wv.add(s->w_v.p + inst_voff[i], x.vertex_weights, sizeof(int32_t) * ni));
+      if (mi > 0 && x.net_weights) CK(c_we.add(s->w_e.p + inst_noff[i], x.net_weights, sizeof(int32_t) * mi));
     }
+    CK(c_off.flush());
+    CK(c_pin.flush());
+    CK(c_wv.flush());
+    CK(c_we.flush());
     CK(cudaMemcpyAsync(s->net_off.p + m, &P, sizeof(int64_t), cudaMemcpyHostToDevice, st));  // synchronized below
   }
   if (n > 0) CK(cudaMemsetAsync(s->next_flag.p, 0, n, st));
@@ -537,7 +573,8 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
       TmpBuf<int64_t> poff(s->mem);
       CK(poff.alloc(I + 1));
       CK(cudaMemcpyAsync(poff.p(), inst_poff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
-      CK(launch_rebase_instances(L, I, s->inst_voff.p, s->inst_noff.p, poff.p(), s->net_off.p, s->pins.p));
+      CK(launch_rebase_instances(L, I, s->inst_voff.p, s->inst_noff.p, poff.p(), s->net_off.p, s->pins.p,
+                                 staged.p()));
       CK(cudaStreamSynchronize(st));
     }
   } else {
@@ -667,10 +704,12 @@ static lpgpu_status set_partition_impl(lpgpu_session* s, int32_t K, int32_t kmax
   if (part_dev) {
     if (s->n > 0) CK(cudaMemcpyAsync(s->part.p, part_dev, sizeof(int32_t) * s->n, cudaMemcpyDeviceToDevice, st));
   } else if (parts) {
+    CopyRun run{st, cudaMemcpyHostToDevice};
     for (int32_t i = 0; i < s->num_inst; ++i) {
       const int64_t v0 = s->h_inst_voff[i], ni = s->h_inst_voff[i + 1] - v0;
-      if (ni > 0) CK(cudaMemcpyAsync(s->part.p + v0, parts[i], sizeof(int32_t) * ni, cudaMemcpyHostToDevice, st));
+      if (ni > 0) CK(run.add(s->part.p + v0, parts[i], sizeof(int32_t) * ni));
     }
+    CK(run.flush());
   } else if (s->n > 0) {
     CK(cudaMemcpyAsync(s->part.p, part, sizeof(int32_t) * s->n, cudaMemcpyHostToDevice, st));
   }
@@ -1029,10 +1068,12 @@ lpgpu_status lpgpu_session_get_partition_instances(lpgpu_session* s, int32_t* co
     if (!partitions[i] && s->h_inst_voff[i + 1] > s->h_inst_voff[i]) return invalid("null output");
   DeviceGuard g(s->device);
   CK(launch_local_blocks(s->launch(), s->n, s->part.p, s->vinst.p, s->inst_boff.p, s->seg_w.p));
+  CopyRun run{s->st, cudaMemcpyDeviceToHost};
   for (int32_t i = 0; i < s->num_inst; ++i) {
     const int64_t v0 = s->h_inst_voff[i], ni = s->h_inst_voff[i + 1] - v0;
-    if (ni > 0) CK(cudaMemcpyAsync(partitions[i], s->seg_w.p + v0, sizeof(int32_t) * ni, cudaMemcpyDeviceToHost, s->st));
+    if (ni > 0) CK(run.add(partitions[i], s->seg_w.p + v0, sizeof(int32_t) * ni));
   }
+  CK(run.flush());
   CK(cudaStreamSynchronize(s->st));
   return LPGPU_OK;
 }

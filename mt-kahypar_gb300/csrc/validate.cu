@@ -195,16 +195,21 @@ __global__ void k_check_partition(int64_t n, int32_t* __restrict__ part, int k, 
 // CTA i shifts instance i's pins by its first vertex and its net offsets by
 // its first pin (the ranges come from the host, so no access depends on the
 // unchecked input).
+// Instance-local ids to union ids, one CTA per instance. With `staged`, the
+// instances' offset arrays (m_i + 1 entries each) lie back to back there,
+// instance i's starting at inst_noff[i] + i, and are moved into place.
 __global__ void k_rebase_instances(const int64_t* __restrict__ inst_voff, const int64_t* __restrict__ inst_noff,
                                    const int64_t* __restrict__ inst_poff, int64_t* __restrict__ net_off,
-                                   int32_t* __restrict__ pins) {
+                                   int32_t* __restrict__ pins, const int64_t* __restrict__ staged) {
   const int i = blockIdx.x;
   const int32_t v0 = (int32_t)inst_voff[i];
   const int64_t p0 = inst_poff[i];
   if (v0)
     for (int64_t q = p0 + threadIdx.x; q < inst_poff[i + 1]; q += blockDim.x)
       pins[q] = (int32_t)((uint32_t)pins[q] + (uint32_t)v0);  // wraps: out-of-range ids stay out of range
-  if (p0)
+  if (staged)
+    for (int64_t e = inst_noff[i] + threadIdx.x; e < inst_noff[i + 1]; e += blockDim.x) net_off[e] = staged[e + i] + p0;
+  else if (p0)
     for (int64_t e = inst_noff[i] + threadIdx.x; e < inst_noff[i + 1]; e += blockDim.x) net_off[e] += p0;
 }
 
@@ -270,9 +275,10 @@ cudaError_t launch_check_partition(const Launch& L, int64_t n, int32_t* part, in
 }
 
 cudaError_t launch_rebase_instances(const Launch& L, int I, const int64_t* inst_voff, const int64_t* inst_noff,
-                                    const int64_t* inst_poff, int64_t* net_off, int32_t* pins) {
+                                    const int64_t* inst_poff, int64_t* net_off, int32_t* pins,
+                                    const int64_t* staged) {
   if (I > 0) {
-    k_rebase_instances<<<I, 256, 0, L.st>>>(inst_voff, inst_noff, inst_poff, net_off, pins);
+    k_rebase_instances<<<I, 256, 0, L.st>>>(inst_voff, inst_noff, inst_poff, net_off, pins, staged);
     add_kernel_launches(1);
   }
   return cudaGetLastError();

@@ -97,6 +97,54 @@ def test_instance_buffers_equal_union(lp, seed):
         assert np.array_equal(a.pin_counts(), b.pin_counts())
 
 
+@pytest.mark.parametrize("seed", range(2))
+def test_instance_buffers_back_to_back(lp, seed):
+    """Instances whose arrays lie back to back in shared buffers (copies that
+    the library merges), some of them without nets or weights, give the same
+    results as separate buffers; outputs written back to back as well."""
+    from lpgpu import gen
+    insts = _instances(seed + 20, 7)
+    # an instance without nets and one with unit weights (NULL) in the middle
+    empty = gen.Hypergraph(5, 0, np.zeros(1, np.int64), np.zeros(0, np.int32), np.ones(5, np.int32),
+                           np.zeros(0, np.int32))
+    hgs = [x.hg for x in insts[:3]] + [empty] + [x.hg for x in insts[3:]]
+    ks = [x.k for x in insts[:3]] + [2] + [x.k for x in insts[3:]]
+    parts = [x.part for x in insts[:3]] + [np.array([0, 1, 0, 1, 0], np.int32)] + [x.part for x in insts[3:]]
+
+    def arena(arrays, dtype):
+        buf = np.concatenate([np.asarray(a, dtype) for a in arrays]) if arrays else np.zeros(0, dtype)
+        views, o = [], 0
+        for a in arrays:
+            views.append(buf[o:o + len(a)])
+            o += len(a)
+        return buf, views
+
+    b_off, offs = arena([h.net_off for h in hgs], np.int64)
+    b_pin, pins = arena([h.pins for h in hgs], np.int32)
+    b_wv, wvs = arena([h.w_v for h in hgs], np.int32)
+    b_we, wes = arena([h.w_e for h in hgs], np.int32)
+    b_pt, pts = arena(parts, np.int32)
+    packed = [gen.Hypergraph(h.n, h.m, offs[i], pins[i], wvs[i], None if i == 5 else wes[i])
+              for i, h in enumerate(hgs)]
+    loose = [gen.Hypergraph(h.n, h.m, h.net_off.copy(), h.pins.copy(), h.w_v.copy(),
+                            None if i == 5 else h.w_e.copy()) for i, h in enumerate(hgs)]
+    cfg = lp.default_config(rounds=4)
+    with lp.Session(0) as a, lp.Session(0) as b:
+        a.upload_instances(packed)
+        a.set_partition_instances(ks, pts, eps=0.05)
+        ra = a.refine(cfg)
+        b_out, outs = arena([np.zeros(h.n, np.int32) for h in hgs], np.int32)
+        a.partition_instances(outs)
+        b.upload_instances(loose)
+        b.set_partition_instances(ks, [p.copy() for p in parts], eps=0.05)
+        rb = b.refine(cfg)
+        pb = b.partition_instances()
+        assert (ra.km1_before, ra.km1_after, ra.delta) == (rb.km1_before, rb.km1_after, rb.delta)
+        assert all(np.array_equal(x, y) for x, y in zip(outs, pb))
+        assert np.array_equal(a.pin_counts(), b.pin_counts())
+        assert np.array_equal(a.instance_km1(), b.instance_km1())
+
+
 def test_instance_buffers_are_checked(lp):
     from lpgpu import gen
     insts = _instances(5, 4)
