@@ -114,6 +114,23 @@ def _p(a, t):
     return None if a is None else a.ctypes.data_as(t)
 
 
+# lpgpu_instance as a numpy record (same layout as InstanceDesc on 64-bit
+# hosts): descriptors of many instances are filled column by column.
+_INSTANCE_DTYPE = np.dtype([("num_vertices", "<i8"), ("num_nets", "<i8"), ("net_offsets", "<u8"),
+                            ("pins", "<u8"), ("vertex_weights", "<u8"), ("net_weights", "<u8")])
+assert _INSTANCE_DTYPE.itemsize == ctypes.sizeof(InstanceDesc)
+
+
+def _addr(a):
+    """Address of a contiguous array's first element (0 for None)."""
+    return 0 if a is None else a.__array_interface__["data"][0]
+
+
+def _addresses(arrays):
+    """uintptr_t array of the arrays' addresses (a C array of pointers)."""
+    return np.fromiter((_addr(a) for a in arrays), np.uintp, len(arrays))
+
+
 def default_config(**over) -> Config:
     c = Config()
     lib().lpgpu_config_default(ctypes.byref(c))
@@ -177,18 +194,23 @@ class Session:
     def upload_instances(self, hgs):
         """Uploads a list of hypergraphs as one batch from their own buffers
         (lpgpu_session_upload_instances: no union is built on the host)."""
-        keep = []
-        descs = (InstanceDesc * len(hgs))()
-        for i, h in enumerate(hgs):
-            arrs = (np.ascontiguousarray(h.net_off, np.int64), np.ascontiguousarray(h.pins, np.int32),
-                    None if h.w_v is None else np.ascontiguousarray(h.w_v, np.int32),
-                    None if h.w_e is None else np.ascontiguousarray(h.w_e, np.int32))
-            keep.append(arrs)
-            descs[i] = InstanceDesc(h.n, h.m, _p(arrs[0], I64P), _p(arrs[1], I32P), _p(arrs[2], I32P),
-                                    _p(arrs[3], I32P))
-        nv = np.array([0] + [h.n for h in hgs], np.int64).cumsum()
-        ne = np.array([0] + [h.m for h in hgs], np.int64).cumsum()
-        _check(lib().lpgpu_session_upload_instances(self._h, ctypes.c_int32(len(hgs)), descs))
+        def arr(a, dt):
+            return None if a is None else np.ascontiguousarray(a, dt)
+        offs = [arr(h.net_off, np.int64) for h in hgs]
+        pins = [arr(h.pins, np.int32) for h in hgs]
+        wvs = [arr(h.w_v, np.int32) for h in hgs]
+        wes = [arr(h.w_e, np.int32) for h in hgs]
+        descs = np.zeros(len(hgs), _INSTANCE_DTYPE)
+        descs["num_vertices"] = [h.n for h in hgs]
+        descs["num_nets"] = [h.m for h in hgs]
+        descs["net_offsets"] = _addresses(offs)
+        descs["pins"] = _addresses(pins)
+        descs["vertex_weights"] = _addresses(wvs)
+        descs["net_weights"] = _addresses(wes)
+        nv = np.concatenate([[0], np.cumsum(descs["num_vertices"])]).astype(np.int64)
+        ne = np.concatenate([[0], np.cumsum(descs["num_nets"])]).astype(np.int64)
+        _check(lib().lpgpu_session_upload_instances(self._h, ctypes.c_int32(len(hgs)),
+                                                    ctypes.c_void_p(descs.ctypes.data)))
         self.n, self.m = int(nv[-1]), int(ne[-1])
         self.inst_voff, self.inst_noff = nv, ne
         self.num_inst = len(hgs)
@@ -199,11 +221,12 @@ class Session:
         ks = np.ascontiguousarray(ks, np.int32)
         ep = np.ascontiguousarray(np.broadcast_to(np.asarray(eps, np.float64), ks.shape), np.float64)
         arrs = [np.ascontiguousarray(p, np.int32) for p in parts]
-        ptrs = (I32P * len(arrs))(*[_p(a, I32P) for a in arrs])
+        ptrs = _addresses(arrs)
         self.k = int(ks.max())
         self.num_blocks = int(ks.sum())
         _check(lib().lpgpu_session_set_partition_instances(self._h, _p(ks, I32P),
-                                                           ep.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ptrs))
+                                                           ep.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                           ctypes.c_void_p(ptrs.ctypes.data)))
         return self
 
     def partition_instances(self, out=None):
@@ -211,8 +234,10 @@ class Session:
         off = self.inst_voff
         outs = out if out is not None else [np.empty(int(off[i + 1] - off[i]), np.int32)
                                             for i in range(self.num_inst)]
-        ptrs = (I32P * len(outs))(*[_p(a, I32P) for a in outs])
-        _check(lib().lpgpu_session_get_partition_instances(self._h, ptrs))
+        if any(not a.flags.c_contiguous or a.dtype != np.int32 for a in outs):
+            raise ValueError("outputs must be contiguous int32 arrays")
+        ptrs = _addresses(outs)
+        _check(lib().lpgpu_session_get_partition_instances(self._h, ctypes.c_void_p(ptrs.ctypes.data)))
         return outs
 
     def set_partition_batch(self, ks, parts, eps=0.03):
