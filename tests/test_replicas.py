@@ -48,7 +48,7 @@ def test_dist_max_and_sum_over_two_gloo_ranks():
 
 @pytest.mark.slow
 def test_reference_arm_under_torchrun_two_ranks():
-    """`bench.py --impl reference` launched as the driver does for N = 2: rank 0
+    """`bench.py --impl reference` under torchrun with two ranks on one node: rank 0
     prints one JSON line, the other rank exits 0 without work."""
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
