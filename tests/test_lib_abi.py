@@ -40,6 +40,20 @@ def test_config_defaults_match_preset(lp):
     assert c.subrounds >= 1
 
 
+def test_instance_descriptor_layout(lp):
+    """The numpy record the binding fills for lpgpu_session_upload_instances has
+    the field offsets of the C struct (ctypes mirror), and the pointer arrays
+    hold the arrays' addresses (0 for a missing one)."""
+    import numpy as np
+    dt = lp._INSTANCE_DTYPE
+    assert dt.itemsize == ctypes.sizeof(lp.InstanceDesc)
+    for name, _ in lp.InstanceDesc._fields_:
+        assert dt.fields[name][1] == getattr(lp.InstanceDesc, name).offset, name
+    a, b = np.arange(5, dtype=np.int32), np.arange(3, dtype=np.int64)
+    ptrs = lp._addresses([a, None, b])
+    assert ptrs.dtype == np.uintp and list(ptrs) == [a.ctypes.data, 0, b.ctypes.data]
+
+
 def test_status_strings(lp):
     L = lp.lib()
     for s in range(8):
