@@ -173,6 +173,27 @@ def test_hub_vertices_and_heavy_weights(lp, orc, seed, k, weighted):
         out[0].close()
 
 
+@pytest.mark.parametrize("weighted", [False, True])
+def test_heavy_vertices_above_128_blocks(lp, orc, weighted):
+    """k = 200 (8 words per net record): hubs of degree > 1,024 are heavy for the
+    warp-window sweep, so they lead their sub-round's list and run on the
+    sweep's dedicated CTAs (LP rounds) or in k_sweep_heavy (best-move query)."""
+    from lpgpu import gen
+    inst = gen.random_small(7, n=3000, m=4000, k=200, max_size=6, weighted=weighted, hubs=2, hub_frac=0.4,
+                            vw_hi=3)
+    hg, part = inst.hg, inst.part
+    assert np.diff(hg.vtx_off).max() > 1024
+    s = session(lp, hg, inst.k, part, lmax=inst.lmax, perfect=inst.perfect)
+    to, gain, border = s.best_moves()
+    eto, egain, eborder = orc.best_moves(hg, inst.k, part, inst.lmax)
+    assert np.array_equal(to, eto) and np.array_equal(gain, egain) and np.array_equal(border, eborder)
+    s.close()
+    for mode in (LP_MODES[1], LP_MODES[2]):
+        out = run_both(lp, orc, inst, 3, mode)
+        assert_same_run(*out, orc, inst)
+        out[0].close()
+
+
 LP_MODES = [
     dict(subrounds=1, revert=0, rollback=0, rebalancing=1),
     dict(subrounds=1, revert=1, rollback=1, rebalancing=1),
