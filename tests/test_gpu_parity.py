@@ -194,6 +194,29 @@ def test_heavy_vertices_above_128_blocks(lp, orc, weighted):
         out[0].close()
 
 
+def test_every_vertex_heavy(lp, orc):
+    """Net weights up to 2,000: w(e) >= 2^8 makes every vertex with an incident
+    net heavy for the lane counters, so nearly all of the sweep runs on its
+    heavy CTAs (one vertex per CTA) and one CTA walks the rest."""
+    from lpgpu import gen
+    inst = gen.random_small(3, n=400, m=480, k=6, max_size=7, weighted=True)
+    rng = np.random.default_rng(9)
+    hg = inst.hg
+    w_e = rng.integers(1, 2000, size=hg.m).astype(np.int32)
+    w_e[0] = 1999
+    heavy = gen.Hypergraph(hg.n, hg.m, hg.net_off, hg.pins, hg.w_v, w_e).with_incidence()
+    inst2 = gen.Instance("heavy", heavy, inst.k, inst.eps, inst.part, 4)
+    s = session(lp, heavy, inst2.k, inst2.part, lmax=inst2.lmax, perfect=inst2.perfect)
+    to, gain, border = s.best_moves()
+    eto, egain, eborder = orc.best_moves(heavy, inst2.k, inst2.part, inst2.lmax)
+    assert np.array_equal(to, eto) and np.array_equal(gain, egain) and np.array_equal(border, eborder)
+    s.close()
+    for mode in (LP_MODES[1], LP_MODES[2]):
+        out = run_both(lp, orc, inst2, 4, mode)
+        assert_same_run(*out, orc, inst2)
+        out[0].close()
+
+
 LP_MODES = [
     dict(subrounds=1, revert=0, rollback=0, rebalancing=1),
     dict(subrounds=1, revert=1, rollback=1, rebalancing=1),
