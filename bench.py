@@ -4,8 +4,11 @@
 A step is one full refinement of the row-net workload from its initial
 partition: initializePartition (block weights, pin counts, connectivity sets)
 followed by 10 synchronous LP rounds and the km1 recompute. The metric is
-pins processed per second (sum over rounds of the degrees of the swept
-vertices, divided by the step time).
+pins per LP round per second: the instance's pin count times the configured
+rounds, divided by the step time. Both arms count the same nominal work, so
+the ratio of their values is the ratio of their refinement times; the pins
+each arm actually swept (sum over rounds of the degrees of its active
+vertices) are reported beside it as `swept_pins_per_s`.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
 
@@ -13,8 +16,10 @@ GPU arm (`value`): inputs resident in HBM, device time with CUDA events on
 the session stream. `e2e`: the same work through the public session API from
 pinned host buffers (upload + set_partition + refine + download per step),
 wall-clock. `roofline`: the sweep kernel (dominant) against the measured HBM
-copy bandwidth. `cpu_baseline`: the reference-style asynchronous LP (CPU
-restatement, all host cores) on one full refinement of the same instance.
+copy bandwidth, and `round_frac`: the algorithmic bytes of sweep, selection
+and commit of a whole step over the step time, against the same peak.
+`cpu_baseline`: the reference-style asynchronous LP (CPU restatement, all
+host cores) on one full refinement of the same instance.
 
 Reference arm (`--impl reference`): the reference's LP algorithm cannot be
 built here (TBB legacy task API, hwloc, Boost, un-vendored submodule), so its
@@ -38,7 +43,7 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-METRIC = "LP refinement throughput (pins processed per second)"
+METRIC = "LP refinement throughput (pins per LP round per second: pins x rounds / refinement time)"
 UNIT = "pins/s"
 FALLBACK_HBM_GBS = 6800.0
 
@@ -181,7 +186,22 @@ def sweep_bytes(stats, k):
     return sum(s["active"] * 28 + s["pins"] * (12 + L) for s in stats)
 
 
+def round_bytes(stats, k, subrounds):
+    """Algorithmic bytes of the LP rounds of one refinement: sweep (above);
+    selection: the candidate record read and the sorted key written per swept
+    vertex (8 + 8 B) plus 8 B per block and sub-round; commit: per committed
+    move its record, offsets and part write (8 + 8 + 4 B), per incidence of a
+    committed move its net id, two Φ read-modify-writes and w(e)
+    (4 + 2 * (4 + 4) + 4 B), and 8 B per connectivity-set bit change."""
+    sweep = sweep_bytes(stats, k)
+    select = sum(s["active"] * 16 for s in stats) + len(stats) * subrounds * k * 8
+    commit = sum((s["moved"] + s["reverted"]) * 20 + s["moved_pins"] * 24 + s["toggles"] * 8 for s in stats)
+    return sweep, select, commit
+
+
 def run_cpu_async(inst, threads, rounds):
+    """One asynchronous refinement on the host cores: (nominal pins per round
+    per second, swept pins per second, swept pins, seconds, wall, stats)."""
     import oracle
     oracle.build_oracle()
     t0 = time.perf_counter()
@@ -190,7 +210,7 @@ def run_cpu_async(inst, threads, rounds):
     wall = time.perf_counter() - t0
     secs = sum(s["seconds"] for s in stats)
     pins = sum(s["pins"] for s in stats)
-    return pins / secs, pins, secs, wall, stats
+    return inst.hg.num_pins * rounds / secs, pins / secs, pins, secs, wall, stats
 
 
 def config_dict(args, inst, cfg=None):
@@ -215,17 +235,19 @@ def reference_arm(args):
         return 0
     inst = make_instance(args.workload, args.seed)
     threads = os.cpu_count() or 1
-    values, times = [], []
+    times, swept = [], []
     for i in range(args.warmup + args.steps):
-        v, pins, secs, wall, _ = run_cpu_async(inst, threads, inst.rounds)
+        _, sv, pins, secs, wall, _ = run_cpu_async(inst, threads, inst.rounds)
         if i >= args.warmup:
-            values.append(v)
             times.append(secs)
-    value = statistics.mean(values) if values else 0.0
+            swept.append(sv)
+    mean_s = statistics.mean(times) if times else float("inf")
+    value = inst.hg.num_pins * inst.rounds / mean_s
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * mean_s,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded generator, same instance as the GPU arm)",
+            "swept_pins_per_s": statistics.mean(swept) if swept else 0.0,
             "config": config_dict(args, inst),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"one full {inst.rounds}-round asynchronous LP refinement per step "
@@ -292,18 +314,23 @@ def gpu_arm(args):
     clk = clocks.stop()
     dist.barrier()
     max_ms = dist.reduce(elapsed_ms, "max")
-    total_pins = dist.reduce(pins, "sum")
-    value = total_pins / (max_ms / 1e3)
+    nominal = hg.num_pins * inst.rounds * args.steps  # pins x configured rounds, as the reference arm counts
+    value = dist.reduce(nominal, "sum") / (max_ms / 1e3)
+    swept = dist.reduce(pins, "sum") / (max_ms / 1e3)
 
     peak, peak_kind = hbm_peak()
     achieved = (sweep_alg / sweep_launches) / ((sweep_ms / sweep_launches) / 1e3) / 1e9
     ratio = ncu_traffic_ratio()
+    b_sweep, b_select, b_commit = round_bytes(stats, inst.k, cfg.subrounds)  # every step is the same refinement
+    step_s = max_ms / args.steps / 1e3
     roofline = {"bound": "hbm", "kernel": "k_sweep", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
                 if peak_kind == "measured" else "fallback 6.8 TB/s",
                 "traffic": None if ratio is None else ratio * sweep_alg / sweep_launches,
                 "algorithmic_bytes_per_launch": sweep_alg / sweep_launches,
-                "avg_launch_ms": sweep_ms / sweep_launches, "launches": sweep_launches}
+                "avg_launch_ms": sweep_ms / sweep_launches, "launches": sweep_launches,
+                "round_frac": (b_sweep + b_select + b_commit) / step_s / 1e9 / peak,
+                "round_bytes_per_step": {"sweep": b_sweep, "select": b_select, "commit": b_commit}}
 
     e2e = None
     if not args.no_e2e:
@@ -311,15 +338,16 @@ def gpu_arm(args):
     cpu = None
     if not args.no_baseline and rank == 0 and world == 1:
         threads = os.cpu_count() or 1
-        v, cpins, secs, wall, _ = run_cpu_async(inst, threads, inst.rounds)
-        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+        v, sv, cpins, secs, wall, _ = run_cpu_async(inst, threads, inst.rounds)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "swept_pins_per_s": sv,
                "sample": f"one full {inst.rounds}-round asynchronous LP refinement of the same instance "
-                         f"({cpins} pins in {secs:.2f} s; CPU restatement of the reference's TBB LP refiner)"}
+                         f"({inst.rounds} x {hg.num_pins} nominal pins, {cpins} pins swept, in {secs:.2f} s; "
+                         "CPU restatement of the reference's TBB LP refiner)"}
     r0 = results[-1]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": max_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic (seeded generator; no public dataset)",
+            "data": "synthetic (seeded generator; no public dataset)", "swept_pins_per_s": swept,
             "config": dict(config_dict(args, inst, cfg), parallelism=f"replicas{world}"),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk,
@@ -358,12 +386,11 @@ def e2e_leg(args, inst, cfg, device, dist):
         one()
     dist.barrier()
     t0 = time.perf_counter()
-    pins = 0
     for _ in range(args.steps):
-        pins += one().pins_processed
+        one()
     wall = time.perf_counter() - t0
     wall = dist.reduce(wall, "max")
-    pins = dist.reduce(pins, "sum")
+    pins = dist.reduce(hg.num_pins * inst.rounds * args.steps, "sum")
     s.close()
     h2d = 8 * (hg.m + 1) + 4 * hg.num_pins + 4 * hg.n + 4 * hg.m + 4 * hg.n
     return {"value": pins / wall, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4 * hg.n,

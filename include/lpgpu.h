@@ -90,12 +90,14 @@ typedef struct {
 
 /* Per-round statistics. */
 typedef struct {
-  int64_t active;
-  int64_t pins;
-  int64_t candidates;
-  int64_t moved;
-  int64_t reverted;
-  int64_t delta;
+  int64_t active;      /* vertices swept */
+  int64_t pins;        /* sum of the degrees of the swept vertices */
+  int64_t candidates;  /* vertices with a move to offer */
+  int64_t moved;       /* moves kept at the end of the round */
+  int64_t reverted;    /* moves undone (hindsight reverts and rolled-back sub-rounds) */
+  int64_t delta;       /* summed attributed objective delta */
+  int64_t moved_pins;  /* incidences of the committed moves, before reverts and rollbacks */
+  int64_t toggles;     /* connectivity-set bits the commits changed */
 } lpgpu_round_stats;
 
 typedef struct lpgpu_session_s lpgpu_session;
@@ -301,9 +303,28 @@ LPGPU_API lpgpu_status lpgpu_session_project_partition(lpgpu_session* fine, cons
  * selection (target-side prefix within L_max, source blocks kept non-empty)
  * and are committed. Stops when balanced, after max_rounds, or when a round
  * moves nothing; lpgpu_session_round_stats gives the rounds (active =
- * vertices in overloaded blocks). The reference's empty-block repair
- * (repairEmptyBlocks) is not part of it. */
+ * vertices in overloaded blocks). As in the reference (rebalancer.cpp:59-62),
+ * an imbalanced partition with empty blocks first gets the moves of
+ * lpgpu_session_repair_empty_blocks, each applied only if its target stays
+ * within its max weight and its source keeps weight > 0 (moveVertex,
+ * rebalancer.h:84-103); they form a first statistics record (active = n,
+ * pins = all pins, candidates = moves proposed, moved = moves applied). */
 LPGPU_API lpgpu_status lpgpu_session_rebalance(lpgpu_session* s, int32_t max_rounds, lpgpu_result* result);
+
+/* Rebalancer::repairEmptyBlocks (rebalancing/rebalancer.cpp:169-269) on the
+ * current partition, computed on the device and not applied. For every empty
+ * block b (weight 0), in increasing id: a vertex u in block p is eligible when
+ * c(p) > w(u) and w(u) <= L_max(b); its gain (km1Gain, positive = better) is
+ * Σ w(e) over its nets whose connectivity set holds b minus Σ w(e) over its
+ * nets with Φ(e, p) > 1. The k eligible vertices of highest gain (lowest id on
+ * ties: the bounded heap of rebalancer.cpp:204-213 on vertices in id order)
+ * are ordered by gain, then c(p), then id, all descending
+ * (rebalancer.cpp:228-232), and the first one no earlier block took is b's
+ * move. A block without an eligible vertex stays empty. The arrays receive
+ * up to k moves (each needs k entries); *count their number. Single-instance
+ * sessions only. */
+LPGPU_API lpgpu_status lpgpu_session_repair_empty_blocks(lpgpu_session* s, int32_t* vertices, int32_t* from,
+                                                         int32_t* to, int32_t* gain, int32_t* count);
 
 /* Device-resident gain cache (initializeGainCache, partitioned_hypergraph.h:707-809)
  * kept up to date by lpgpu_session_apply_moves with the transition rules of
@@ -356,15 +377,22 @@ LPGPU_API void lpgpu_host_free(void* p);
 /* Block weights c(V_b), km1 and cut of a partition, computed from device
  * buffers the caller already holds, without allocating any device memory.
  * This entry point has no counterpart in the reference; it exists for callers
- * that cannot let a library allocate: code running while a CUDA graph is
- * being captured (cudaMalloc/cudaFree synchronize and cannot be captured),
- * runtimes that own every byte of device memory through their own pool, and
- * latency-bound loops that must not block in the allocator.
+ * that cannot let a library allocate: runtimes that own every byte of device
+ * memory through their own pool or memory plan (a framework's caching
+ * allocator that has reserved the device, a server with a fixed budget), and
+ * latency-bound loops that must not block or fail in cudaMalloc, which can
+ * synchronize the device.
  *
  *   - All array arguments are device pointers: net_offsets (int64, m+1),
  *     pins (int32), vertex_weights / net_weights (int32, NULL = unit),
  *     partition (int32, n) and the outputs block_weights (int64, k), km1 and
- *     cut (one int64 each). Block ids outside [0, k) are ignored.
+ *     cut (one int64 each).
+ *   - The inputs are not validated the way lpgpu_session_upload validates
+ *     them: net_offsets must start at 0, be non-decreasing and end at the
+ *     number of entries of `pins`. Pins outside [0, n) and block ids outside
+ *     [0, k) are skipped (the sums are then not meaningful), weights are
+ *     summed as given (negative ones included), and nets with m > 0 but
+ *     n == 0 are rejected with LPGPU_ERR_INVALID_ARG.
  *   - k must be in [1, LPGPU_MAX_K]; larger k is rejected with
  *     LPGPU_ERR_INVALID_ARG. The cross-block accumulators live in one fixed
  *     file-scope device array of LPGPU_MAX_K + 2 64-bit words (8 KB), which

@@ -96,7 +96,17 @@ enum ValidateCode : int {
 };
 
 // Per-round statistics slots (lpgpu_round_stats order).
-enum Stat : int { kStActive = 0, kStPins, kStCands, kStMoved, kStReverted, kStDelta, kStats = 8 };
+enum Stat : int {
+  kStActive = 0,
+  kStPins,
+  kStCands,
+  kStMoved,
+  kStReverted,
+  kStDelta,
+  kStMovedPins,  // incidences of the moves k_commit applied (before reverts and rollbacks)
+  kStToggles,    // Λ bits k_commit changed
+  kStats = 8
+};
 
 // Device pointers of the round kernels.
 struct RoundCtx {
@@ -277,6 +287,12 @@ cudaError_t launch_expand_nets(const Launch& L, const RoundCtx& c, int S, PhaseT
 // rb_score: n-entry scratch; rb: 5k + 1 int64 scratch.
 cudaError_t launch_rebalance_round(const Launch& L, const RoundCtx& c, int round, int32_t* rb_to,
                                    int32_t* rb_score, int64_t* rb);
+// Empty-block repair candidates of block `blk` on a single-instance session:
+// the (at most k) vertices the reference's bounded heap keeps, as (vertex,
+// gain, block, weight) records in `out`; scratch[0] receives their number.
+// keys / ws: n-entry scratch; scratch: 2 int64.
+cudaError_t launch_repair_candidates(const Launch& L, const RoundCtx& c, int blk, uint64_t* keys, int32_t* ws,
+                                     int4* out, int64_t* scratch);
 
 // Optional per-phase CUDA-event timing.
 struct PhaseTimer {

@@ -2346,7 +2346,7 @@ __device__ __forceinline__ int flat_find(const FlatSmem& f, int n, int x) {
 // 0 and +w(e) when Φ(e, t) reaches 1; a[q] is each incidence's part.
 template <int Q>
 __device__ __forceinline__ void commit_group(const RoundCtx& c, const bool (&h)[Q], const int64_t (&e)[Q],
-                                             const int (&f)[Q], const int (&t)[Q], int (&a)[Q]) {
+                                             const int (&f)[Q], const int (&t)[Q], int (&a)[Q], int& toggles) {
   const int W = c.W;
   const int64_t k = c.kmax;
   int of[Q], ot[Q];
@@ -2365,9 +2365,9 @@ __device__ __forceinline__ void commit_group(const RoundCtx& c, const bool (&h)[
     const int we = c.unit_nets ? 1 : c.w_e[e[q]];
     uint32_t* rec = c.conn + e[q] * 2 * W;
     const uint32_t fb = 1u << (f[q] & 31), tb = 1u << (t[q] & 31);
-    if (of[q] == 1) { atomicXor(&rec[f[q] >> 5], fb); a[q] -= we; }
+    if (of[q] == 1) { atomicXor(&rec[f[q] >> 5], fb); a[q] -= we; ++toggles; }
     if (of[q] == 1 || of[q] == 2) atomicXor(&rec[W + (f[q] >> 5)], fb);
-    if (ot[q] == 0) { atomicXor(&rec[t[q] >> 5], tb); a[q] += we; }
+    if (ot[q] == 0) { atomicXor(&rec[t[q] >> 5], tb); a[q] += we; ++toggles; }
     if (ot[q] == 0 || ot[q] == 1) atomicXor(&rec[W + (t[q] >> 5)], tb);
   }
 }
@@ -2379,10 +2379,13 @@ __device__ __forceinline__ void commit_group(const RoundCtx& c, const bool (&h)[
 
 // Moves every incidence of the CTA's collected vertices from their `from` to
 // their `to` block (flat over the CTA). Returns this thread's summed delta;
-// per-vertex sums go to f.att when `per_item`.
-__device__ __forceinline__ int64_t flat_commit(const RoundCtx& c, FlatSmem& f, int n, int total, bool per_item) {
+// per-vertex sums go to f.att when `per_item`; *toggles counts this thread's
+// Λ bit changes.
+__device__ __forceinline__ int64_t flat_commit(const RoundCtx& c, FlatSmem& f, int n, int total, bool per_item,
+                                               int64_t* toggles = nullptr) {
   constexpr int Q = LPGPU_COMMIT_GROUP;
   int64_t att = 0;
+  int tg = 0;
   for (int x0 = threadIdx.x; x0 < total; x0 += Q * kFlatThreads) {
     bool h[Q];
     int64_t e[Q];
@@ -2397,13 +2400,14 @@ __device__ __forceinline__ int64_t flat_commit(const RoundCtx& c, FlatSmem& f, i
       fr[q] = ft & 0xffff;
       to[q] = ft >> 16;
     }
-    commit_group<Q>(c, h, e, fr, to, a);
+    commit_group<Q>(c, h, e, fr, to, a, tg);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       att += a[q];
       if (per_item && a[q]) atomicAdd(&f.att[it[q]], a[q]);
     }
   }
+  if (toggles) *toggles += tg;
   return att;
 }
 
@@ -2423,7 +2427,7 @@ __global__ void __launch_bounds__(kFlatThreads) k_commit(RoundCtx c, int round, 
   for (int b = threadIdx.x; b < kdw; b += blockDim.x) s_dw[b] = 0;
   const int64_t beg = c.sub_off[sub], end = c.sub_off[sub + 1];
   constexpr int PER = kFlatItems / kFlatThreads;
-  int64_t att = 0, moved = 0;
+  int64_t att = 0, moved = 0, moved_pins = 0, toggles = 0;
   for (int64_t r0 = beg + (int64_t)blockIdx.x * kFlatItems; r0 < end; r0 += (int64_t)gridDim.x * kFlatItems) {
     if (threadIdx.x == 0) f.n = 0;
     __syncthreads();
@@ -2473,7 +2477,8 @@ __global__ void __launch_bounds__(kFlatThreads) k_commit(RoundCtx c, int round, 
     __syncthreads();
     const int n = f.n;
     const int total = flat_scan(f, n);
-    att += flat_commit(c, f, n, total, batched);
+    if (threadIdx.x == 0) moved_pins += total;
+    att += flat_commit(c, f, n, total, batched, &toggles);
     __syncthreads();
     if (batched)
       for (int i = threadIdx.x; i < n; i += blockDim.x)
@@ -2481,9 +2486,13 @@ __global__ void __launch_bounds__(kFlatThreads) k_commit(RoundCtx c, int round, 
   }
   att = block_sum_i64(att);
   moved = block_sum_i64(moved);
+  toggles = block_sum_i64(toggles);
   if (threadIdx.x == 0) {
+    int64_t* st = c.stats + (int64_t)round * kStats;
     atomicAdd(reinterpret_cast<ull*>(&c.scal[kDeltaSub]), (ull)att);
-    atomicAdd(reinterpret_cast<ull*>(&c.stats[(int64_t)round * kStats + kStMoved]), (ull)moved);
+    atomicAdd(reinterpret_cast<ull*>(&st[kStMoved]), (ull)moved);
+    if (moved_pins) atomicAdd(reinterpret_cast<ull*>(&st[kStMovedPins]), (ull)moved_pins);
+    if (toggles) atomicAdd(reinterpret_cast<ull*>(&st[kStToggles]), (ull)toggles);
   }
   __syncthreads();
   for (int b = threadIdx.x; b < kdw; b += blockDim.x)
@@ -2994,6 +3003,80 @@ __global__ void k_rb_emit(RoundCtx c, const int32_t* __restrict__ rb_to, const i
     c.rec[v] = r;
   }
   if (last_cta(&c.scal[kDone])) plan_to(c);
+}
+
+// ---- empty-block repair (Rebalancer::repairEmptyBlocks, rebalancer.cpp:169-269)
+//
+// For one empty block `blk`: every vertex u eligible for it (c(part(u)) >
+// w(u), w(u) <= L_max(blk)) gets its gain score(blk) - unremovable(u)
+// (rebalancer.cpp:190-201; score = Σ w(e) of incident nets with blk in Λ(e),
+// unremovable = Σ w(e) of incident nets with Φ(e, part(u)) > 1, read as
+// part(u) not in Λ1(e)) and the key (gain descending, vertex ascending) with
+// weight 1; ineligible vertices get key ~0 and weight 0. A radix selection
+// then finds the k-th smallest key: the keys up to it are the k vertices the
+// reference's bounded per-thread heap keeps (rebalancer.cpp:204-213).
+__global__ void k_repair_keys(RoundCtx c, int blk, uint64_t* __restrict__ keys, int32_t* __restrict__ ws) {
+  const int W = c.W;
+  const int64_t cap = c.lmax[blk];
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < c.n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int p = c.part[v];
+    const int64_t wv = c.w_v[v];
+    uint64_t key = ~0ull;
+    if (p != blk && c.bw[p] > wv && wv <= cap) {
+      int64_t score = 0, unremovable = 0;
+      for (int64_t j = c.vtx_off[v]; j < c.vtx_off[v + 1]; ++j) {
+        const int64_t e = c.inets[j];
+        const int we = c.w_e[e];
+        const uint32_t* rec = c.conn + e * 2 * W;
+        if ((rec[blk >> 5] >> (blk & 31)) & 1u) score += we;
+        if (!((rec[W + (p >> 5)] >> (p & 31)) & 1u)) unremovable += we;
+      }
+      const int32_t gain = (int32_t)(score - unremovable);
+      key = ((uint64_t)(~((uint32_t)gain ^ 0x80000000u)) << 32) | (uint32_t)v;
+    }
+    keys[v] = key;
+    ws[v] = key == ~0ull ? 0 : 1;
+  }
+}
+
+// One CTA: the k-th smallest key (budget k - 1 over unit weights), or ~0
+// when fewer than k vertices are eligible.
+__global__ void __launch_bounds__(kSelThreads) k_repair_select(const uint64_t* __restrict__ keys,
+                                                               const int32_t* __restrict__ ws, int64_t n, int k,
+                                                               uint64_t* thr) {
+  const uint64_t t = cta_radix_select(keys, ws, n, (int64_t)k - 1);
+  if (threadIdx.x == 0) *thr = t;
+}
+
+// The kept vertices (key <= threshold) as (vertex, gain, block, weight);
+// *count receives their number (at most k).
+__global__ void k_repair_collect(RoundCtx c, const uint64_t* __restrict__ keys, const uint64_t* __restrict__ thr,
+                                 int4* __restrict__ out, int64_t* count) {
+  const uint64_t t = *thr;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < c.n; v += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t key = keys[v];
+    if (key == ~0ull || key > t) continue;
+    const int32_t gain = (int32_t)((~(uint32_t)(key >> 32)) ^ 0x80000000u);
+    const ull slot = atomicAdd(reinterpret_cast<ull*>(count), 1ull);
+    out[slot] = make_int4((int)v, gain, c.part[v], c.w_v[v]);
+  }
+}
+
+cudaError_t launch_repair_candidates(const Launch& L, const RoundCtx& c, int blk, uint64_t* keys, int32_t* ws,
+                                     int4* out, int64_t* scratch) {
+  if (c.n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(int64_t) * 2, L.st);
+  if (e != cudaSuccess) return e;
+  const int g = grid_for(L, c.n, 256);
+  k_repair_keys<<<g, 256, 0, L.st>>>(c, blk, keys, ws);
+  LAUNCHED("k_repair_keys");
+  cudaFuncSetAttribute(k_repair_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
+  k_repair_select<<<1, kSelThreads, kSelSmem, L.st>>>(keys, ws, c.n, c.k,
+                                                      reinterpret_cast<uint64_t*>(scratch + 1));
+  LAUNCHED("k_repair_select");
+  k_repair_collect<<<g, 256, 0, L.st>>>(c, keys, reinterpret_cast<const uint64_t*>(scratch + 1), out, scratch);
+  LAUNCHED("k_repair_collect");
+  return cudaGetLastError();
 }
 
 cudaError_t launch_rebalance_round(const Launch& L, const RoundCtx& c, int round, int32_t* rb_to,

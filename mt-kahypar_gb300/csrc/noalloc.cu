@@ -1,13 +1,13 @@
 // Allocation-free partition metrics (lpgpu_partition_metrics_noalloc).
 //
-// Some callers cannot let a library allocate device memory: code that runs
-// while a CUDA graph is being captured (cudaMalloc / cudaFree synchronize the
-// device and are not capturable), runtimes that hand out every byte of device
-// memory from their own pool or budget, and real-time loops where an
-// allocation's latency or failure is not acceptable. This entry point serves
-// them: the caller passes device-resident inputs and outputs, and the only
-// other device memory it uses is the file-scope array below, a fixed 8 KB
-// that every GPU loading the library holds until the process exits.
+// Some callers cannot let a library allocate device memory: runtimes that
+// hand out every byte of device memory from their own pool or budget (a
+// framework's caching allocator that has reserved the device, or a serving
+// process with a fixed memory plan), and real-time loops where a cudaMalloc
+// may synchronize the device or fail at the wrong moment. This entry point
+// serves them: the caller passes device-resident inputs and outputs, and the
+// only other device memory it uses is the file-scope array below, a fixed
+// 8 KB that every GPU loading the library holds until the process exits.
 #include <algorithm>
 #include <mutex>
 #include <string>
@@ -65,7 +65,9 @@ __global__ void k_noalloc_block_weights(int64_t n, const int32_t* __restrict__ p
 }
 
 // λ(e) per net from a per-warp k-bit shared set, summed into km1 and cut.
-__global__ void k_noalloc_connectivity(int64_t m, const int64_t* __restrict__ net_off,
+// Pins outside [0, n) and nets with a negative first offset are skipped, so
+// a malformed CSR gives wrong sums instead of reads outside the partition.
+__global__ void k_noalloc_connectivity(int64_t n, int64_t m, const int64_t* __restrict__ net_off,
                                        const int32_t* __restrict__ pins, const int32_t* __restrict__ w_e,
                                        const int32_t* __restrict__ part, int k,
                                        unsigned long long* scratch) {
@@ -78,8 +80,11 @@ __global__ void k_noalloc_connectivity(int64_t m, const int64_t* __restrict__ ne
   long long km1 = 0, cut = 0;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < m; e += warps) {
-    for (int64_t i = net_off[e] + lane; i < net_off[e + 1]; i += 32) {
-      const int b = part[pins[i]];
+    const int64_t lo = net_off[e], hi = net_off[e + 1];
+    for (int64_t i = lo >= 0 ? lo + lane : hi; i < hi; i += 32) {
+      const int32_t p = pins[i];
+      if ((uint64_t)(int64_t)p >= (uint64_t)n) continue;
+      const int b = part[p];
       if (b >= 0 && b < k) atomicOr(&bits[b >> 5], 1u << (b & 31));
     }
     __syncwarp();
@@ -136,6 +141,10 @@ extern "C" lpgpu_status lpgpu_partition_metrics_noalloc(
     set_error("null device pointer");
     return LPGPU_ERR_INVALID_ARG;
   }
+  if (num_nets > 0 && num_vertices == 0) {
+    set_error("nets without vertices: every pin must name a vertex in [0, num_vertices)");
+    return LPGPU_ERR_INVALID_ARG;
+  }
   cudaGetLastError();
   unsigned long long* scratch = nullptr;
   cudaError_t e = scratch_for_current_device(&scratch);
@@ -149,14 +158,15 @@ extern "C" lpgpu_status lpgpu_partition_metrics_noalloc(
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   k_noalloc_clear<<<1, 1024, 0, st>>>(scratch, k + 2);
   if (num_vertices > 0) {
-    const int blocks = (int)std::min<int64_t>(1024, (num_vertices + 255) / 256);
+    const int blocks = (int)std::min<int64_t>(1024, num_vertices / 256 + 1);
     k_noalloc_block_weights<<<blocks, 256, sizeof(unsigned long long) * k, st>>>(
         num_vertices, partition, vertex_weights, k, scratch);
   }
   if (num_nets > 0) {
-    const int blocks = (int)std::min<int64_t>(2048, (num_nets * 32 + 255) / 256);
+    // a warp per net, 8 warps per CTA, at most 2,048 CTAs striding over the nets
+    const int blocks = (int)std::min<int64_t>(2048, num_nets / 8 + 1);
     k_noalloc_connectivity<<<blocks, 256, sizeof(unsigned) * 8 * ((k + 31) / 32), st>>>(
-        num_nets, net_offsets, pins, net_weights, partition, k, scratch);
+        num_vertices, num_nets, net_offsets, pins, net_weights, partition, k, scratch);
   }
   k_noalloc_finish<<<(k + 255) / 256, 256, 0, st>>>(scratch, k, block_weights, km1, cut);
   e = cudaGetLastError();

@@ -1007,7 +1007,8 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
     const int64_t* x = &hs[r * kStats];
     if (x[kStActive] == 0) stopped = true;
     if (stopped) continue;
-    lpgpu_round_stats rs{x[kStActive], x[kStPins], x[kStCands], x[kStMoved], x[kStReverted], x[kStDelta]};
+    lpgpu_round_stats rs{x[kStActive], x[kStPins],  x[kStCands],     x[kStMoved],
+                         x[kStReverted], x[kStDelta], x[kStMovedPins], x[kStToggles]};
     s->last_stats.push_back(rs);
     ++executed;
     delta += rs.delta;
@@ -1327,6 +1328,82 @@ lpgpu_status lpgpu_session_restore_partition(lpgpu_session* s) {
   return LPGPU_OK;
 }
 
+// The moves of repairEmptyBlocks (rebalancer.cpp:169-269) on the current
+// state, in empty-block order: per empty block the device keeps the k
+// eligible vertices of highest gain (lowest id on ties), and the first of
+// them in (gain, weight of its block, id) descending order that no earlier
+// block took is the block's move. Block weights are read into *bw_out.
+struct RepairMove {
+  int32_t v, from, to, gain, w;
+};
+static lpgpu_status repair_moves(lpgpu_session* s, std::vector<RepairMove>* moves, std::vector<int64_t>* bw_out) {
+  const int k = s->k;
+  cudaStream_t st = s->st;
+  std::vector<int64_t>& bw = *bw_out;
+  bw.assign(k, 0);
+  CK(cudaMemcpyAsync(bw.data(), s->bw.p, sizeof(int64_t) * k, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  moves->clear();
+  std::vector<int> empty;
+  for (int b = 0; b < k; ++b)
+    if (bw[b] == 0) empty.push_back(b);
+  if (empty.empty() || s->n == 0) return LPGPU_OK;
+  TmpBuf<int4> cand(s->mem);
+  TmpBuf<int64_t> scratch(s->mem);
+  CK(cand.alloc(k));
+  CK(scratch.alloc(2));
+  RoundCtx c = s->ctx();
+  std::vector<int4> h(k);
+  std::vector<uint8_t> used(s->n, 0);
+  for (int blk : empty) {
+    CK(launch_repair_candidates(s->launch(), c, blk, s->seg_key.p, s->seg_w.p, cand.p(), scratch.p()));
+    int64_t count = 0;
+    CK(cudaMemcpyAsync(&count, scratch.p(), sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (count > k) return cuda_fail(cudaErrorUnknown, "repair candidate count above k");
+    if (count == 0) continue;
+    CK(cudaMemcpyAsync(h.data(), cand.p(), sizeof(int4) * count, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::sort(h.begin(), h.begin() + count, [&](const int4& a, const int4& b) {
+      if (a.y != b.y) return a.y > b.y;
+      if (bw[a.z] != bw[b.z]) return bw[a.z] > bw[b.z];
+      return a.x > b.x;
+    });
+    for (int64_t i = 0; i < count; ++i) {
+      if (used[h[i].x]) continue;
+      used[h[i].x] = 1;
+      moves->push_back(RepairMove{h[i].x, h[i].z, blk, h[i].y, h[i].w});
+      break;
+    }
+  }
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_repair_empty_blocks(lpgpu_session* s, int32_t* vertices, int32_t* from, int32_t* to,
+                                               int32_t* gain, int32_t* count) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  if (s->batched) {
+    set_error("this call needs a single-instance session");
+    return LPGPU_ERR_STATE;
+  }
+  if (!count) return invalid("null count pointer");
+  DeviceGuard g(s->device);
+  std::vector<RepairMove> mv;
+  std::vector<int64_t> bw;
+  ps = repair_moves(s, &mv, &bw);
+  if (ps != LPGPU_OK) return ps;
+  if (!mv.empty() && (!vertices || !from || !to || !gain)) return invalid("null move output array");
+  for (size_t i = 0; i < mv.size(); ++i) {
+    vertices[i] = mv[i].v;
+    from[i] = mv[i].from;
+    to[i] = mv[i].to;
+    gain[i] = mv[i].gain;
+  }
+  *count = (int32_t)mv.size();
+  return LPGPU_OK;
+}
+
 lpgpu_status lpgpu_session_rebalance(lpgpu_session* s, int32_t max_rounds, lpgpu_result* result) {
   lpgpu_status ps = need_part(s);
   if (ps != LPGPU_OK) return ps;
@@ -1355,6 +1432,54 @@ lpgpu_status lpgpu_session_rebalance(lpgpu_session* s, int32_t max_rounds, lpgpu
   c.rollback = 0;
   s->last_stats.clear();
   int64_t delta = 0, moves = 0, pins = 0;
+  {
+    // rebalancer.cpp:59-62: on an imbalanced partition the moves of
+    // repairEmptyBlocks come first, each applied as moveVertex does
+    // (rebalancer.h:84-103: the target stays within L_max, the source keeps
+    // weight > 0); they form the first statistics record
+    CK(cudaMemcpyAsync(hb.data(), s->bw.p, sizeof(int64_t) * k, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    bool over = false, empty = false;
+    for (int b = 0; b < k; ++b) {
+      over = over || hb[b] > hl[b];
+      empty = empty || hb[b] == 0;
+    }
+    if (over && empty) {
+      std::vector<RepairMove> mv;
+      std::vector<int64_t> bwr;
+      ps = repair_moves(s, &mv, &bwr);
+      if (ps != LPGPU_OK) return ps;
+      std::vector<int32_t> av, af, at;
+      for (const RepairMove& x : mv) {
+        if (bwr[x.to] + x.w <= hl[x.to] && bwr[x.from] - x.w > 0) {
+          bwr[x.to] += x.w;
+          bwr[x.from] -= x.w;
+          av.push_back(x.v);
+          af.push_back(x.from);
+          at.push_back(x.to);
+        }
+      }
+      int64_t d = 0;
+      if (!av.empty()) {
+        const size_t cnt = av.size();
+        TmpBuf<int32_t> dv(s->mem), df(s->mem), dt(s->mem);
+        CK(dv.alloc(cnt));
+        CK(df.alloc(cnt));
+        CK(dt.alloc(cnt));
+        CK(cudaMemcpyAsync(dv.p(), av.data(), sizeof(int32_t) * cnt, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(df.p(), af.data(), sizeof(int32_t) * cnt, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dt.p(), at.data(), sizeof(int32_t) * cnt, cudaMemcpyHostToDevice, st));
+        CK(launch_apply_moves(s->launch(), c, (int64_t)cnt, dv.p(), df.p(), dt.p(), GainCache{nullptr, nullptr, nullptr}));
+        CK(cudaMemcpyAsync(&d, s->scal.p + kApplyDelta, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+      }
+      lpgpu_round_stats rs{s->n, s->P, (int64_t)mv.size(), (int64_t)av.size(), 0, d, 0, 0};
+      s->last_stats.push_back(rs);
+      delta += d;
+      moves += rs.moved;
+      pins += rs.pins;
+    }
+  }
   for (int r = 0; r < R; ++r) {
     CK(cudaMemcpyAsync(hb.data(), s->bw.p, sizeof(int64_t) * k, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -1368,7 +1493,8 @@ lpgpu_status lpgpu_session_rebalance(lpgpu_session* s, int32_t max_rounds, lpgpu
     CK(cudaMemcpyAsync(hs.data(), s->stats.p + (int64_t)r * kStats, sizeof(int64_t) * kStats,
                        cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    lpgpu_round_stats rs{hs[kStActive], hs[kStPins], hs[kStCands], hs[kStMoved], hs[kStReverted], hs[kStDelta]};
+    lpgpu_round_stats rs{hs[kStActive],   hs[kStPins],  hs[kStCands],     hs[kStMoved],
+                         hs[kStReverted], hs[kStDelta], hs[kStMovedPins], hs[kStToggles]};
     s->last_stats.push_back(rs);
     delta += rs.delta;
     moves += rs.moved;

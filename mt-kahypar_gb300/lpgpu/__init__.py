@@ -50,7 +50,8 @@ class Result(ctypes.Structure):
 class RoundStats(ctypes.Structure):
     _fields_ = [("active", ctypes.c_int64), ("pins", ctypes.c_int64),
                 ("candidates", ctypes.c_int64), ("moved", ctypes.c_int64),
-                ("reverted", ctypes.c_int64), ("delta", ctypes.c_int64)]
+                ("reverted", ctypes.c_int64), ("delta", ctypes.c_int64),
+                ("moved_pins", ctypes.c_int64), ("toggles", ctypes.c_int64)]
 
 
 class PhaseTime(ctypes.Structure):
@@ -82,6 +83,7 @@ SYMBOLS = [
     "lpgpu_session_set_partition_instances", "lpgpu_session_get_partition_instances", "lpgpu_read_hgr",
     "lpgpu_free", "lpgpu_read_partition", "lpgpu_write_partition", "lpgpu_session_init_gain_cache",
     "lpgpu_session_drop_gain_cache", "lpgpu_session_project_partition", "lpgpu_session_rebalance",
+    "lpgpu_session_repair_empty_blocks",
 ]
 
 
@@ -331,6 +333,15 @@ class Session:
         r = Result()
         _check(lib().lpgpu_session_rebalance(self._h, ctypes.c_int32(max_rounds), ctypes.byref(r)))
         return r
+
+    def repair_empty_blocks(self):
+        """Moves of repairEmptyBlocks (lpgpu_session_repair_empty_blocks), not applied:
+        a list of (vertex, from, to, gain) in empty-block order."""
+        k = max(1, self.k)
+        out = [np.zeros(k, np.int32) for _ in range(4)]
+        cnt = ctypes.c_int32()
+        _check(lib().lpgpu_session_repair_empty_blocks(self._h, *[_p(a, I32P) for a in out], ctypes.byref(cnt)))
+        return [tuple(int(a[i]) for a in out) for i in range(cnt.value)]
 
     def project_partition(self, coarse, fine_to_coarse):
         """This (fine) session's partition from `coarse`'s through the vertex map."""

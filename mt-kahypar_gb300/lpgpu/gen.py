@@ -243,6 +243,21 @@ def rownet(seed=0, n=4194304, k=128, eps=0.03, rounds=10, target_nnz=None) -> In
     return Instance("rownet", hg, k, eps, part, rounds)
 
 
+def seed_partition(inst: Instance, seed: int) -> np.ndarray:
+    """The initial partition of a plain workload drawn with another seed (the
+    workload's own rule: random balanced for plain_small, weight-balanced greedy
+    for plain_large, contiguous blocks with 10 % reassigned for rownet), for
+    runs over several seeds on one hypergraph."""
+    hg = inst.hg
+    if inst.name == "plain_small":
+        return random_balanced_partition(hg.n, inst.k, np.random.default_rng([seed, 2]))
+    if inst.name == "plain_large":
+        return greedy_weight_partition(hg.w_v, inst.k, np.random.default_rng([seed, 12]))
+    if inst.name == "rownet":
+        return contiguous_perturbed_partition(hg.n, inst.k, 0.10, np.random.default_rng([seed, 22]))
+    raise ValueError(f"no seed partition rule for {inst.name}")
+
+
 def batch_instance(seed, idx, lo=1024, hi=65536, ks=(2, 4, 8, 16), eps=0.03, rounds=5,
                    incidence=True) -> Instance:
     rng = np.random.default_rng([seed, 31, idx])

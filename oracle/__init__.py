@@ -124,11 +124,22 @@ def lp_sync(hg, k, lmax, part, perfect=None, **cfg):
 def rebalance(hg, k, lmax, part, max_rounds=16):
     """Deterministic rebalancer (orc_rebalance): partition and per-round stats."""
     p = np.array(part, np.int32, copy=True)
-    stats = (RoundStats * max(1, max_rounds))()
+    stats = (RoundStats * (max_rounds + 1))()
     lm = np.ascontiguousarray(lmax, np.int64)
     r = lib().orc_rebalance(*_hg_args(hg), ctypes.c_int32(k), _p(lm, I64P), _p(p, I32P),
                             ctypes.c_int32(max_rounds), stats)
     return p, [_stat_dict(stats[i]) for i in range(r)]
+
+
+def repair_empty_blocks(hg, k, lmax, part):
+    """Moves of repairEmptyBlocks (orc_repair_empty_blocks): (vertex, from, to, gain) per
+    empty block that received one, in block order; gain is km1Gain (positive = better)."""
+    out = [np.zeros(max(1, k), np.int32) for _ in range(4)]
+    lm = np.ascontiguousarray(lmax, np.int64)
+    c = lib().orc_repair_empty_blocks(*_hg_args(hg), ctypes.c_int32(k), _p(lm, I64P),
+                                      _p(np.ascontiguousarray(part, np.int32), I32P),
+                                      *[_p(a, I32P) for a in out])
+    return [tuple(int(a[i]) for a in out) for i in range(c)]
 
 
 def lp_async(hg, k, lmax, perfect, part, **cfg):

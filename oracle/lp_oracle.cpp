@@ -151,6 +151,25 @@ struct State {
     return internal - pen;
   }
 
+  // scores[b] = objective delta of moving v from `cur` to b, for every block
+  // (no balance check); the all-blocks form of move_score.
+  void move_scores(int64_t v, int cur, std::vector<int64_t>& scores) const {
+    int64_t internal = 0;
+    for (int64_t i = hg->vtx_off[v]; i < hg->vtx_off[v + 1]; ++i) {
+      const int64_t e = hg->inets[i];
+      const int64_t we = hg->w_e[e];
+      if (phi[e * k + cur] > 1) internal += we;
+      for (int w = 0; w < W; ++w) {
+        uint32_t bits = conn[e * W + w];
+        while (bits) {
+          scores[w * 32 + __builtin_ctz(bits)] -= we;
+          bits &= bits - 1;
+        }
+      }
+    }
+    for (int b = 0; b < k; ++b) scores[b] += internal;
+  }
+
   // changeNodePart body after the weight check (partitioned_hypergraph.h:553-557)
   // with updatePinCountOfHyperedge (1133-1143) and km1Delta (hypergraph_common.h:133-140).
   int64_t apply_move(int64_t v, int from, int to) {
@@ -187,6 +206,33 @@ Hg make_hg(int64_t n, int64_t m, const int64_t* net_off, const int32_t* pins,
   return Hg{n, m, net_off, pins, vtx_off, inets, w_v, w_e};
 }
 
+// body(i, scratch) for i in [0, count) on `threads` std::threads (contiguous
+// chunks handed out dynamically); each thread owns a zeroed int64 scratch
+// vector of `scratch_len` entries that body must leave zeroed.
+template <typename Body>
+void parallel_for(int threads, int64_t count, Body body, int scratch_len) {
+  const int64_t chunk = 1024;
+  if (threads <= 1 || count <= chunk) {
+    std::vector<int64_t> scratch(scratch_len, 0);
+    for (int64_t i = 0; i < count; ++i) body(i, scratch);
+    return;
+  }
+  std::atomic<int64_t> next{0};
+  auto worker = [&]() {
+    std::vector<int64_t> scratch(scratch_len, 0);
+    for (;;) {
+      const int64_t b = next.fetch_add(chunk);
+      if (b >= count) break;
+      const int64_t e = std::min(count, b + chunk);
+      for (int64_t i = b; i < e; ++i) body(i, scratch);
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < threads; ++t) pool.emplace_back(worker);
+  worker();
+  for (auto& th : pool) th.join();
+}
+
 inline uint32_t mix32(uint32_t x) {
   x ^= x >> 16;
   x *= 0x7feb352dU;
@@ -218,7 +264,7 @@ typedef struct {
   int32_t subrounds;             // sub-rounds per round (>= 1)
   int32_t revert;                // 1: undo moves that turned out harmful
   int32_t rollback;              // 1: undo a whole sub-round whose delta is positive
-  int32_t threads;               // async mode only
+  int32_t threads;               // worker threads (async mode; sync mode's per-vertex sweep)
   int32_t zero_gain;             // 1: deterministic zero-gain rebalancing moves (sync mode)
   int64_t seed;                  // async mode only
 } orc_lp_cfg;
@@ -339,7 +385,6 @@ int32_t orc_lp_sync(int64_t n, int64_t m, const int64_t* net_off, const int32_t*
   Hg hg = make_hg(n, m, net_off, pins, vtx_off, inets, w_v, w_e);
   State s{&hg, k, words_for(k), {}, {}, {}, {}};
   s.init(part_inout);
-  std::vector<int64_t> scores(k, 0);
   // initializeActiveNodes (label_propagation_refiner.cpp:194-233): all vertices
   // with rebalancing, else the border vertices
   std::vector<int32_t> active;
@@ -348,6 +393,7 @@ int32_t orc_lp_sync(int64_t n, int64_t m, const int64_t* net_off, const int32_t*
   std::vector<uint8_t> next_flag(n, 0);
   const int S = std::max(1, cfg->subrounds);
   const int64_t T = cfg->activation_threshold <= 0 ? INT64_MAX : cfg->activation_threshold;
+  const int threads = std::max(1, cfg->threads);
 
   struct Cand { int32_t v, from, to; int64_t gain; int64_t w; };
   int32_t r = 0;
@@ -357,28 +403,45 @@ int32_t orc_lp_sync(int64_t n, int64_t m, const int64_t* net_off, const int32_t*
     orc_round_stats st{};
     std::fill(next_flag.begin(), next_flag.end(), 0);
     for (int sub = 0; sub < S; ++sub) {
-      std::vector<Cand> cands;
+      // the sub-round's vertices in active-list order, then their moves on the
+      // snapshot (a pure function of the state, so worker threads give the
+      // same candidates as one thread)
+      std::vector<int32_t> group;
       for (int32_t v : active) {
         if (S > 1 && (int)(mix32((uint32_t)(v >> 5) ^ (0x9E3779B9u * (uint32_t)(r + 1))) % S) != sub)
           continue;
+        group.push_back(v);
         st.active++;
         st.pins += vtx_off[v + 1] - vtx_off[v];
-        if (!s.is_border(v)) continue;
+      }
+      std::vector<Cand> found(group.size());
+      std::vector<uint8_t> has(group.size(), 0);
+      parallel_for(threads, (int64_t)group.size(), [&](int64_t i, std::vector<int64_t>& scores) {
+        const int32_t v = group[i];
+        if (!s.is_border(v)) return;
         int64_t g = 0;
+        const int from = s.part[v];
         int to = s.best_move(v, s.bw.data(), lmax, scores, &g);
-        if (to == s.part[v] && cfg->zero_gain && perfect) {
+        if (to == from && cfg->zero_gain && perfect) {
           // lowest-id feasible block with score 0 under the rebalancing rule of
           // label_propagation_refiner.h:88-95
-          const int from = s.part[v];
+          s.move_scores(v, from, scores);
           for (int b = 0; b < k; ++b) {
             if (b == from || s.bw[b] + w_v[v] > lmax[b]) continue;
-            if (s.move_score(v, from, b) != 0) continue;
+            if (scores[b] != 0) continue;
             if (s.bw[from] - 1 > s.bw[b] + 1 && s.bw[b] < perfect[b]) { to = b; g = 0; }
             break;
           }
+          std::fill(scores.begin(), scores.end(), 0);
         }
-        if (to != s.part[v] && g <= 0) cands.push_back({v, s.part[v], to, g, w_v[v]});
-      }
+        if (to != from && g <= 0) {
+          found[i] = {v, from, to, g, w_v[v]};
+          has[i] = 1;
+        }
+      }, k);
+      std::vector<Cand> cands;
+      for (size_t i = 0; i < group.size(); ++i)
+        if (has[i]) cands.push_back(found[i]);
       st.candidates += (int64_t)cands.size();
       auto key_less = [](const Cand& a, const Cand& b) {
         return a.gain != b.gain ? a.gain < b.gain : a.v < b.v;
@@ -420,8 +483,9 @@ int32_t orc_lp_sync(int64_t n, int64_t m, const int64_t* net_off, const int32_t*
       }
       if (cfg->revert && !moved.empty()) {
         std::vector<uint8_t> back(moved.size(), 0);
-        for (size_t i = 0; i < moved.size(); ++i)
+        parallel_for(threads, (int64_t)moved.size(), [&](int64_t i, std::vector<int64_t>&) {
           back[i] = s.move_score(moved[i].v, moved[i].to, moved[i].from) < 0;
+        }, 0);
         std::vector<Cand> kept;
         for (size_t i = 0; i < moved.size(); ++i) {
           if (back[i]) {
@@ -460,10 +524,109 @@ int32_t orc_lp_sync(int64_t n, int64_t m, const int64_t* net_off, const int32_t*
   return r;
 }
 
+}  // extern "C"
+
+namespace {
+
+struct RepairMove {
+  int32_t v, from, to, gain;
+};
+
+// Rebalancer::repairEmptyBlocks (rebalancing/rebalancer.cpp:169-269) as one
+// worker thread computes it. For every empty block i (c(i) = 0), ascending:
+//   * a vertex u in block p = part(u) is eligible when c(p) > w(u) and
+//     w(u) <= L_max(i); its gain (positive = better, km1Gain) is
+//     score(i) - unremovable(u), with score(i) = Σ w(e) over the incident nets
+//     whose connectivity set holds i and unremovable(u) = Σ w(e) over the
+//     incident nets with Φ(e, p) > 1 (rebalancer.cpp:190-201);
+//   * the worker's bounded heap keeps the k eligible vertices of highest gain,
+//     the earlier (lower) id on ties, as the heap of rebalancer.cpp:204-213
+//     does for vertices scanned in id order;
+//   * among them, ordered by gain, then c(part(u)), then u, all descending
+//     (prefer_highest_gain, rebalancer.cpp:228-232), the first vertex not yet
+//     chosen for an earlier block is the block's move (rebalancer.cpp:242-254).
+// Block weights are those of the call (no move is applied here). A block
+// without an eligible vertex stays empty: the reference's outer loop would
+// repeat the same scan forever in that case, so one pass is the whole result.
+std::vector<RepairMove> repair_empty_blocks(const State& s, const int64_t* lmax) {
+  const Hg& hg = *s.hg;
+  const int k = s.k;
+  std::vector<RepairMove> moves;
+  std::vector<uint8_t> used(hg.n, 0);
+  std::vector<int64_t> unremovable(hg.n, 0);
+  for (int64_t v = 0; v < hg.n; ++v)
+    for (int64_t i = hg.vtx_off[v]; i < hg.vtx_off[v + 1]; ++i) {
+      const int64_t e = hg.inets[i];
+      if (s.phi[e * k + s.part[v]] > 1) unremovable[v] += hg.w_e[e];
+    }
+  struct C { int64_t gain; int32_t v; };
+  for (int i = 0; i < k; ++i) {
+    if (s.bw[i] != 0) continue;
+    std::vector<C> top;
+    for (int64_t v = 0; v < hg.n; ++v) {
+      const int p = s.part[v];
+      if (p == i || s.bw[p] <= hg.w_v[v] || hg.w_v[v] > lmax[i]) continue;
+      int64_t score = 0;
+      for (int64_t j = hg.vtx_off[v]; j < hg.vtx_off[v + 1]; ++j) {
+        const int64_t e = hg.inets[j];
+        if (bit_of(s.conn.data(), s.W, e, i)) score += hg.w_e[e];
+      }
+      top.push_back({score - unremovable[v], (int32_t)v});
+    }
+    auto heap_order = [](const C& a, const C& b) { return a.gain != b.gain ? a.gain > b.gain : a.v < b.v; };
+    if ((int64_t)top.size() > k) {
+      std::nth_element(top.begin(), top.begin() + k, top.end(), heap_order);
+      top.resize(k);
+    }
+    std::sort(top.begin(), top.end(), [&](const C& a, const C& b) {
+      const int64_t wa = s.bw[s.part[a.v]], wb = s.bw[s.part[b.v]];
+      if (a.gain != b.gain) return a.gain > b.gain;
+      if (wa != wb) return wa > wb;
+      return a.v > b.v;
+    });
+    for (const C& c : top) {
+      if (used[c.v]) continue;
+      used[c.v] = 1;
+      moves.push_back({c.v, s.part[c.v], i, (int32_t)c.gain});
+      break;
+    }
+  }
+  return moves;
+}
+
+}  // namespace
+
+extern "C" {
+
+// The moves of repairEmptyBlocks on `part_in` (see repair_empty_blocks), in
+// empty-block order; returns their number (at most k), written to
+// vertices/from/to/gain (each k entries).
+int32_t orc_repair_empty_blocks(int64_t n, int64_t m, const int64_t* net_off, const int32_t* pins,
+                                const int64_t* vtx_off, const int32_t* inets, const int32_t* w_v,
+                                const int32_t* w_e, int32_t k, const int64_t* lmax, const int32_t* part_in,
+                                int32_t* vertices, int32_t* from, int32_t* to, int32_t* gain) {
+  Hg hg = make_hg(n, m, net_off, pins, vtx_off, inets, w_v, w_e);
+  State s{&hg, k, words_for(k), {}, {}, {}, {}};
+  s.init(part_in);
+  const std::vector<RepairMove> mv = repair_empty_blocks(s, lmax);
+  for (size_t i = 0; i < mv.size(); ++i) {
+    vertices[i] = mv[i].v;
+    from[i] = mv[i].from;
+    to[i] = mv[i].to;
+    gain[i] = mv[i].gain;
+  }
+  return (int32_t)mv.size();
+}
+
 // Deterministic rebalancer (the device's lpgpu_session_rebalance), a
 // synchronous restatement of Rebalancer::rebalance (rebalancing/rebalancer.cpp:34-171,
 // whose thread-local priority queues make the reference order-dependent).
-// Per round, while some block is above its max weight:
+// If some block is above its max weight and some block is empty, the moves of
+// repairEmptyBlocks are applied first, in their order, each as moveVertex
+// does (rebalancer.h:84-103: only if the target stays within L_max and the
+// source keeps weight > 0); they form a first statistics record (active = n,
+// pins = P, candidates = moves proposed, moved = moves applied).
+// Then per round, while some block is above its max weight:
 //   * every border vertex of an overloaded block computes its Km1Policy best
 //     move with rebalance = true (gain_policy.h:108-167): the feasible block
 //     (c(b) + w(v) <= L_max(b), b != from) of minimum score, any sign, lowest id
@@ -478,7 +641,8 @@ int32_t orc_lp_sync(int64_t n, int64_t m, const int64_t* net_off, const int32_t*
 //     longest prefix that leaves it non-empty; they are committed with km1Delta
 //     attribution.
 // Stops when no block is overloaded, after max_rounds, or when a round moves
-// nothing. Returns the rounds executed; stats[r] gets candidates, moved, delta.
+// nothing. Returns the statistics records written (the repair record, if any,
+// plus the rounds executed; `stats` holds max_rounds + 1 records).
 int32_t orc_rebalance(int64_t n, int64_t m, const int64_t* net_off, const int32_t* pins,
                       const int64_t* vtx_off, const int32_t* inets, const int32_t* w_v,
                       const int32_t* w_e, int32_t k, const int64_t* lmax, int32_t* part_inout,
@@ -489,8 +653,33 @@ int32_t orc_rebalance(int64_t n, int64_t m, const int64_t* net_off, const int32_
   std::vector<int64_t> scores(k, 0);
   struct Cand { int32_t v, from, to; int64_t gain; int64_t w; };
   auto key_less = [](const Cand& a, const Cand& b) { return a.gain != b.gain ? a.gain < b.gain : a.v < b.v; };
-  int32_t r = 0;
-  for (; r < max_rounds; ++r) {
+  int32_t rec = 0;  // statistics records written
+  {
+    bool over = false, empty = false;
+    for (int b = 0; b < k; ++b) {
+      over = over || s.bw[b] > lmax[b];
+      empty = empty || s.bw[b] == 0;
+    }
+    if (over && empty) {
+      // rebalancer.cpp:59-62: repairEmptyBlocks, then moveVertex per move
+      orc_round_stats st{};
+      st.active = n;
+      st.pins = vtx_off[n];
+      const std::vector<RepairMove> mv = repair_empty_blocks(s, lmax);
+      st.candidates = (int64_t)mv.size();
+      for (const RepairMove& x : mv) {
+        const int64_t wv = w_v[x.v];
+        if (s.bw[x.to] + wv <= lmax[x.to] && s.bw[x.from] - wv > 0) {
+          st.delta += s.apply_move(x.v, x.from, x.to);
+          st.moved++;
+        }
+      }
+      st.km1_after = s.km1();
+      if (stats) stats[rec] = st;
+      ++rec;
+    }
+  }
+  for (int32_t r = 0; r < max_rounds; ++r) {
     bool over = false;
     for (int b = 0; b < k; ++b) over = over || s.bw[b] > lmax[b];
     if (!over) break;
@@ -569,14 +758,12 @@ int32_t orc_rebalance(int64_t n, int64_t m, const int64_t* net_off, const int32_
       st.moved++;
     }
     st.km1_after = s.km1();
-    if (stats) stats[r] = st;
-    if (st.moved == 0) {
-      ++r;
-      break;
-    }
+    if (stats) stats[rec] = st;
+    ++rec;
+    if (st.moved == 0) break;
   }
   std::memcpy(part_inout, s.part.data(), sizeof(int32_t) * n);
-  return r;
+  return rec;
 }
 
 // Reference-style asynchronous LP (label_propagation_refiner.{h,cpp}):

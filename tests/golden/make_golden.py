@@ -9,7 +9,8 @@ test suite needs no access to the reference tree. For every fixture the
 CPU oracle's outputs (Φ, Λ, km1, best moves, gain cache, a synchronous LP run)
 are stored beside the input as golden vectors.
 
-Run from the repository root:  python tests/golden/make_golden.py [reference_root]
+Run from the repository root:  python tests/golden/make_golden.py <reference_root>
+(the Mt-KaHyPar source tree; MTK_REFERENCE_ROOT is read when no argument is given)
 """
 import os
 import sys
@@ -85,4 +86,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MTK_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py <reference_root>  (or set MTK_REFERENCE_ROOT)")
+    main(root)

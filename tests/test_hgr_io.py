@@ -43,11 +43,11 @@ def test_round_trip_of_golden_hypergraphs(lp, tmp_path, name, typ):
 
 def test_reference_instances_match_fixtures(lp):
     """The reader gives the fixtures' CSR for the reference's own test instances
-    (when the reference tree is present)."""
-    root = os.environ.get("MTK_REFERENCE_ROOT", "/root/reference")
-    inst = os.path.join(root, "tests", "instances")
-    if not os.path.isdir(inst):
-        pytest.skip("reference test instances not present")
+    (when MTK_REFERENCE_ROOT names a Mt-KaHyPar source tree)."""
+    root = os.environ.get("MTK_REFERENCE_ROOT")
+    inst = os.path.join(root, "tests", "instances") if root else None
+    if not inst or not os.path.isdir(inst):
+        pytest.skip("MTK_REFERENCE_ROOT does not name a tree with tests/instances")
     for name in GOLDEN:
         hg, _ = load_golden(name)
         got, _ = lp.read_hgr(os.path.join(inst, name + ".hgr"))

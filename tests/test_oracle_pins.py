@@ -221,3 +221,56 @@ def test_lp_refiner_properties_ibm01(orc, k, mode):
     assert km1_1 <= km1_0
     assert (bw1 / perfect).max() - 1.0 <= 0.25 + 0.05
     assert (bw1 <= lmax).all()
+
+
+def _rebalance_test_partition(hg, k):
+    """rebalance_test.cc:56-73: contracted_ibm01, k = 8, the first n / 4
+    vertices in block 0, the next n / 4 in block 1, ...; blocks 4..7 empty."""
+    per = hg.n // (k - 4)
+    assert hg.n % (k - 4) == 0
+    return (np.arange(hg.n) // per).astype(np.int32)
+
+
+def test_repair_empty_blocks_finds_moves_ibm01(orc):
+    """rebalance_test.cc:56-103 (FindsMoves): four moves, one per empty block;
+    each gain equals km1Gain recomputed from the state (positive = better); a
+    zero gain only for a vertex whose nets all hold it as their one pin in its
+    block; sources are the filled blocks, targets the empty ones; after the
+    moves are applied no block is empty and repairEmptyBlocks finds nothing."""
+    from lpgpu import gen
+    hg, _ = load_golden("contracted_ibm01")
+    k = 8
+    perfect, lmax = gen.part_weights(int(hg.w_v.sum()), k, 0.03)
+    part = _rebalance_test_partition(hg, k)
+    phi, _, bw = orc.init_partition(hg, k, part)
+    benefit, penalty = orc.gain_cache(hg, k, part)
+    moves = orc.repair_empty_blocks(hg, k, lmax, part)
+    assert len(moves) == 4
+    for v, f, t, g in moves:
+        assert g == benefit[v] - penalty[v, t]  # km1Gain = moveFromBenefit - moveToPenalty
+        if g == 0:
+            assert all(phi[e, f] == 1 for e in hg.inets[hg.vtx_off[v]:hg.vtx_off[v + 1]])
+        assert f == part[v] and bw[t] == 0
+        assert t >= k - 4 and f < k - 4
+    assert len({v for v, _, _, _ in moves}) == 4
+    after = _apply(orc, hg, k, part, [(v, f, t) for v, f, t, _ in moves])
+    assert orc.repair_empty_blocks(hg, k, lmax, after) == []
+
+
+def test_rebalance_repairs_empty_blocks_first(orc):
+    """rebalancer.cpp:34-62: an imbalanced partition with empty blocks gets the
+    repair moves first (their record leads the statistics), then the rebalancing
+    rounds; the result is balanced with no empty block and exact km1 bookkeeping."""
+    from lpgpu import gen
+    hg, _ = load_golden("contracted_ibm01")
+    k = 8
+    perfect, lmax = gen.part_weights(int(hg.w_v.sum()), k, 0.03)
+    part = _rebalance_test_partition(hg, k)
+    moves = orc.repair_empty_blocks(hg, k, lmax, part)
+    p, stats = orc.rebalance(hg, k, lmax, part, 32)
+    assert stats[0]["candidates"] == 4 and stats[0]["moved"] == 4 and stats[0]["active"] == hg.n
+    assert stats[0]["delta"] == _delta(orc, hg, k, part, _apply(orc, hg, k, part, [m[:3] for m in moves]))
+    _, conn, bw = orc.init_partition(hg, k, p)
+    assert (bw <= lmax).all() and (bw > 0).all()
+    _, conn0, _ = orc.init_partition(hg, k, part)
+    assert orc.metrics(hg, k, conn)[0] == orc.metrics(hg, k, conn0)[0] + sum(s["delta"] for s in stats)
