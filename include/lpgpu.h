@@ -74,6 +74,39 @@ typedef struct {
 /* lpgpu_config.flags: launch the refine directly instead of capturing it once
  * as a CUDA graph and replaying it (useful when every call has new sizes). */
 #define LPGPU_FLAG_NO_GRAPH 1
+/* lpgpu_config.flags: run the refine as one persistent launch per round (every
+ * CTA refines whole instances taken from a device work queue), or force the
+ * multi-launch sub-round pipeline. Without either flag the session's tuning
+ * decides (lpgpu_session_set_tuning, else the process-wide tuning table).
+ * The persistent form needs every instance's k <= LPGPU_PERSISTENT_MAX_K and
+ * no explicit refinement node list; otherwise the refine returns
+ * LPGPU_ERR_INVALID_ARG when it is forced and takes the multi-launch form
+ * when it is only tuned. Both forms give identical results. */
+#define LPGPU_FLAG_PERSISTENT 2
+#define LPGPU_FLAG_MULTI_LAUNCH 4
+#define LPGPU_PERSISTENT_MAX_K 64
+
+/* How a refine runs (the knobs the autotuner searches). */
+typedef enum {
+  LPGPU_MODE_MULTI_LAUNCH = 0, /* the sub-round pipeline over the whole (union) hypergraph */
+  LPGPU_MODE_PERSISTENT = 1    /* one launch per round, instances as work items */
+} lpgpu_mode;
+
+typedef struct {
+  int32_t mode;        /* lpgpu_mode */
+  int32_t ctas_per_sm; /* persistent: resident CTAs per SM (1: up to 128 registers, 2: up to 64) */
+  int32_t unroll;      /* persistent: incidences per lane step of the sweep (4 or 8) */
+  int32_t order;       /* persistent: 0 largest instance first, 1 instance order */
+} lpgpu_tuning;
+
+/* One row of the tuning table: applies to a refine whose session holds at
+ * least min_instances instances of at most max_mean_pins pins on average. */
+typedef struct {
+  int64_t max_mean_pins;
+  int32_t min_instances;
+  int32_t reserved;
+  lpgpu_tuning tuning;
+} lpgpu_tuning_entry;
 
 /* Result of one refine call. Mirrors the kahypar::Metrics update done in
  * LabelPropagationRefiner::refineImpl (label_propagation_refiner.cpp:48-67). */
@@ -239,6 +272,17 @@ LPGPU_API lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config
                                             const int32_t* refinement_nodes,
                                             int64_t num_refinement_nodes,
                                             lpgpu_result* result);
+
+/* Process-wide tuning table (the autotuner's output, rows in priority order;
+ * the first row that applies wins; count 0 clears it). Without a matching
+ * row, and without a session tuning, refines use the multi-launch form. This
+ * has no counterpart in the reference, which has no device code to tune. */
+LPGPU_API lpgpu_status lpgpu_set_tuning_table(const lpgpu_tuning_entry* entries, int32_t count);
+
+/* Tuning of one session (NULL: back to the table). lpgpu_session_tuning gives
+ * the tuning the next refine of the session's current upload uses. */
+LPGPU_API lpgpu_status lpgpu_session_set_tuning(lpgpu_session* s, const lpgpu_tuning* tuning);
+LPGPU_API lpgpu_status lpgpu_session_tuning(lpgpu_session* s, lpgpu_tuning* out);
 
 /* Statistics of the last refine: up to max_rounds records, returns the count in *rounds. */
 LPGPU_API lpgpu_status lpgpu_session_round_stats(lpgpu_session* s, lpgpu_round_stats* out,

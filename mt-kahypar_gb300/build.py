@@ -20,7 +20,8 @@ LIB = os.path.join(HERE, "lpgpu", "liblpgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
-              "-I" + INCLUDE, "-I" + CSRC]
+              "-I" + INCLUDE, "-I" + CSRC,
+              "--split-compile", "0"]  # the large kernel file's functions are optimized in parallel
 # extra nvcc flags, e.g. "-DLPGPU_LV_UNROLL=8" to build a tuning variant
 NVCC_FLAGS += os.environ.get("LPGPU_NVCC_EXTRA", "").split()
 

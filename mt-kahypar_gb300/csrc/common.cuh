@@ -77,6 +77,7 @@ enum Scalar : int {
   kOverCount = 10, // number of overflowing target blocks
   kHeavyCount = 11, // heavy vertices a per-vertex query deferred to k_sweep_heavy
   kRevCount = 12,  // moves marked for revert in the current sub-round
+  kPxQueue = 13,   // work queue counter of a persistent round
   kScalars = 16
 };
 
@@ -293,6 +294,59 @@ cudaError_t launch_rebalance_round(const Launch& L, const RoundCtx& c, int round
 // keys / ws: n-entry scratch; scratch: 2 int64.
 cudaError_t launch_repair_candidates(const Launch& L, const RoundCtx& c, int blk, uint64_t* keys, int32_t* ws,
                                      int4* out, int64_t* scratch);
+
+// ---- persistent rounds (one launch per LP round of a batch of small instances)
+
+// Largest k of an instance the persistent round kernel takes (Λ records of
+// at most 2 words).
+constexpr int kPxMaxK = 64;
+
+// One instance of a persistent round. Arrays are indexed by the ids the
+// instance's CSR stores (union ids in a batched session), so several
+// instances may share one set of arrays; keys / kw / cand hold v1 - v0
+// entries of per-instance scratch starting at their pointer.
+struct PxInst {
+  const int64_t* net_off;
+  const int32_t* pins;
+  const int64_t* vtx_off;
+  const int32_t* inets;
+  const int32_t* w_v;
+  const int32_t* w_e;
+  int32_t* part;        // global block ids: boff + local id
+  int32_t* phi;
+  uint32_t* conn;
+  int64_t* bw;          // block weights at [boff, boff + k)
+  const int64_t* lmax;
+  const int64_t* perfect;
+  uint8_t* flag;        // bit 0: active this round, bit 1: active next round
+  int4* rec;            // per vertex: (to, gain, -, from) of its candidate move
+  uint8_t* status;      // per vertex: 1 committed, 2 reverted, 3 rolled back
+  uint64_t* keys;       // selection keys (scratch)
+  int32_t* kw;          // selection weights (scratch)
+  int32_t* cand;        // the sub-round's candidates as local ids (scratch)
+  int32_t* net_epoch;   // round stamp of nets whose pins were activated
+  int64_t* stats;       // kStats counters per round, round r at r * kStats (added to)
+  int64_t v0, v1;
+  int32_t boff, k;
+  int32_t kstride;      // Φ row length
+  int32_t W;            // Λ words per record half (1 or 2)
+  int32_t unit_nets, phi16, max_we;
+  int32_t round;        // round of this instance (when the launch does not set one)
+};
+
+struct PxParams {
+  int32_t S, zero_gain, revert, rollback;
+  int64_t act_threshold;
+  int32_t round;        // >= 0: every instance runs this round; < 0: its own `round`
+  int32_t unroll;       // incidences per lane step of the sweep (4 or 8)
+};
+
+// Runs one LP round of `count` instances, taken in `order` (null:
+// 0..count-1) from the work queue counter `queue` (zeroed here). W: Λ words
+// class of all instances (1 or 2); unit: every net weight is 1; ctas_per_sm:
+// the 1- or 2-CTA-per-SM build of the kernel.
+cudaError_t launch_px_round(const Launch& L, const PxInst* insts, const int32_t* order, int32_t count,
+                            const PxParams& P, int W, bool unit, int ctas_per_sm, int64_t* queue);
 
 // Optional per-phase CUDA-event timing.
 struct PhaseTimer {

@@ -539,20 +539,22 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t x) {
   return x;
 }
 
-template <int W>
+// W words of a Λ record. NC: through the read-only data path (records that
+// no thread of the running kernel changes); otherwise plain coherent loads.
+template <int W, bool NC = true>
 __device__ __forceinline__ void load_words(const uint32_t* __restrict__ p, uint32_t (&w)[W]) {
   if constexpr (W % 4 == 0) {
 #pragma unroll
     for (int i = 0; i < W / 4; ++i) {
-      const uint4 q = __ldg(reinterpret_cast<const uint4*>(p) + i);
+      const uint4 q = NC ? __ldg(reinterpret_cast<const uint4*>(p) + i) : reinterpret_cast<const uint4*>(p)[i];
       w[4 * i] = q.x; w[4 * i + 1] = q.y; w[4 * i + 2] = q.z; w[4 * i + 3] = q.w;
     }
   } else if constexpr (W == 2) {
-    const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
+    const uint2 q = NC ? __ldg(reinterpret_cast<const uint2*>(p)) : *reinterpret_cast<const uint2*>(p);
     w[0] = q.x; w[1] = q.y;
   } else {
 #pragma unroll
-    for (int i = 0; i < W; ++i) w[i] = __ldg(p + i);
+    for (int i = 0; i < W; ++i) w[i] = NC ? __ldg(p + i) : p[i];
   }
 }
 
@@ -712,7 +714,7 @@ __device__ __forceinline__ void lv_add_weighted(uint32_t (&cnt)[PL], uint32_t x,
 // One step of a lane's vertex: the next U incidences (from index j) of the
 // vertex with incidences [o0, o0 + d) and source block `from` (local) are
 // added into the bit-sliced counters and the internal weight.
-template <int W, bool UNIT, int PL, int U>
+template <int W, bool UNIT, int PL, int U, bool NC = true>
 __device__ __forceinline__ void lv_accumulate(const RoundCtx& c, int64_t o0, int d, int j, int from,
                                               uint32_t (&cnt)[W][PL], int& internal) {
   constexpr int W2 = 2 * W;
@@ -731,8 +733,8 @@ __device__ __forceinline__ void lv_accumulate(const RoundCtx& c, int64_t o0, int
     we[u] = 0;
     if (ee[u] >= 0) {
       const uint32_t* rec = c.conn + (int64_t)ee[u] * W2;
-      load_words<W>(rec, wd[u]);
-      l1[u] = __ldg(rec + W + fw);
+      load_words<W, NC>(rec, wd[u]);
+      l1[u] = NC ? __ldg(rec + W + fw) : rec[W + fw];
       we[u] = UNIT ? 1 : __ldg(&c.w_e[ee[u]]);
     }
   }
@@ -839,21 +841,23 @@ __device__ __forceinline__ void lv_decide(const RoundCtx& c, const uint32_t (&cn
   }
 }
 
-// Best move of one vertex by its own lane (accumulate all incidences, decide).
-template <int W, bool UNIT, int PL>
+// Best move of one vertex by its own lane (accumulate all incidences, decide);
+// U incidences per step have their gathers in flight together; NC as in
+// load_words.
+template <int W, bool UNIT, int PL, int U = LPGPU_LV_UNROLL, bool NC = true>
 __device__ __forceinline__ void lv_vertex(const RoundCtx& c, int64_t o0, int d, int from, int wv, int bo,
                                           int inst, bool batched, int zero_gain,
                                           const uint32_t* __restrict__ s_fmask, const int* __restrict__ s_slack,
                                           const int64_t* __restrict__ s_bw, const int64_t* __restrict__ s_perf,
                                           int& to, int& gain, bool& border) {
-  constexpr int U = LPGPU_LV_UNROLL;
+  static_assert(U % 4 == 0, "the carry-save adder takes four vectors at a time");
   uint32_t cnt[W][PL];
 #pragma unroll
   for (int t = 0; t < W; ++t)
 #pragma unroll
     for (int p = 0; p < PL; ++p) cnt[t][p] = 0;
   int internal = 0;  // Σ w(e) over incident nets with Φ(e, from) > 1
-  for (int j = 0; j < d; j += U) lv_accumulate<W, UNIT, PL, U>(c, o0, d, j, from, cnt, internal);
+  for (int j = 0; j < d; j += U) lv_accumulate<W, UNIT, PL, U, NC>(c, o0, d, j, from, cnt, internal);
   lv_decide<W, PL>(c, cnt, internal, from, wv, bo, inst, batched, zero_gain, s_fmask, s_slack, s_bw, s_perf, to,
                    gain, border);
 }
@@ -2043,7 +2047,8 @@ __device__ __forceinline__ void sel_hist(const uint64_t* __restrict__ keys, cons
 }
 
 __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const int32_t* __restrict__ gws,
-                                     int64_t cnt, int64_t budget0) {
+                                     int64_t cnt, int64_t budget0, unsigned char* stage = nullptr,
+                                     int stage_cap = kSelStage) {
   constexpr int NW = kSelThreads / 32;
   extern __shared__ __align__(16) unsigned char sel_smem[];
   __shared__ unsigned hist[NW][256];
@@ -2052,9 +2057,11 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const i
   __shared__ int64_t s_budget;
   __shared__ int s_sel;
   const int lane = lane_id(), wid = threadIdx.x >> 5;
-  const bool staged = cnt <= kSelStage;
-  uint64_t* skeys = reinterpret_cast<uint64_t*>(sel_smem);
-  int32_t* sws = reinterpret_cast<int32_t*>(skeys + kSelStage);
+  // segments of up to stage_cap keys are staged in `stage` (default: the
+  // kernel's dynamic shared memory, kSelStage keys)
+  const bool staged = cnt <= stage_cap;
+  uint64_t* skeys = reinterpret_cast<uint64_t*>(stage ? stage : sel_smem);
+  int32_t* sws = reinterpret_cast<int32_t*>(skeys + stage_cap);
   uint64_t ka = ~0ull, ko = 0;
 #pragma unroll 4
   for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
@@ -2075,7 +2082,7 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const i
   if (lane == 0) { s_and[wid] = ka; s_or[wid] = ko; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < NW; ++w) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {  // any CTA width up to kSelThreads
       ka &= s_and[w];
       ko |= s_or[w];
     }
@@ -3159,6 +3166,467 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
     LAUNCHED("k_rollback");
   }
   return cudaSuccess;
+}
+
+// ======================================================= persistent rounds
+//
+// A batch of many small instances runs one launch per LP round. Every CTA
+// takes whole instances from a device work queue (largest first unless the
+// tuning says otherwise) and runs all S sub-rounds of that instance's round
+// itself: sweep, target- and source-side selection, commit, hindsight
+// reverts, rollback and activation, separated by CTA barriers instead of
+// grid-wide launch boundaries. Instances are independent, so no CTA ever
+// waits for another, and a CTA that finishes a small instance takes the next
+// one while others are still on large ones. Each phase follows the same rule
+// as the multi-launch pipeline (the same lane-per-vertex sweep, selection
+// thresholds and CTA-flat commit), so every instance ends exactly as when it
+// is refined alone. The sweep reads the Λ records that the same kernel's
+// commits change, so it loads them through the coherent path, not __ldg.
+
+constexpr int kPxThreads = kFlatThreads;  // the CTA-flat helpers are written for this width
+constexpr int kPxWarps = kPxThreads / 32;
+static_assert(kPxThreads <= kSelThreads, "the radix selection's histograms cover the CTA");
+
+struct PxShared {
+  int64_t bw[kPxMaxK], lmax[kPxMaxK], perf[kPxMaxK];
+  int slack[kPxMaxK];
+  uint32_t fmask[kLvWeights * 2];
+  ull in_w[kPxMaxK], acc_w[kPxMaxK];
+  unsigned in_cnt[kPxMaxK], acc_cnt[kPxMaxK];
+  int64_t seg[kPxMaxK + 1];
+  unsigned cursor[kPxMaxK];
+  uint64_t thr_to[kPxMaxK], thr_from[kPxMaxK];
+  int pen[kPxWarps][kPxMaxK];
+  int ncand, nrev, item;
+  long long st[kStats];
+};
+
+__device__ __forceinline__ RoundCtx px_ctx(const PxInst& I) {
+  RoundCtx c{};
+  c.vtx_off = I.vtx_off;
+  c.inets = I.inets;
+  c.w_v = I.w_v;
+  c.w_e = I.w_e;
+  c.part = I.part;
+  c.phi = I.phi;
+  c.conn = I.conn;
+  c.k = I.k;
+  c.W = I.W;
+  c.kmax = I.kstride;
+  c.unit_nets = I.unit_nets;
+  c.phi16 = I.phi16;
+  c.max_we = I.max_we;
+  return c;
+}
+
+// A candidate move of local vertex lv: its record, the per-block totals and
+// the sub-round's candidate list.
+__device__ __forceinline__ void px_candidate(const PxInst& I, PxShared& s, int64_t lv, int from, int to, int gain,
+                                             int wv) {
+  I.rec[I.v0 + lv] = make_int4(to, gain, 0, from);
+  atomicAdd(&s.in_w[to], (ull)(int64_t)wv);
+  atomicAdd(&s.in_cnt[to], 1u);
+  I.cand[atomicAdd(&s.ncand, 1)] = (int32_t)lv;
+}
+
+// A heavy vertex (summed net weight beyond the lane counters), evaluated by
+// the warp that found it: lanes split its incidences, penalties are summed per
+// block in the warp's shared row, then the block-owning lanes decide (decide:
+// the rule of Km1Policy::computeMaxGainMoveImpl).
+template <int W, bool UNIT>
+__device__ void px_heavy(const PxInst& I, const PxParams& P, PxShared& s, int64_t lv) {
+  const int lane = lane_id(), wid = threadIdx.x >> 5, k = I.k;
+  int* pen = s.pen[wid];
+  const int64_t v = I.v0 + lv;
+  const int64_t o0 = I.vtx_off[v];
+  const int d = (int)(I.vtx_off[v + 1] - o0);
+  const int from = I.part[v] - I.boff, wv = I.w_v[v];
+  for (int b = lane; b < k; b += 32) pen[b] = 0;
+  __syncwarp();
+  const int fw = from >> 5;
+  const uint32_t fbit = 1u << (from & 31);
+  int internal = 0;
+  bool border = false;
+  for (int j = lane; j < d; j += 32) {
+    const int64_t e = I.inets[o0 + j];
+    const int we = UNIT ? 1 : I.w_e[e];
+    const uint32_t* rec = I.conn + e * 2 * W;
+    if (!(rec[W + fw] & fbit)) internal += we;  // Φ(e, from) > 1
+#pragma unroll
+    for (int t = 0; t < W; ++t) {
+      uint32_t bits = rec[t] & (t == fw ? ~fbit : ~0u);
+      border = border || bits != 0;
+      while (bits) {
+        atomicAdd(&pen[32 * t + __ffs(bits) - 1], we);
+        bits &= bits - 1;
+      }
+    }
+  }
+  internal = warp_sum(internal);
+  border = __any_sync(FULLMASK, border);
+  __syncwarp();
+  if (border) {
+    int pn[W], sl[W];
+#pragma unroll
+    for (int t = 0; t < W; ++t) {
+      const int b = 32 * t + lane;
+      pn[t] = b < k ? pen[b] : 0;
+      sl[t] = b < k ? s.slack[b] : -1;
+    }
+    int to = from, gain = 0;
+    decide<W, false>(k, from, wv, internal, P.zero_gain, pn, sl, s.bw, s.perf, to, gain);
+    if (lane == 0 && to != from) px_candidate(I, s, lv, from, to, gain, wv);
+  }
+  __syncwarp();
+}
+
+// Thresholds of the blocks flagged in `over` (bit b): the first key of the
+// block's segment whose weighted prefix exceeds budget(b). The segments are
+// filled from the candidate list by member(rec, lv) (the block a candidate
+// belongs to, or -1); cnt[b] is the size of block b's segment.
+constexpr int kPxStage = 2048;  // selection keys staged in the CTA-flat area (not in use then)
+static_assert(sizeof(FlatSmem) >= (size_t)kPxStage * 12, "staged keys and weights fit the CTA-flat area");
+
+template <typename Member, typename Budget>
+__device__ void px_select(const PxInst& I, PxShared& s, FlatSmem& f, uint64_t over, const unsigned* cnt,
+                          uint64_t* thr, Member member, Budget budget) {
+  if (threadIdx.x == 0) {
+    int64_t run = 0;
+    for (int b = 0; b < I.k; ++b) {
+      s.seg[b] = run;
+      s.cursor[b] = (unsigned)run;
+      if ((over >> b) & 1) run += cnt[b];
+    }
+    s.seg[I.k] = run;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < s.ncand; i += blockDim.x) {
+    const int lv = I.cand[i];
+    const int4 r = I.rec[I.v0 + lv];
+    const int b = member(r, lv);
+    if (b >= 0 && ((over >> b) & 1)) {
+      const unsigned slot = atomicAdd(&s.cursor[b], 1u);
+      I.keys[slot] = move_key(r.y, lv);
+      I.kw[slot] = I.w_v[I.v0 + lv];
+    }
+  }
+  __syncthreads();
+  for (int b = 0; b < I.k; ++b) {
+    if (!((over >> b) & 1)) continue;
+    const uint64_t t = cta_radix_select(I.keys + s.seg[b], I.kw + s.seg[b], s.seg[b + 1] - s.seg[b], budget(b),
+                                        reinterpret_cast<unsigned char*>(&f), kPxStage);
+    if (threadIdx.x == 0) thr[b] = t;
+    __syncthreads();
+  }
+}
+
+// Moves the collected items of f (local vertex ids in f.pos, local
+// from | to << 16 in f.ft) between their blocks: part, block weights and,
+// CTA-flat, Φ / Λ / Λ1 with km1Delta attribution. Returns this thread's
+// attributed delta.
+__device__ __forceinline__ int64_t px_move_items(const RoundCtx& c, const PxInst& I, PxShared& s, FlatSmem& f,
+                                                 int64_t* moved_pins, int64_t* toggles) {
+  __syncthreads();
+  const int n = f.n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int64_t v = I.v0 + f.pos[i];
+    const int from = f.ft[i] & 0xffff, to = f.ft[i] >> 16;
+    const int64_t wv = I.w_v[v];
+    I.part[v] = I.boff + to;
+    atomicAdd(reinterpret_cast<ull*>(&s.bw[to]), (ull)wv);
+    atomicAdd(reinterpret_cast<ull*>(&s.bw[from]), (ull)(-wv));
+  }
+  const int total = flat_scan(f, n);
+  if (moved_pins && threadIdx.x == 0) *moved_pins += total;
+  const int64_t att = flat_commit(c, f, n, total, false, toggles);
+  __syncthreads();
+  return att;
+}
+
+// Collects into f the candidates [c0, c0 + kFlatItems) of the sub-round list
+// with status `want` (0: the accepted ones), as moves from `from` to `to`
+// (back: the reverse), and sets their status to `set` (0: unchanged).
+// Returns this thread's number of collected items.
+template <bool ACCEPT>
+__device__ __forceinline__ int px_gather(const PxInst& I, PxShared& s, FlatSmem& f, int c0, int ncand, int want,
+                                         bool back, int set) {
+  constexpr int PER = kFlatItems / kPxThreads;
+  if (threadIdx.x == 0) f.n = 0;
+  __syncthreads();
+  int got = 0;
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int i = c0 + q * kPxThreads + threadIdx.x;
+    bool take = false;
+    int lv = 0;
+    int4 r = make_int4(0, 0, 0, 0);
+    if (i < ncand) {
+      lv = I.cand[i];
+      r = I.rec[I.v0 + lv];
+      if constexpr (ACCEPT) {
+        const uint64_t key = move_key(r.y, lv);
+        take = key < s.thr_to[r.x] && key < s.thr_from[r.w];
+      } else {
+        take = I.status[I.v0 + lv] == want;
+      }
+    }
+    const int slot = flat_append(f, take);
+    if (take) {
+      const int64_t v = I.v0 + lv;
+      f.o0[slot] = I.vtx_off[v];
+      f.pre[slot] = (int)(I.vtx_off[v + 1] - f.o0[slot]);
+      f.ft[slot] = back ? (r.x | (r.w << 16)) : (r.w | (r.x << 16));
+      f.att[slot] = 0;
+      f.pos[slot] = lv;
+      if (set) I.status[v] = (uint8_t)set;
+      ++got;
+    }
+  }
+  return got;
+}
+
+template <int W, bool UNIT, int U>
+__device__ void px_instance_round(const PxInst& I, const PxParams& P, PxShared& s, FlatSmem& f) {
+  constexpr int PL = UNIT ? 6 : 8;
+  const RoundCtx c = px_ctx(I);
+  const int k = I.k, S = P.S;
+  const int round = P.round >= 0 ? P.round : I.round;
+  const int64_t ni = I.v1 - I.v0;
+  for (int b = threadIdx.x; b < k; b += blockDim.x) {
+    s.bw[b] = I.bw[I.boff + b];
+    s.lmax[b] = I.lmax[I.boff + b];
+    s.perf[b] = I.perfect[I.boff + b];
+  }
+  if (threadIdx.x < kStats) s.st[threadIdx.x] = 0;
+  int64_t t_active = 0, t_pins = 0, t_moved_pins = 0, t_toggles = 0;
+  __syncthreads();
+  for (int sub = 0; sub < S; ++sub) {
+    // ---- slack, feasibility masks, per-block totals
+    for (int b = threadIdx.x; b < k; b += blockDim.x) {
+      const int64_t sl = s.lmax[b] - s.bw[b];
+      s.slack[b] = sl < 0 ? -1 : (sl > INT_MAX ? INT_MAX : (int)sl);
+      s.in_w[b] = s.acc_w[b] = 0;
+      s.in_cnt[b] = s.acc_cnt[b] = 0;
+      s.thr_to[b] = s.thr_from[b] = ~0ull;
+    }
+    if (threadIdx.x == 0) {
+      s.ncand = 0;
+      s.nrev = 0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kLvWeights * W; i += blockDim.x) {
+      const int w = i / W + 1, t = i % W;
+      uint32_t msk = 0;
+      for (int l = 0; l < 32; ++l) {
+        const int b = 32 * t + l;
+        if (b < k && s.slack[b] >= w) msk |= 1u << l;
+      }
+      s.fmask[i] = msk;
+    }
+    __syncthreads();
+    // ---- sweep: a sub-round holds whole 32-vertex chunks; warps take the
+    // sub-round's chunks independently (no CTA barrier), a lane evaluates its
+    // own vertex, and the warp evaluates the chunk's heavy vertices together
+    {
+      const int lane = lane_id(), wid = threadIdx.x >> 5;
+      const int64_t nch = (ni + 31) >> kChunkShift;
+      for (int64_t ch = wid; ch < nch; ch += kPxWarps) {
+        if (subround_of(ch << kChunkShift, round, S) != sub) continue;
+        const int64_t lv = (ch << kChunkShift) + lane, v = I.v0 + lv;
+        bool heavy = false;
+        if (lv < ni && (I.flag[v] & 1)) {
+          I.status[v] = 0;
+          const int64_t o0 = I.vtx_off[v], dd = I.vtx_off[v + 1] - o0;
+          ++t_active;
+          t_pins += dd;
+          const int d = dd > kHighDegree ? 0 : (int)dd;  // isBorderNode is false above the threshold
+          heavy = sweep_heavy(d, W, UNIT, I.max_we);
+          if (!heavy && d > 0) {
+            const int from = I.part[v] - I.boff, wv = I.w_v[v];
+            int to = from, gain = 0;
+            bool border = false;
+            lv_vertex<W, UNIT, PL, U, false>(c, o0, d, from, wv, 0, 0, false, P.zero_gain, s.fmask, s.slack, s.bw,
+                                             s.perf, to, gain, border);
+            if (to != from) px_candidate(I, s, lv, from, to, gain, wv);
+          }
+        }
+        for (unsigned hm = __ballot_sync(FULLMASK, heavy); hm; hm &= hm - 1)
+          px_heavy<W, UNIT>(I, P, s, (ch << kChunkShift) + __ffs(hm) - 1);
+      }
+    }
+    __syncthreads();
+    const int ncand = s.ncand;
+    // ---- target side (the atomic weight check of changeNodePart, h:548-562):
+    // per block the longest (gain, vertex) prefix within L_max
+    uint64_t over = 0;
+    for (int b = 0; b < k; ++b)
+      if ((int64_t)s.in_w[b] > s.lmax[b] - s.bw[b]) over |= 1ull << b;
+    if (over)
+      px_select(I, s, f, over, s.in_cnt, s.thr_to, [](const int4& r, int) { return r.x; },
+                [&](int b) { return s.lmax[b] - s.bw[b]; });
+    // ---- source side (from_weight_after > 0, h:551): per block the longest
+    // prefix of its target-accepted moves that leaves weight >= 1
+    for (int i = threadIdx.x; i < ncand; i += blockDim.x) {
+      const int lv = I.cand[i];
+      const int4 r = I.rec[I.v0 + lv];
+      if (move_key(r.y, lv) < s.thr_to[r.x]) {
+        atomicAdd(&s.acc_w[r.w], (ull)(int64_t)I.w_v[I.v0 + lv]);
+        atomicAdd(&s.acc_cnt[r.w], 1u);
+      }
+    }
+    __syncthreads();
+    uint64_t over_from = 0;
+    for (int b = 0; b < k; ++b)
+      if (s.bw[b] - (int64_t)s.acc_w[b] < 1) over_from |= 1ull << b;
+    if (over_from)
+      px_select(I, s, f, over_from, s.acc_cnt, s.thr_from,
+                [&](const int4& r, int lv) { return move_key(r.y, lv) < s.thr_to[r.x] ? r.w : -1; },
+                [&](int b) { return s.bw[b] - 1; });
+    // ---- commit of the accepted moves
+    int64_t att = 0;
+    for (int c0 = 0; c0 < ncand; c0 += kFlatItems) {
+      px_gather<true>(I, s, f, c0, ncand, 0, false, 1);
+      att += px_move_items(c, I, s, f, &t_moved_pins, &t_toggles);
+    }
+    // ---- hindsight reverts: every committed move is evaluated on the
+    // post-commit state before any is undone (moveVertex,
+    // label_propagation_refiner.h:100-137, made deterministic)
+    if (P.revert) {
+      for (int c0 = 0; c0 < ncand; c0 += kFlatItems) {
+        px_gather<false>(I, s, f, c0, ncand, 1, false, 0);
+        __syncthreads();
+        const int n = f.n;
+        const int total = flat_scan(f, n);
+        // gain of moving back: + w(e) if Φ(e, to) > 1, - w(e) if from is in Λ(e)
+        for (int x = threadIdx.x; x < total; x += kPxThreads) {
+          const int it = flat_find(f, n, x);
+          const int64_t e = I.inets[f.o0[it] + (x - f.pre[it])];
+          const int fa = f.ft[it] & 0xffff, ta = f.ft[it] >> 16;
+          const uint32_t* rec = I.conn + e * 2 * W;
+          const int we = UNIT ? 1 : I.w_e[e];
+          const int xa = (((rec[W + (ta >> 5)] >> (ta & 31)) & 1u) ? 0 : we) -
+                         (((rec[fa >> 5] >> (fa & 31)) & 1u) ? we : 0);
+          if (xa) atomicAdd(&f.att[it], xa);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+          if (f.att[i] < 0) {
+            I.status[I.v0 + f.pos[i]] = 2;
+            atomicAdd(&s.nrev, 1);
+          }
+        __syncthreads();
+      }
+      if (s.nrev)
+        for (int c0 = 0; c0 < ncand; c0 += kFlatItems) {
+          px_gather<false>(I, s, f, c0, ncand, 2, true, 0);
+          att += px_move_items(c, I, s, f, nullptr, nullptr);
+        }
+    }
+    // ---- rollback of a sub-round whose summed delta is positive
+    att = block_sum_i64(att);
+    int64_t rolled = 0;
+    if (P.rollback && att > 0) {
+      for (int c0 = 0; c0 < ncand; c0 += kFlatItems) {
+        rolled += px_gather<false>(I, s, f, c0, ncand, 1, true, 3);
+        att += block_sum_i64(px_move_items(c, I, s, f, nullptr, nullptr));
+      }
+      rolled = block_sum_i64(rolled);
+    }
+    // ---- activation of the kept moves (label_propagation_refiner.h:112-128):
+    // the vertex and the pins of its nets with |e| <= threshold, once per net
+    int64_t kept = 0;
+    const int stamp = round + 1;
+    for (int c0 = 0; c0 < ncand; c0 += kFlatItems) {
+      kept += px_gather<false>(I, s, f, c0, ncand, 1, false, 0);
+      __syncthreads();
+      const int n = f.n;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) I.flag[I.v0 + f.pos[i]] |= 2;
+      const int total = flat_scan(f, n);
+      for (int x = threadIdx.x; x < total; x += kPxThreads) {
+        const int it = flat_find(f, n, x);
+        const int64_t e = I.inets[f.o0[it] + (x - f.pre[it])];
+        const int64_t p0 = I.net_off[e], p1 = I.net_off[e + 1];
+        if (p1 - p0 <= P.act_threshold && atomicExch(&I.net_epoch[e], stamp) != stamp)
+          for (int64_t j = p0; j < p1; ++j) I.flag[I.pins[j]] |= 2;
+      }
+      __syncthreads();
+    }
+    kept = block_sum_i64(kept);
+    if (threadIdx.x == 0) {
+      s.st[kStCands] += ncand;
+      s.st[kStMoved] += kept;
+      s.st[kStReverted] += s.nrev + rolled;
+      s.st[kStDelta] += att;
+    }
+    __syncthreads();
+  }
+  // ---- end of the instance's round: next round's flags, weights, statistics
+  for (int64_t lv = threadIdx.x; lv < ni; lv += blockDim.x) I.flag[I.v0 + lv] >>= 1;
+  for (int b = threadIdx.x; b < k; b += blockDim.x) I.bw[I.boff + b] = s.bw[b];
+  t_active = block_sum_i64(t_active);
+  t_pins = block_sum_i64(t_pins);
+  t_moved_pins = block_sum_i64(t_moved_pins);
+  t_toggles = block_sum_i64(t_toggles);
+  if (threadIdx.x == 0) {
+    int64_t* st = I.stats + (int64_t)round * kStats;
+    s.st[kStActive] = t_active;
+    s.st[kStPins] = t_pins;
+    s.st[kStMovedPins] = t_moved_pins;
+    s.st[kStToggles] = t_toggles;
+    for (int j = 0; j < kStats; ++j)
+      if (s.st[j]) atomicAdd(reinterpret_cast<ull*>(&st[j]), (ull)s.st[j]);
+  }
+  __syncthreads();
+}
+
+template <int W, bool UNIT, int U, int MINB>
+__global__ void __launch_bounds__(kPxThreads, MINB) k_px_round(const PxInst* __restrict__ insts,
+                                                               const int32_t* __restrict__ order, int32_t count,
+                                                               PxParams P, int64_t* queue) {
+  extern __shared__ __align__(16) unsigned char px_smem[];
+  FlatSmem& f = *reinterpret_cast<FlatSmem*>(px_smem);
+  PxShared& s = *reinterpret_cast<PxShared*>(px_smem + ((sizeof(FlatSmem) + 15) & ~size_t(15)));
+  for (;;) {
+    if (threadIdx.x == 0) s.item = (int)atomicAdd(reinterpret_cast<ull*>(queue), 1ull);
+    __syncthreads();
+    const int it = s.item;
+    __syncthreads();
+    if (it >= count) break;
+    px_instance_round<W, UNIT, U>(insts[order ? order[it] : it], P, s, f);
+  }
+}
+
+constexpr size_t kPxSmem = ((sizeof(FlatSmem) + 15) & ~size_t(15)) + sizeof(PxShared);
+
+// Kernel variant: W words, unit net weights, sweep unroll 4 or 8, compiled for
+// 1 resident CTA per SM (up to 128 registers) or 2 (64 registers).
+template <int W, bool UNIT>
+static const void* px_kernel_wu(int unroll, int minb) {
+  if (minb >= 2) return unroll == 8 ? (const void*)k_px_round<W, UNIT, 8, 2> : (const void*)k_px_round<W, UNIT, 4, 2>;
+  return unroll == 8 ? (const void*)k_px_round<W, UNIT, 8, 1> : (const void*)k_px_round<W, UNIT, 4, 1>;
+}
+
+static const void* px_kernel_for(int W, bool unit, int unroll, int minb) {
+  if (W == 1) return unit ? px_kernel_wu<1, true>(unroll, minb) : px_kernel_wu<1, false>(unroll, minb);
+  return unit ? px_kernel_wu<2, true>(unroll, minb) : px_kernel_wu<2, false>(unroll, minb);
+}
+
+cudaError_t launch_px_round(const Launch& L, const PxInst* insts, const int32_t* order, int32_t count,
+                            const PxParams& P, int W, bool unit, int ctas_per_sm, int64_t* queue) {
+  if (count <= 0) return cudaSuccess;
+  if (W != 1 && W != 2) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(int64_t), L.st);
+  if (e != cudaSuccess) return e;
+  const int minb = ctas_per_sm >= 2 ? 2 : 1;
+  const void* kern = px_kernel_for(W, unit, P.unroll, minb);
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPxSmem);
+  const int occ = std::max(1, occupancy(kern, kPxThreads, kPxSmem));
+  const int per_sm = std::min(minb, occ);
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(count, (int64_t)per_sm * L.num_sms));
+  void* args[] = {(void*)&insts, (void*)&order, (void*)&count, (void*)&P, (void*)&queue};
+  e = cudaLaunchKernel(kern, dim3(grid), dim3(kPxThreads), args, kPxSmem, L.st);
+  if (e != cudaSuccess) return e;
+  return launched("k_px_round");
 }
 
 }  // namespace lpgpu

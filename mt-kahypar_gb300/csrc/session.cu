@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -171,7 +172,14 @@ struct lpgpu_session_s {
   int32_t num_inst = 0;
   int32_t kmax = 0;
   std::vector<int64_t> h_inst_voff, h_inst_noff, h_inst_weight;
+  std::vector<int64_t> h_inst_pins;  // pins of every instance (work estimate of the persistent rounds)
   std::vector<int32_t> h_inst_boff, h_inst_k;
+  // persistent rounds: instance descriptors, work order, what they were built from
+  DevBuf<PxInst> px;
+  DevBuf<int32_t> px_order;
+  std::vector<int64_t> px_key;
+  bool has_tuning = false;
+  lpgpu_tuning tuning{};
   DevBuf<int32_t> vinst, inst_boff, inst_k, over_ids;
   DevBuf<int64_t> inst_voff, inst_noff, inst_delta;
   DevBuf<int64_t> vout;  // result words of the device-side input checks
@@ -317,6 +325,9 @@ struct lpgpu_session_s {
     for (auto* b : b32) b->release(&mem);
     next_flag.release(&mem);
     saved_part.release(&mem);
+    px.release(&mem);
+    px_order.release(&mem);
+    px_key.clear();
     vinst.release(&mem);
     inst_voff.release(&mem);
     inst_noff.release(&mem);
@@ -557,6 +568,9 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
   // instance ranges of a batched session
   s->batched = inst_voff != nullptr;
   s->num_inst = I;
+  s->h_inst_pins.assign(I, P);
+  for (int32_t i = 0; inst_voff && i < I; ++i)
+    s->h_inst_pins[i] = insts ? inst_poff[i + 1] - inst_poff[i] : net_off[inst_noff[i + 1]] - net_off[inst_noff[i]];
   s->h_inst_voff.assign(2, 0);
   s->h_inst_noff.assign(2, 0);
   s->h_inst_voff[1] = n;
@@ -876,6 +890,122 @@ static lpgpu_status need_part(lpgpu_session* s) {
   return LPGPU_OK;
 }
 
+// ---- tuning (the autotuner's table and per-session choices)
+
+static std::mutex g_tuning_mutex;
+static std::vector<lpgpu_tuning_entry> g_tuning_table;
+
+static lpgpu_tuning default_tuning() {
+  lpgpu_tuning t{};
+  t.mode = LPGPU_MODE_MULTI_LAUNCH;
+  t.ctas_per_sm = 1;
+  t.unroll = 4;
+  t.order = 0;
+  return t;
+}
+
+static bool valid_tuning(const lpgpu_tuning& t) {
+  return (t.mode == LPGPU_MODE_MULTI_LAUNCH || t.mode == LPGPU_MODE_PERSISTENT) &&
+         (t.ctas_per_sm == 1 || t.ctas_per_sm == 2) && (t.unroll == 4 || t.unroll == 8) &&
+         (t.order == 0 || t.order == 1);
+}
+
+// The session's tuning, else the first table row whose instance count and
+// mean instance size it meets, else the multi-launch form.
+static lpgpu_tuning session_tuning(const lpgpu_session* s) {
+  if (s->has_tuning) return s->tuning;
+  const int64_t count = s->batched ? s->num_inst : 1;
+  int64_t pins = 0;
+  for (int64_t p : s->h_inst_pins) pins += p;
+  const int64_t mean = count > 0 ? pins / count : 0;
+  std::lock_guard<std::mutex> lock(g_tuning_mutex);
+  for (const lpgpu_tuning_entry& e : g_tuning_table)
+    if (count >= e.min_instances && mean <= e.max_mean_pins) return e.tuning;
+  return default_tuning();
+}
+
+// Instance descriptors of the persistent rounds over the session's current
+// buffers, and the work order (rebuilt when a buffer or the order changed).
+static lpgpu_status build_px(lpgpu_session* s, int order) {
+  const int32_t I = s->batched ? s->num_inst : 1;
+  const std::vector<int64_t> key = {
+      (int64_t)s->stats.p, (int64_t)s->part.p, (int64_t)s->phi.p,  (int64_t)s->conn.p,      (int64_t)s->bw.p,
+      (int64_t)s->rec.p,   (int64_t)s->seg_key.p, (int64_t)s->revl.p, (int64_t)s->next_flag.p, (int64_t)s->net_off.p,
+      (int64_t)s->inets.p, (int64_t)s->lmax.p, order, s->kmax, s->k, s->W, s->n, s->m, I, s->max_we,
+      s->unit_nets ? 1 : 0};
+  if (s->px.p && s->px_key == key) return LPGPU_OK;
+  std::vector<PxInst> h(I);
+  for (int32_t i = 0; i < I; ++i) {
+    PxInst& x = h[i];
+    x.net_off = s->net_off.p;
+    x.pins = s->pins.p;
+    x.vtx_off = s->vtx_off.p;
+    x.inets = s->inets.p;
+    x.w_v = s->w_v.p;
+    x.w_e = s->w_e.p;
+    x.part = s->part.p;
+    x.phi = s->phi.p;
+    x.conn = s->conn.p;
+    x.bw = s->bw.p;
+    x.lmax = s->lmax.p;
+    x.perfect = s->perfect.p;
+    x.flag = s->next_flag.p;
+    x.rec = s->rec.p;
+    x.status = s->status.p;
+    x.v0 = s->h_inst_voff[i];
+    x.v1 = s->h_inst_voff[i + 1];
+    x.keys = s->seg_key.p + x.v0;
+    x.kw = s->seg_w.p + x.v0;
+    x.cand = s->revl.p + x.v0;
+    x.net_epoch = s->net_epoch.p;
+    x.stats = s->stats.p;
+    x.boff = s->batched ? s->h_inst_boff[i] : 0;
+    x.k = s->batched ? s->h_inst_k[i] : s->k;
+    x.kstride = s->batched ? s->kmax : s->k;
+    x.W = s->W;
+    x.unit_nets = s->unit_nets ? 1 : 0;
+    x.phi16 = s->phi16() ? 1 : 0;
+    x.max_we = s->max_we;
+    x.round = 0;
+  }
+  std::vector<int32_t> ord(I);
+  for (int32_t i = 0; i < I; ++i) ord[i] = i;
+  if (order == 0)  // largest instance first: the longest jobs start first on the work queue
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int32_t a, int32_t b) { return s->h_inst_pins[a] > s->h_inst_pins[b]; });
+  Mem* fp = &s->mem;
+  CK(s->px.alloc(I, fp));
+  CK(s->px_order.alloc(I, fp));
+  CK(cudaMemcpyAsync(s->px.p, h.data(), sizeof(PxInst) * I, cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(s->px_order.p, ord.data(), sizeof(int32_t) * I, cudaMemcpyHostToDevice, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  s->px_key = key;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_set_tuning_table(const lpgpu_tuning_entry* entries, int32_t count) {
+  if (count < 0 || (count > 0 && !entries)) return invalid("bad tuning table");
+  for (int32_t i = 0; i < count; ++i)
+    if (!valid_tuning(entries[i].tuning)) return invalid("tuning row " + std::to_string(i) + " is out of range");
+  std::lock_guard<std::mutex> lock(g_tuning_mutex);
+  g_tuning_table.assign(entries, entries + count);
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_set_tuning(lpgpu_session* s, const lpgpu_tuning* t) {
+  if (!s) return invalid("null session");
+  if (t && !valid_tuning(*t)) return invalid("tuning out of range");
+  s->has_tuning = t != nullptr;
+  if (t) s->tuning = *t;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_tuning(lpgpu_session* s, lpgpu_tuning* out) {
+  if (!s || !out) return invalid("null argument");
+  *out = session_tuning(s);
+  return LPGPU_OK;
+}
+
 lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
                                   const int32_t* nodes, int64_t num_nodes, lpgpu_result* result) {
   lpgpu_status ps = need_part(s);
@@ -885,13 +1015,37 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
   if (cfg.rounds < 0) return invalid("rounds must be >= 0");
   if (cfg.subrounds < 1 || cfg.subrounds > kMaxSubrounds) return invalid("subrounds must be in [1, 64]");
   if (num_nodes < 0 || (num_nodes > 0 && !nodes)) return invalid("bad refinement node list");
+  if ((cfg.flags & LPGPU_FLAG_PERSISTENT) && (cfg.flags & LPGPU_FLAG_MULTI_LAUNCH))
+    return invalid("LPGPU_FLAG_PERSISTENT and LPGPU_FLAG_MULTI_LAUNCH exclude each other");
   for (int64_t i = 0; i < num_nodes; ++i)
     if (nodes[i] < 0 || nodes[i] >= s->n) return invalid("refinement node out of range");
+  // persistent rounds: forced by the flag, or chosen by the tuning when eligible
+  const lpgpu_tuning tu = session_tuning(s);
+  const bool px_ok = num_nodes == 0 && (s->batched ? s->kmax : s->k) <= kPxMaxK;
+  bool use_px = tu.mode == LPGPU_MODE_PERSISTENT;
+  if (cfg.flags & LPGPU_FLAG_PERSISTENT) {
+    if (!px_ok) return invalid("persistent rounds need every k <= 64 and no refinement node list");
+    use_px = true;
+  }
+  if (cfg.flags & LPGPU_FLAG_MULTI_LAUNCH) use_px = false;
+  use_px = use_px && px_ok;
   DeviceGuard g(s->device);
   s->gc_valid = false;  // refinement moves without gain-cache maintenance
   const int R = cfg.rounds, S = cfg.subrounds;
   Mem* fp = &s->mem;
   CK(s->stats.alloc(std::max(1, R) * kStats, fp));
+  if (use_px) {
+    ps = build_px(s, tu.order);
+    if (ps != LPGPU_OK) return ps;
+  }
+  PxParams pxp{};
+  pxp.S = S;
+  pxp.zero_gain = cfg.rebalancing ? 1 : 0;
+  pxp.revert = cfg.revert;
+  pxp.rollback = cfg.rollback;
+  pxp.act_threshold = cfg.activation_threshold <= 0 ? INT64_MAX : cfg.activation_threshold;
+  pxp.unroll = tu.unroll;
+  const int32_t px_count = s->batched ? s->num_inst : 1;
   cudaStream_t st = s->st;
   int64_t km1_before = 0;
   lpgpu_status ms = read_metrics(s, &km1_before, nullptr);
@@ -920,6 +1074,16 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
       if (s->n > 0 && (e = cudaMemsetAsync(s->next_flag.p, 0, s->n, st)) != cudaSuccess) return e;
       if ((e = launch_mark_all(L, c, cfg.rebalancing)) != cudaSuccess) return e;
     }
+    if (use_px) {  // one persistent launch per round
+      for (int r = 0; r < R; ++r) {
+        pxp.round = r;
+        if ((e = launch_px_round(L, s->px.p, s->px_order.p, px_count, pxp, s->W, s->unit_nets, tu.ctas_per_sm,
+                                 s->scal.p + kPxQueue)) != cudaSuccess)
+          return e;
+      }
+      if (s->n > 0 && (e = cudaMemsetAsync(s->next_flag.p, 0, s->n, st)) != cudaSuccess) return e;
+      return cudaSuccess;
+    }
     for (int r = 0; r < R; ++r) {
       if ((e = launch_bin_active(L, c, r, S, s->tile_cnt.p, s->tile_off.p, s->scan_tmp.p, s->scan_tmp_n, tm)) != cudaSuccess)
         return e;
@@ -939,15 +1103,25 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
     // key: every pointer and parameter baked into the captured launches
     struct Key {
       RoundCtx c;
-      int R, S, timing;
+      int R, S, timing, px;
       int64_t* p[3];
       int64_t scan_n;
+      lpgpu_tuning tu;
+      const void* px_ptr[2];
+      int32_t px_count;
     } key;
     std::memset(&key, 0, sizeof(key));
     key.c = c;
     key.R = R;
     key.S = S;
     key.timing = 0;
+    key.px = use_px ? 1 : 0;
+    if (use_px) {
+      key.tu = tu;
+      key.px_ptr[0] = s->px.p;
+      key.px_ptr[1] = s->px_order.p;
+      key.px_count = px_count;
+    }
     key.p[0] = s->tile_cnt.p;
     key.p[1] = s->tile_off.p;
     key.p[2] = s->scan_tmp.p;

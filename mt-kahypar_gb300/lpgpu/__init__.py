@@ -22,6 +22,25 @@ U8P = ctypes.POINTER(ctypes.c_uint8)
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_ADMISSION, ERR_TIMEOUT, ERR_CUDA, ERR_NO_DEVICE, ERR_STATE = range(8)
 MAX_K = 1024
 FLAG_NO_GRAPH = 1
+FLAG_PERSISTENT = 2
+FLAG_MULTI_LAUNCH = 4
+PERSISTENT_MAX_K = 64
+MODE_MULTI_LAUNCH, MODE_PERSISTENT = 0, 1
+# tuning table written by lpgpu.autotune on a GB300 (loaded with the library)
+TUNING_PATH = os.path.join(HERE, "tuning_gb300.json")
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("unroll", ctypes.c_int32),
+                ("order", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class TuningEntry(ctypes.Structure):
+    _fields_ = [("max_mean_pins", ctypes.c_int64), ("min_instances", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("tuning", Tuning)]
 
 
 class Config(ctypes.Structure):
@@ -83,7 +102,8 @@ SYMBOLS = [
     "lpgpu_session_set_partition_instances", "lpgpu_session_get_partition_instances", "lpgpu_read_hgr",
     "lpgpu_free", "lpgpu_read_partition", "lpgpu_write_partition", "lpgpu_session_init_gain_cache",
     "lpgpu_session_drop_gain_cache", "lpgpu_session_project_partition", "lpgpu_session_rebalance",
-    "lpgpu_session_repair_empty_blocks",
+    "lpgpu_session_repair_empty_blocks", "lpgpu_set_tuning_table", "lpgpu_session_set_tuning",
+    "lpgpu_session_tuning",
 ]
 
 
@@ -103,7 +123,27 @@ def lib():
         L.lpgpu_host_alloc.argtypes = [ctypes.c_size_t]
         L.lpgpu_host_free.argtypes = [ctypes.c_void_p]
         _lib = L
+        if os.path.exists(TUNING_PATH):
+            load_tuning(TUNING_PATH)
     return _lib
+
+
+def set_tuning_table(rows):
+    """Process-wide tuning table (lpgpu_set_tuning_table): rows of dicts with
+    max_mean_pins, min_instances, mode, ctas_per_sm, unroll, order."""
+    arr = (TuningEntry * max(1, len(rows)))()
+    for i, r in enumerate(rows):
+        arr[i].max_mean_pins = int(r["max_mean_pins"])
+        arr[i].min_instances = int(r["min_instances"])
+        arr[i].tuning = Tuning(int(r["mode"]), int(r["ctas_per_sm"]), int(r["unroll"]), int(r["order"]))
+    _check(lib().lpgpu_set_tuning_table(arr, ctypes.c_int32(len(rows))))
+
+
+def load_tuning(path=TUNING_PATH):
+    """Loads an autotuner table (JSON with an "entries" list) into the library."""
+    import json
+    with open(path) as f:
+        set_tuning_table(json.load(f)["entries"])
 
 
 def _check(status):
@@ -333,6 +373,21 @@ class Session:
         r = Result()
         _check(lib().lpgpu_session_rebalance(self._h, ctypes.c_int32(max_rounds), ctypes.byref(r)))
         return r
+
+    def set_tuning(self, mode=None, ctas_per_sm=1, unroll=4, order=0):
+        """Per-session tuning (lpgpu_session_set_tuning); mode None: back to the table."""
+        if mode is None:
+            _check(lib().lpgpu_session_set_tuning(self._h, None))
+        else:
+            t = Tuning(int(mode), int(ctas_per_sm), int(unroll), int(order))
+            _check(lib().lpgpu_session_set_tuning(self._h, ctypes.byref(t)))
+        return self
+
+    def tuning(self):
+        """The tuning the next refine uses (lpgpu_session_tuning)."""
+        t = Tuning()
+        _check(lib().lpgpu_session_tuning(self._h, ctypes.byref(t)))
+        return t.as_dict()
 
     def repair_empty_blocks(self):
         """Moves of repairEmptyBlocks (lpgpu_session_repair_empty_blocks), not applied:
