@@ -26,6 +26,13 @@ built here (TBB legacy task API, hwloc, Boost, un-vendored submodule), so its
 CPU restatement runs with all host threads on the same workload, one full
 refinement per step.
 
+Systems workloads (default run, one GPU; `--no-systems` skips them; also
+alone with `--workload batch|served`): `batch`, 4,096 small hypergraphs refined
+together (persistent rounds when the tuning table picks them) against the
+plain one-instance-per-call loop; `served`, 256 Poisson-arriving requests
+through the round-granular server against the plain sequential loop (p50,
+p99, throughput). Both check that every result is identical.
+
 Multi-GPU: the path runs as independent replicas (one instance per rank, no
 collective); `value` is the sum over ranks of pins / the max step time.
 """
@@ -59,9 +66,9 @@ def parse_args():
     ap.add_argument("--instances", type=int, default=None,
                     help="batch: instances (default 4096); served: requests (default 256)")
     ap.add_argument("--rate", type=float, default=2000.0, help="served: Poisson arrival rate (req/s)")
-    ap.add_argument("--slots", type=int, default=2, help="served: concurrent batched sessions")
-    ap.add_argument("--batch-pins", type=float, default=1e8,
-                    help="served: a batch stops growing at this many pins (0: memory budget only)")
+    ap.add_argument("--slots", type=int, default=2, help="served: solo lanes for large requests")
+    ap.add_argument("--no-systems", action="store_true",
+                    help="default run: skip the batched and served measurements")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--subrounds", type=int, default=7)
     ap.add_argument("--no-baseline", action="store_true", help="skip the CPU baseline leg")
@@ -354,11 +361,22 @@ def gpu_arm(args):
             "phases_ms_per_step": {k: round(v[1] / args.steps, 3) for k, v in sorted(phase_tot.items())},
             "quality": {"km1_before": r0.km1_before, "km1_after": r0.km1_after, "delta": r0.delta,
                         "moves": r0.moves, "imbalance": r0.imbalance, "rounds": r0.rounds}}
+    s.close()
+    ok = True
+    if not args.no_systems and world == 1:
+        # the batched (4,096 small hypergraphs) and served (Poisson requests)
+        # workloads, measured in the same run and reported as extra keys
+        from lpgpu import gen
+        batch_insts = gen.generate_many("batch_instance", args.seed, 4096)
+        line["batch"] = batch_measure(args, batch_insts, plain_modes=(None,))
+        del batch_insts
+        served_insts = gen.generate_many("served_request", args.seed, 256)
+        line["served"] = served_measure(args, served_insts)
+        ok = line["batch"]["km1_identical"] and line["served"]["identical_results"]
     if rank == 0:
         print(json.dumps(line), flush=True)
-    s.close()
     dist.close()
-    return 0
+    return 0 if ok else 1
 
 
 def e2e_leg(args, inst, cfg, device, dist):
@@ -422,20 +440,20 @@ def pinned_instances(lpgpu, gen, insts):
     return hgs, parts, outs, (a_off, a_pin, a_wv, a_we, a_pt, a_out)
 
 
-def batch_arm(args):
-    """Many small hypergraphs (vertex counts log-uniform in [1,024, 65,536], nets 1.1x,
-    geometric net sizes, k in {2,4,8,16}): one batched session refining all of them
-    together vs. the plain loop (one instance per call sequence), both end to end
-    from host buffers (upload, set partition, 5 rounds, download). Per-instance km1
-    must be identical."""
+def batch_measure(args, insts, plain_modes=(0, None)):
+    """Many small hypergraphs refined by one batched session (the tuned form,
+    persistent rounds when the tuning table picks them) vs the plain loop (one
+    instance per call sequence), both end to end from page-locked host buffers
+    (upload, set partition, 5 rounds, download); device-resident refines of
+    both the persistent and the multi-launch form from the same start. Every
+    instance's km1 must be identical in all of them."""
     import lpgpu
     from lpgpu import I32P, _check, gen, lib
-    insts = gen.generate_many("batch_instance", args.seed, args.instances or 4096)  # before any CUDA call
-    lpgpu.build()
     hgs, parts, outs, arenas = pinned_instances(lpgpu, gen, insts)
     ks = [x.k for x in insts]
     cfg = lpgpu.default_config(rounds=5, subrounds=args.subrounds)
     pins_total = sum(h.num_pins for h in hgs)
+    steps = max(1, min(args.steps, 5))
 
     def batched_once(s):
         s.upload_instances(hgs)
@@ -445,31 +463,36 @@ def batch_arm(args):
         return r.pins_processed, s.instance_km1()
 
     with lpgpu.Session(0) as s:
-        for _ in range(max(1, args.warmup)):
-            batched_once(s)
+        batched_once(s)
+        tuning = s.tuning()
         t0 = time.perf_counter()
-        bp = 0
-        for _ in range(args.steps):
-            p, km_b = batched_once(s)
-            bp += p
-        t_batch = (time.perf_counter() - t0) / args.steps
-        # device-resident refine only (inputs in HBM): one refine per step from the same start
+        for _ in range(steps):
+            _, km_b = batched_once(s)
+        t_batch = (time.perf_counter() - t0) / steps
+        # device-resident refines (inputs in HBM), both forms, from the same start
+        s.set_partition_instances(ks, parts, eps=0.03)
         s.save_partition()
-        for _ in range(2):
+        dev = {}
+        for name, flags in (("persistent", lpgpu.FLAG_PERSISTENT), ("multi_launch", lpgpu.FLAG_MULTI_LAUNCH)):
+            dcfg = lpgpu.default_config(rounds=5, subrounds=args.subrounds, flags=flags)
             s.restore_partition()
-            s.refine(cfg)
-        s.synchronize()
-        s.record(0)
-        for _ in range(args.steps):
-            s.restore_partition()
-            r = s.refine(cfg)
-        s.record(1)
-        t_dev = s.elapsed_ms(0, 1) / 1e3 / args.steps
-        dev_pins = r.pins_processed
-
+            s.refine(dcfg)
+            ms = 0.0
+            for _ in range(steps):
+                s.restore_partition()
+                s.synchronize()
+                s.record(0)
+                r = s.refine(dcfg)
+                s.record(1)
+                ms += s.elapsed_ms(0, 1)
+            km_d = s.instance_km1()
+            dev[name] = {"ms_per_refine": ms / steps, "pins_per_s": r.pins_processed / (ms / steps / 1e3),
+                         "km1_identical": bool(np.array_equal(km_d, km_b))}
     best_plain = None
-    for flags in (0, lpgpu.FLAG_NO_GRAPH):
-        pcfg = lpgpu.default_config(rounds=5, subrounds=args.subrounds, flags=flags)
+    for flags in plain_modes:
+        if flags is None:
+            flags = lpgpu.FLAG_NO_GRAPH
+        pcfg = lpgpu.default_config(rounds=5, subrounds=args.subrounds, flags=flags | lpgpu.FLAG_MULTI_LAUNCH)
         with lpgpu.Session(0) as s:
             km_p = np.zeros(len(insts), np.int64)
             pp = 0
@@ -485,60 +508,78 @@ def batch_arm(args):
         if best_plain is None or t_plain < best_plain[0]:
             best_plain = (t_plain, flags, km_p, pp)
     t_plain, flags, km_p, pp = best_plain
-    same = bool(np.array_equal(km_b, km_p))
-    line = {"metric": "batched LP refinement throughput (pins processed per second, end to end)",
-            "value": (bp / args.steps) / t_batch, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * t_batch, "higher_is_better": True,
+    same = bool(np.array_equal(km_b, km_p)) and all(d["km1_identical"] for d in dev.values())
+    nominal = pins_total * 5
+    return {"workload": f"{len(insts)} independent hypergraphs, {sum(h.n for h in hgs)} vertices, "
+                        f"{pins_total} pins in total, k in {{2,4,8,16}}, 5 rounds",
+            "e2e_ms_per_step": 1e3 * t_batch, "e2e_pins_per_s": nominal / t_batch, "tuning": tuning,
+            "device_resident": dev,
+            "plain_loop": {"ms_per_step": 1e3 * t_plain, "pins_per_s": nominal / t_plain,
+                           "launch_mode": "direct" if flags & lpgpu.FLAG_NO_GRAPH else "graph"},
+            "speedup_vs_plain_loop": t_plain / t_batch, "km1_identical": same, "km1_total": int(km_b.sum())}
+
+
+def batch_arm(args):
+    import lpgpu
+    from lpgpu import gen
+    insts = gen.generate_many("batch_instance", args.seed, args.instances or 4096)  # before any CUDA call
+    lpgpu.build()
+    b = batch_measure(args, insts)
+    line = {"metric": "batched LP refinement throughput (pins per LP round per second, end to end)",
+            "value": b["e2e_pins_per_s"], "unit": UNIT, "n_gpus": 1, "steps": max(1, min(args.steps, 5)),
+            "warmup": 1, "ms_per_step": b["e2e_ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": f"{len(insts)} independent hypergraphs, {sum(h.n for h in hgs)} vertices, "
-                                   f"{pins_total} pins in total, k in {{2,4,8,16}}, 5 rounds",
-                       "subrounds": args.subrounds},
-            "device_resident": {"value": dev_pins / t_dev, "ms_per_step": 1e3 * t_dev},
-            "plain_loop": {"value": pp / t_plain, "ms_per_step": 1e3 * t_plain,
-                           "launch_mode": "direct" if flags else "graph"},
-            "speedup_vs_plain_loop": t_plain / t_batch, "km1_identical": same,
-            "km1_total": int(km_b.sum())}
+            "config": {"workload": b["workload"], "subrounds": args.subrounds}, **b}
     print(json.dumps(line), flush=True)
-    return 0 if same else 1
+    return 0 if b["km1_identical"] else 1
 
 
-def served_arm(args):
+def served_measure(args, insts):
     """Refine requests arriving as a Poisson stream (vertex counts log-uniform in
-    [1,024, 2,097,152], Zipf nets, k in {2..64}, 8 rounds): the continuous-batching
-    server vs. the plain sequential loop on the same arrival times. Reports p50/p99
-    latency and throughput; every request's km1 must be identical."""
+    [1,024, 2,097,152], Zipf nets, k in {2..64}, 8 rounds): the round-granular
+    continuous-batching server vs the plain sequential loop on the same arrival
+    times, requests in page-locked host buffers. Every request's partition must
+    be identical."""
     import lpgpu
     from lpgpu import gen, serve
-    insts = gen.generate_many("served_request", args.seed, args.instances or 256)  # before any CUDA call
-    lpgpu.build()
     arr = serve.poisson_arrivals(len(insts), args.rate, args.seed)
-    # requests arrive in page-locked host buffers (both arms read the same ones)
     hgs, parts, _, arenas = pinned_instances(lpgpu, gen, insts)
 
     def requests():
         return [serve.Request(i, hgs[i], x.k, x.eps, parts[i], x.rounds, float(arr[i])) for i, x in enumerate(insts)]
 
-    # warm-up: one small batch through a server and one plain call
     warm = [serve.Request(0, hgs[0], insts[0].k, insts[0].eps, parts[0], insts[0].rounds, 0.0)]
-    serve.replay(serve.RefineServer(slots=args.slots), warm)
-    serve.plain_loop(warm)
+    serve.replay(serve.RefineServer(solo_slots=args.slots, subrounds=args.subrounds), warm)
+    serve.plain_loop(warm, subrounds=args.subrounds)
     rs = requests()
-    cap = int(args.batch_pins) if args.batch_pins and args.batch_pins > 0 else None
-    st_s = serve.replay(serve.RefineServer(slots=args.slots, subrounds=args.subrounds, max_batch_pins=cap), rs)
+    srv = serve.RefineServer(solo_slots=args.slots, subrounds=args.subrounds)
+    st_s = serve.replay(srv, rs)
     rp = requests()
     st_p = serve.plain_loop(rp, subrounds=args.subrounds)
     same = all(a.km1 == b.km1 and np.array_equal(a.result, b.result) for a, b in zip(rs, rp))
     ss, sp = st_s.summary(), st_p.summary()
-    line = {"metric": "served LP refinement p99 latency (Poisson arrivals)", "value": ss["p99_ms"], "unit": "ms",
-            "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": False, "scaling": "weak",
+    return {"workload": f"{len(insts)} requests at {args.rate:.0f} req/s, "
+                        f"{sum(x.hg.num_pins for x in insts)} pins in total, 8 rounds each",
+            "solo_slots": args.slots, "large_pins": srv.large_pins, "budget_gb": 150,
+            "server": ss, "plain_loop": sp, "p50_ratio": ss["p50_ms"] / sp["p50_ms"],
+            "p99_ratio": ss["p99_ms"] / sp["p99_ms"], "throughput_ratio": ss["req_per_s"] / sp["req_per_s"],
+            "identical_results": same, "errors": len(srv.errors),
+            "error_samples": [f"{rids}: {exc}" for rids, exc in srv.errors[:5]]}
+
+
+def served_arm(args):
+    import lpgpu
+    from lpgpu import gen
+    insts = gen.generate_many("served_request", args.seed, args.instances or 256)  # before any CUDA call
+    lpgpu.build()
+    v = served_measure(args, insts)
+    line = {"metric": "served LP refinement p99 latency (Poisson arrivals)", "value": v["server"]["p99_ms"],
+            "unit": "ms", "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": f"{len(insts)} requests at {args.rate:.0f} req/s, "
-                                   f"{sum(x.hg.num_pins for x in insts)} pins in total, 8 rounds each",
-                       "slots": args.slots, "budget_gb": 150, "subrounds": args.subrounds,
-                       "batch_pins": cap, "inputs": "page-locked host buffers"},
-            "server": ss, "plain_loop": sp, "identical_results": same}
+            "config": {"workload": v["workload"], "subrounds": args.subrounds, "inputs": "page-locked host buffers"},
+            **v}
     print(json.dumps(line), flush=True)
-    return 0 if same else 1
+    return 0 if v["identical_results"] else 1
 
 
 def main():

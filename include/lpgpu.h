@@ -284,6 +284,41 @@ LPGPU_API lpgpu_status lpgpu_set_tuning_table(const lpgpu_tuning_entry* entries,
 LPGPU_API lpgpu_status lpgpu_session_set_tuning(lpgpu_session* s, const lpgpu_tuning* tuning);
 LPGPU_API lpgpu_status lpgpu_session_tuning(lpgpu_session* s, lpgpu_tuning* out);
 
+/* ------------------------------------------------------- stepped rounds
+ *
+ * Continuous batching at round granularity (no counterpart in the
+ * reference, which refines one hypergraph per call): each request lives in
+ * its own session; lpgpu_stepper_launch runs the next LP round of every
+ * listed session in one persistent launch per group of equal round
+ * parameters on the stepper's own stream, so sessions may join the list or
+ * leave it between any two rounds, and each one ends exactly as
+ * lpgpu_session_refine would leave it. The stepper's stream waits for the
+ * work each session enqueued before the launch, and each session's stream
+ * waits for the round, so uploads and downloads of other sessions overlap
+ * with it. */
+typedef struct lpgpu_stepper_s lpgpu_stepper;
+
+LPGPU_API lpgpu_status lpgpu_stepper_create(int32_t device, lpgpu_stepper** out);
+LPGPU_API lpgpu_status lpgpu_stepper_destroy(lpgpu_stepper* stepper);
+
+/* Starts a stepped refinement of the session's partition with cfg (its
+ * rounds are the session's round budget): the round-0 active set, cleared
+ * statistics and km1 before. Every k must be <= LPGPU_PERSISTENT_MAX_K. */
+LPGPU_API lpgpu_status lpgpu_session_begin_rounds(lpgpu_session* s, const lpgpu_config* cfg);
+
+/* Enqueues the next round of every listed session (each begun and not done,
+ * listed once) and returns without waiting. */
+LPGPU_API lpgpu_status lpgpu_stepper_launch(lpgpu_stepper* stepper, lpgpu_session* const* sessions,
+                                            int32_t count);
+
+/* Waits for the launched round; done[i] = 1 when session i of the launch has
+ * used its round budget or its last round found no active vertex. */
+LPGPU_API lpgpu_status lpgpu_stepper_wait(lpgpu_stepper* stepper, int32_t* done);
+
+/* Ends a stepped refinement: the refine result and per-round statistics
+ * (lpgpu_session_round_stats) as lpgpu_session_refine gives them. */
+LPGPU_API lpgpu_status lpgpu_session_end_rounds(lpgpu_session* s, lpgpu_result* result);
+
 /* Statistics of the last refine: up to max_rounds records, returns the count in *rounds. */
 LPGPU_API lpgpu_status lpgpu_session_round_stats(lpgpu_session* s, lpgpu_round_stats* out,
                                                  int32_t max_rounds, int32_t* rounds);

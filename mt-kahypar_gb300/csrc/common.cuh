@@ -347,6 +347,8 @@ struct PxParams {
 // the 1- or 2-CTA-per-SM build of the kernel.
 cudaError_t launch_px_round(const Launch& L, const PxInst* insts, const int32_t* order, int32_t count,
                             const PxParams& P, int W, bool unit, int ctas_per_sm, int64_t* queue);
+// out[i]: active vertices of instance i's round `insts[i].round` (from its statistics).
+cudaError_t launch_px_active(const Launch& L, const PxInst* insts, int32_t count, int64_t* out);
 
 // Optional per-phase CUDA-event timing.
 struct PhaseTimer {

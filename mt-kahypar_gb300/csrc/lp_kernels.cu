@@ -5,6 +5,9 @@
 // element counts from device memory (so a whole refine needs no host sync),
 // and privatize per-block accumulators in shared memory.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "common.cuh"
 
@@ -70,6 +73,24 @@ static int grid_for(const Launch& L, int64_t work_items, int threads, int per_sm
   const int64_t cap = (int64_t)L.num_sms * (per_sm > 0 ? per_sm : blocks_per_sm_hint);
   const int64_t need = (work_items + threads - 1) / threads;
   return (int)std::max<int64_t>(1, std::min<int64_t>(cap, need));
+}
+
+// Raises a kernel's dynamic shared memory limit on the current device to at
+// least `bytes`. The limit belongs to the kernel, not to the launch, and
+// sessions driven from several host threads launch the same kernel with
+// different sizes: it only ever grows, under a lock, so that no thread lowers
+// it below the size another thread is about to launch with.
+template <typename Kernel>
+static void allow_dyn_smem(Kernel kern_fn, size_t bytes) {
+  const void* kern = (const void*)kern_fn;
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> limits;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = limits[{dev, kern}];
+  if (bytes > cur && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess)
+    cur = bytes;
 }
 
 // Resident CTAs per SM of `kern` (at least 1).
@@ -1365,7 +1386,7 @@ static cudaError_t launch_sweep(const Launch& L, const RoundCtx& c, int round, i
   const size_t smem = sweep_smem(c.batched ? 0 : c.k, c.W, c.batched != 0);
   LPGPU_DISPATCH_W(c.W, {
     auto kern = c.unit_nets ? k_sweep<kW, true> : k_sweep<kW, false>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_dyn_smem(kern, smem);
     const int per_sm = occupancy((const void*)kern, kSweepThreads, smem);
     int grid = grid_for(L, c.n * 4, kSweepThreads, per_sm);
     // CTAs for the heavy vertices: their share of the work, at least two
@@ -1437,7 +1458,7 @@ __global__ void __launch_bounds__(256) k_gain_cache(RoundCtx c, int32_t* benefit
 cudaError_t launch_gain_cache(const Launch& L, const RoundCtx& c, int32_t* benefit, int32_t* penalty) {
   if (c.n == 0) return cudaSuccess;
   const size_t smem = sizeof(int) * c.k * 8;
-  cudaFuncSetAttribute(k_gain_cache, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  allow_dyn_smem(k_gain_cache, smem);
   k_gain_cache<<<grid_for(L, c.n * 32, 256), 256, smem, L.st>>>(c, benefit, penalty);
   LAUNCHED("k_gain_cache");
   return cudaGetLastError();
@@ -3077,7 +3098,7 @@ cudaError_t launch_repair_candidates(const Launch& L, const RoundCtx& c, int blk
   const int g = grid_for(L, c.n, 256);
   k_repair_keys<<<g, 256, 0, L.st>>>(c, blk, keys, ws);
   LAUNCHED("k_repair_keys");
-  cudaFuncSetAttribute(k_repair_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
+  allow_dyn_smem(k_repair_select, kSelSmem);
   k_repair_select<<<1, kSelThreads, kSelSmem, L.st>>>(keys, ws, c.n, c.k,
                                                       reinterpret_cast<uint64_t*>(scratch + 1));
   LAUNCHED("k_repair_select");
@@ -3093,7 +3114,7 @@ cudaError_t launch_rebalance_round(const Launch& L, const RoundCtx& c, int round
   cudaError_t e = cudaMemsetAsync(rb, 0, sizeof(int64_t) * 2 * k, L.st);
   if (e != cudaSuccess) return e;
   const size_t smem = sizeof(int) * k * 8;
-  cudaFuncSetAttribute(k_rb_candidates, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  allow_dyn_smem(k_rb_candidates, smem);
   k_rb_candidates<<<grid_for(L, c.n * 32, 256), 256, smem, L.st>>>(c, round, rb_to, rb_score, rb);
   LAUNCHED("k_rb_candidates");
   k_rb_src_plan<<<1, 1024, 0, L.st>>>(c, rb);
@@ -3101,7 +3122,7 @@ cudaError_t launch_rebalance_round(const Launch& L, const RoundCtx& c, int round
   const int g = grid_for(L, c.n, 256);
   k_rb_src_bin<<<g, 256, 0, L.st>>>(c, rb_to, rb_score, rb);
   LAUNCHED("k_rb_src_bin");
-  cudaFuncSetAttribute(k_rb_src_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
+  allow_dyn_smem(k_rb_src_select, kSelSmem);
   k_rb_src_select<<<(unsigned)std::min<int64_t>(k, 4 * (int64_t)L.num_sms), kSelThreads, kSelSmem, L.st>>>(c, rb);
   LAUNCHED("k_rb_src_select");
   k_rb_emit<<<g, 256, 0, L.st>>>(c, rb_to, rb_score, rb);
@@ -3109,7 +3130,7 @@ cudaError_t launch_rebalance_round(const Launch& L, const RoundCtx& c, int round
   // the LP target-side selection, source floor and commit of one sub-round
   k_bin_moves<<<grid_for(L, c.n, kBinThreads), kBinThreads, 0, L.st>>>(c, 0);
   LAUNCHED("k_bin_moves");
-  cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
+  allow_dyn_smem(k_select, kSelSmem);
   k_select<<<(unsigned)std::min<int64_t>(k, 4 * (int64_t)L.num_sms), kSelThreads, kSelSmem, L.st>>>(c, 0);
   LAUNCHED("k_select");
   const size_t dw_smem = sizeof(ull) * k;
@@ -3141,7 +3162,7 @@ cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int s
     Scope sc(timer, "select");
     k_bin_moves<<<g_bin, kBinThreads, 0, L.st>>>(c, sub);
     LAUNCHED("k_bin_moves");
-    cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSelSmem);
+    allow_dyn_smem(k_select, kSelSmem);
     k_select<<<(unsigned)std::min<int64_t>(k, 4 * (int64_t)L.num_sms), kSelThreads, kSelSmem, L.st>>>(c, sub);
     LAUNCHED("k_select");
   }
@@ -3611,6 +3632,21 @@ static const void* px_kernel_for(int W, bool unit, int unroll, int minb) {
   return unit ? px_kernel_wu<2, true>(unroll, minb) : px_kernel_wu<2, false>(unroll, minb);
 }
 
+// Active vertices of every instance's last persistent round (its round's
+// statistics), for the host's stop rule.
+__global__ void k_px_active(const PxInst* __restrict__ insts, int32_t count, int64_t* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    const PxInst& I = insts[i];
+    out[i] = I.stats[(int64_t)I.round * kStats + kStActive];
+  }
+}
+
+cudaError_t launch_px_active(const Launch& L, const PxInst* insts, int32_t count, int64_t* out) {
+  if (count <= 0) return cudaSuccess;
+  k_px_active<<<(count + 255) / 256, 256, 0, L.st>>>(insts, count, out);
+  return launched("k_px_active");
+}
+
 cudaError_t launch_px_round(const Launch& L, const PxInst* insts, const int32_t* order, int32_t count,
                             const PxParams& P, int W, bool unit, int ctas_per_sm, int64_t* queue) {
   if (count <= 0) return cudaSuccess;
@@ -3619,7 +3655,7 @@ cudaError_t launch_px_round(const Launch& L, const PxInst* insts, const int32_t*
   if (e != cudaSuccess) return e;
   const int minb = ctas_per_sm >= 2 ? 2 : 1;
   const void* kern = px_kernel_for(W, unit, P.unroll, minb);
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPxSmem);
+  allow_dyn_smem(kern, kPxSmem);
   const int occ = std::max(1, occupancy(kern, kPxThreads, kPxSmem));
   const int per_sm = std::min(minb, occ);
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(count, (int64_t)per_sm * L.num_sms));

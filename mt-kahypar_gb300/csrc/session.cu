@@ -4,6 +4,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -180,6 +181,13 @@ struct lpgpu_session_s {
   std::vector<int64_t> px_key;
   bool has_tuning = false;
   lpgpu_tuning tuning{};
+  std::vector<PxInst> h_px;  // host copy of the descriptors
+  // stepped refinement (lpgpu_session_begin_rounds, lpgpu_stepper_*)
+  bool stepping = false, step_done = false;
+  lpgpu_config step_cfg{};
+  int32_t step_round = 0;
+  int64_t step_km1_before = 0;
+  cudaEvent_t step_ev = nullptr;
   DevBuf<int32_t> vinst, inst_boff, inst_k, over_ids;
   DevBuf<int64_t> inst_voff, inst_noff, inst_delta;
   DevBuf<int64_t> vout;  // result words of the device-side input checks
@@ -472,6 +480,7 @@ lpgpu_status lpgpu_session_destroy(lpgpu_session* s) {
     for (auto& ev : s->slots)
       if (ev) cudaEventDestroy(ev);
     if (s->graph) cudaGraphExecDestroy(s->graph);
+    if (s->step_ev) cudaEventDestroy(s->step_ev);
     cudaStreamSynchronize(s->st);
     cudaMemPoolDestroy(s->mem.pool);
     cudaStreamDestroy(s->st);
@@ -977,6 +986,7 @@ static lpgpu_status build_px(lpgpu_session* s, int order) {
   CK(s->px.alloc(I, fp));
   CK(s->px_order.alloc(I, fp));
   CK(cudaMemcpyAsync(s->px.p, h.data(), sizeof(PxInst) * I, cudaMemcpyHostToDevice, s->st));
+  s->h_px = h;
   CK(cudaMemcpyAsync(s->px_order.p, ord.data(), sizeof(int32_t) * I, cudaMemcpyHostToDevice, s->st));
   CK(cudaStreamSynchronize(s->st));
   s->px_key = key;
@@ -1003,6 +1013,46 @@ lpgpu_status lpgpu_session_set_tuning(lpgpu_session* s, const lpgpu_tuning* t) {
 lpgpu_status lpgpu_session_tuning(lpgpu_session* s, lpgpu_tuning* out) {
   if (!s || !out) return invalid("null argument");
   *out = session_tuning(s);
+  return LPGPU_OK;
+}
+
+// Statistics of R rounds (hs: R x kStats, rounds after the first one without
+// an active vertex did not run) into last_stats and the refine result
+// (IRefiner::refine's metrics update, label_propagation_refiner.cpp:48-67).
+static lpgpu_status book_rounds(lpgpu_session* s, const std::vector<int64_t>& hs, int R, int64_t km1_before,
+                                lpgpu_result* result) {
+  s->last_stats.clear();
+  int executed = 0;
+  bool stopped = false;
+  int64_t delta = 0, moves = 0, pins = 0;
+  for (int r = 0; r < R; ++r) {
+    const int64_t* x = &hs[(size_t)r * kStats];
+    if (x[kStActive] == 0) stopped = true;
+    if (stopped) continue;
+    lpgpu_round_stats rs{x[kStActive], x[kStPins],  x[kStCands],     x[kStMoved],
+                         x[kStReverted], x[kStDelta], x[kStMovedPins], x[kStToggles]};
+    s->last_stats.push_back(rs);
+    ++executed;
+    delta += rs.delta;
+    moves += rs.moved;
+    pins += rs.pins;
+  }
+  if (result) {
+    int64_t km1_after = 0;
+    lpgpu_status ms = read_metrics(s, &km1_after, nullptr);
+    if (ms != LPGPU_OK) return ms;
+    double imb = 0;
+    ms = read_imbalance(s, &imb);
+    if (ms != LPGPU_OK) return ms;
+    result->km1_before = km1_before;
+    result->km1_after = km1_after;
+    result->delta = delta;
+    result->moves = moves;
+    result->pins_processed = pins;
+    result->rounds = executed;
+    result->improved = delta < 0;
+    result->imbalance = imb;
+  }
   return LPGPU_OK;
 }
 
@@ -1173,38 +1223,232 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
       s->phase_times.push_back(t);
     }
   }
-  s->last_stats.clear();
-  int executed = 0;
-  bool stopped = false;
-  int64_t delta = 0, moves = 0, pins = 0;
-  for (int r = 0; r < R; ++r) {
-    const int64_t* x = &hs[r * kStats];
-    if (x[kStActive] == 0) stopped = true;
-    if (stopped) continue;
-    lpgpu_round_stats rs{x[kStActive], x[kStPins],  x[kStCands],     x[kStMoved],
-                         x[kStReverted], x[kStDelta], x[kStMovedPins], x[kStToggles]};
-    s->last_stats.push_back(rs);
-    ++executed;
-    delta += rs.delta;
-    moves += rs.moved;
-    pins += rs.pins;
+  return book_rounds(s, hs, R, km1_before, result);
+}
+
+// ---- stepped refinement: one persistent round of many sessions per launch
+
+lpgpu_status lpgpu_session_begin_rounds(lpgpu_session* s, const lpgpu_config* cfg_in) {
+  lpgpu_status ps = need_part(s);
+  if (ps != LPGPU_OK) return ps;
+  lpgpu_config cfg;
+  if (cfg_in) cfg = *cfg_in; else lpgpu_config_default(&cfg);
+  if (cfg.rounds < 0) return invalid("rounds must be >= 0");
+  if (cfg.subrounds < 1 || cfg.subrounds > kMaxSubrounds) return invalid("subrounds must be in [1, 64]");
+  if ((s->batched ? s->kmax : s->k) > kPxMaxK) return invalid("stepped rounds need every k <= 64");
+  DeviceGuard g(s->device);
+  s->gc_valid = false;
+  const int R = cfg.rounds;
+  cudaStream_t st = s->st;
+  CK(s->stats.alloc(std::max(1, R) * kStats, &s->mem));
+  ps = build_px(s, 0);
+  if (ps != LPGPU_OK) return ps;
+  ps = read_metrics(s, &s->step_km1_before, nullptr);
+  if (ps != LPGPU_OK) return ps;
+  if (!s->step_ev) CK(cudaEventCreateWithFlags(&s->step_ev, cudaEventDisableTiming));
+  RoundCtx c = s->ctx(&cfg);
+  CK(cudaMemsetAsync(s->stats.p, 0, sizeof(int64_t) * std::max(1, R) * kStats, st));
+  if (s->m > 0) CK(cudaMemsetAsync(s->net_epoch.p, 0, sizeof(int32_t) * s->m, st));
+  if (s->n > 0) CK(cudaMemsetAsync(s->next_flag.p, 0, s->n, st));
+  CK(launch_mark_all(s->launch(), c, cfg.rebalancing));
+  s->step_cfg = cfg;
+  s->step_round = 0;
+  s->step_done = R == 0;
+  s->stepping = true;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_session_end_rounds(lpgpu_session* s, lpgpu_result* result) {
+  if (!s) return invalid("null session");
+  if (!s->stepping) {
+    set_error("no stepped refinement was begun");
+    return LPGPU_ERR_STATE;
   }
-  if (result) {
-    int64_t km1_after = 0;
-    ms = read_metrics(s, &km1_after, nullptr);
-    if (ms != LPGPU_OK) return ms;
-    double imb = 0;
-    ms = read_imbalance(s, &imb);
-    if (ms != LPGPU_OK) return ms;
-    result->km1_before = km1_before;
-    result->km1_after = km1_after;
-    result->delta = delta;
-    result->moves = moves;
-    result->pins_processed = pins;
-    result->rounds = executed;
-    result->improved = delta < 0;
-    result->imbalance = imb;
+  DeviceGuard g(s->device);
+  const int R = s->step_cfg.rounds;
+  std::vector<int64_t> hs((size_t)std::max(1, R) * kStats);
+  CK(cudaMemcpyAsync(hs.data(), s->stats.p, sizeof(int64_t) * hs.size(), cudaMemcpyDeviceToHost, s->st));
+  if (s->n > 0) CK(cudaMemsetAsync(s->next_flag.p, 0, s->n, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  s->stepping = false;
+  return book_rounds(s, hs, R, s->step_km1_before, result);
+}
+
+}  // extern "C"
+
+struct lpgpu_stepper_s {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  int num_sms = 1;
+  Mem mem;
+  DevBuf<PxInst> table;
+  DevBuf<int64_t> active, queue;
+  cudaEvent_t ev = nullptr;
+  std::vector<lpgpu_session*> pending;  // sessions of the launched round
+  std::vector<int32_t> first;           // their first row of the table
+  std::vector<PxInst> h;
+};
+
+extern "C" {
+
+lpgpu_status lpgpu_stepper_create(int32_t device, lpgpu_stepper** out) {
+  if (!out) return invalid("null output pointer");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    set_error(std::string("no CUDA device: ") + cudaGetErrorString(e));
+    cudaGetLastError();
+    return LPGPU_ERR_NO_DEVICE;
   }
+  if (device < 0 || device >= count) return invalid("device index out of range");
+  DeviceGuard g(device);
+  auto* t = new lpgpu_stepper_s();
+  t->device = device;
+  cudaDeviceProp prop;
+  if ((e = cudaGetDeviceProperties(&prop, device)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&t->st, cudaStreamNonBlocking)) != cudaSuccess) {
+    delete t;
+    return cuda_fail(e, "stepper stream");
+  }
+  t->num_sms = prop.multiProcessorCount;
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  if ((e = cudaMemPoolCreate(&t->mem.pool, &props)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&t->ev, cudaEventDisableTiming)) != cudaSuccess) {
+    if (t->mem.pool) cudaMemPoolDestroy(t->mem.pool);
+    cudaStreamDestroy(t->st);
+    delete t;
+    return cuda_fail(e, "stepper pool");
+  }
+  t->mem.st = t->st;
+  *out = t;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_stepper_destroy(lpgpu_stepper* t) {
+  if (!t) return LPGPU_OK;
+  {
+    DeviceGuard g(t->device);
+    cudaStreamSynchronize(t->st);
+    t->table.release(&t->mem);
+    t->active.release(&t->mem);
+    t->queue.release(&t->mem);
+    cudaStreamSynchronize(t->st);
+    cudaEventDestroy(t->ev);
+    cudaMemPoolDestroy(t->mem.pool);
+    cudaStreamDestroy(t->st);
+  }
+  delete t;
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_stepper_launch(lpgpu_stepper* t, lpgpu_session* const* sessions, int32_t count) {
+  if (!t) return invalid("null stepper");
+  if (count < 0 || (count > 0 && !sessions)) return invalid("bad session list");
+  if (!t->pending.empty()) {
+    set_error("the previous round was not waited for");
+    return LPGPU_ERR_STATE;
+  }
+  for (int32_t i = 0; i < count; ++i) {
+    const lpgpu_session* s = sessions[i];
+    if (!s) return invalid("null session in the list");
+    if (!s->stepping || s->step_done) {
+      set_error("session " + std::to_string(i) + " has no round left to run");
+      return LPGPU_ERR_STATE;
+    }
+    if (s->device != t->device) return invalid("session on another device");
+    for (int32_t j = 0; j < i; ++j)
+      if (sessions[j] == s) return invalid("session listed twice");
+  }
+  DeviceGuard g(t->device);
+  // launches group the sessions whose round parameters agree
+  struct Group {
+    int W, unit, S, zero_gain, revert, rollback;
+    int64_t act;
+    bool operator<(const Group& o) const {
+      return std::tie(W, unit, S, zero_gain, revert, rollback, act) <
+             std::tie(o.W, o.unit, o.S, o.zero_gain, o.revert, o.rollback, o.act);
+    }
+  };
+  std::map<Group, std::vector<int32_t>> groups;
+  for (int32_t i = 0; i < count; ++i) {
+    const lpgpu_session* s = sessions[i];
+    const lpgpu_config& c = s->step_cfg;
+    Group key{s->W, s->unit_nets ? 1 : 0, c.subrounds, c.rebalancing ? 1 : 0, c.revert, c.rollback,
+              c.activation_threshold <= 0 ? INT64_MAX : (int64_t)c.activation_threshold};
+    groups[key].push_back(i);
+  }
+  t->h.clear();
+  t->first.assign(count, 0);
+  std::vector<std::pair<Group, std::pair<int32_t, int32_t>>> ranges;  // group, (first row, rows)
+  for (auto& kv : groups) {
+    const int32_t beg = (int32_t)t->h.size();
+    for (int32_t i : kv.second) {
+      lpgpu_session* s = sessions[i];
+      t->first[i] = (int32_t)t->h.size();
+      for (PxInst x : s->h_px) {
+        x.round = s->step_round;
+        t->h.push_back(x);
+      }
+      // the stepper's stream waits for the session's own work (uploads, begin)
+      CK(cudaEventRecord(s->step_ev, s->st));
+      CK(cudaStreamWaitEvent(t->st, s->step_ev, 0));
+    }
+    ranges.push_back({kv.first, {beg, (int32_t)t->h.size() - beg}});
+  }
+  const size_t rows = t->h.size();
+  if (rows > t->table.count) {
+    CK(t->table.alloc(rows, &t->mem));
+    CK(t->active.alloc(rows, &t->mem));
+  }
+  if (!t->queue.p) CK(t->queue.alloc(1, &t->mem));
+  if (rows > 0)
+    CK(cudaMemcpyAsync(t->table.p, t->h.data(), sizeof(PxInst) * rows, cudaMemcpyHostToDevice, t->st));
+  const Launch L{t->st, t->num_sms};
+  for (const auto& gr : ranges) {
+    const Group& k = gr.first;
+    // the kernel build of the group's first session's tuning when that is a
+    // persistent one, else 2 CTAs per SM with unroll 8
+    const lpgpu_tuning tu = session_tuning(sessions[groups[k].front()]);
+    const bool tuned = tu.mode == LPGPU_MODE_PERSISTENT;
+    PxParams P{};
+    P.S = k.S;
+    P.zero_gain = k.zero_gain;
+    P.revert = k.revert;
+    P.rollback = k.rollback;
+    P.act_threshold = k.act;
+    P.round = -1;  // every instance runs its own round
+    P.unroll = tuned ? tu.unroll : 8;
+    CK(launch_px_round(L, t->table.p + gr.second.first, nullptr, gr.second.second, P, k.W, k.unit != 0,
+                       tuned ? tu.ctas_per_sm : 2, t->queue.p));
+  }
+  if (rows > 0) CK(launch_px_active(L, t->table.p, (int32_t)rows, t->active.p));
+  // the sessions' later work (downloads, the next round's inputs) comes after this round
+  CK(cudaEventRecord(t->ev, t->st));
+  for (int32_t i = 0; i < count; ++i) CK(cudaStreamWaitEvent(sessions[i]->st, t->ev, 0));
+  t->pending.assign(sessions, sessions + count);
+  return LPGPU_OK;
+}
+
+lpgpu_status lpgpu_stepper_wait(lpgpu_stepper* t, int32_t* done) {
+  if (!t) return invalid("null stepper");
+  DeviceGuard g(t->device);
+  const size_t rows = t->h.size();
+  std::vector<int64_t> act(rows);
+  if (rows > 0) CK(cudaMemcpyAsync(act.data(), t->active.p, sizeof(int64_t) * rows, cudaMemcpyDeviceToHost, t->st));
+  CK(cudaStreamSynchronize(t->st));
+  for (size_t i = 0; i < t->pending.size(); ++i) {
+    lpgpu_session* s = t->pending[i];
+    int64_t a = 0;
+    for (size_t j = 0; j < s->h_px.size(); ++j) a += act[t->first[i] + j];
+    s->step_round += 1;
+    s->step_done = s->step_round >= s->step_cfg.rounds || a == 0;
+    if (done) done[i] = s->step_done ? 1 : 0;
+  }
+  t->pending.clear();
   return LPGPU_OK;
 }
 

@@ -103,7 +103,8 @@ SYMBOLS = [
     "lpgpu_free", "lpgpu_read_partition", "lpgpu_write_partition", "lpgpu_session_init_gain_cache",
     "lpgpu_session_drop_gain_cache", "lpgpu_session_project_partition", "lpgpu_session_rebalance",
     "lpgpu_session_repair_empty_blocks", "lpgpu_set_tuning_table", "lpgpu_session_set_tuning",
-    "lpgpu_session_tuning",
+    "lpgpu_session_tuning", "lpgpu_stepper_create", "lpgpu_stepper_destroy", "lpgpu_session_begin_rounds",
+    "lpgpu_stepper_launch", "lpgpu_stepper_wait", "lpgpu_session_end_rounds",
 ]
 
 
@@ -389,6 +390,17 @@ class Session:
         _check(lib().lpgpu_session_tuning(self._h, ctypes.byref(t)))
         return t.as_dict()
 
+    def begin_rounds(self, cfg: Config = None):
+        """Starts a stepped refinement (lpgpu_session_begin_rounds)."""
+        _check(lib().lpgpu_session_begin_rounds(self._h, None if cfg is None else ctypes.byref(cfg)))
+        return self
+
+    def end_rounds(self) -> Result:
+        """Result of a stepped refinement (lpgpu_session_end_rounds)."""
+        r = Result()
+        _check(lib().lpgpu_session_end_rounds(self._h, ctypes.byref(r)))
+        return r
+
     def repair_empty_blocks(self):
         """Moves of repairEmptyBlocks (lpgpu_session_repair_empty_blocks), not applied:
         a list of (vertex, from, to, gain) in empty-block order."""
@@ -455,6 +467,47 @@ class Session:
         cnt = ctypes.c_int32()
         _check(lib().lpgpu_session_phase_times(self._h, buf, 64, ctypes.byref(cnt)))
         return {buf[i].name.decode(): (buf[i].launches, buf[i].ms) for i in range(min(64, cnt.value))}
+
+
+class Stepper:
+    """Runs one LP round of many sessions per persistent launch (lpgpu_stepper_*)."""
+
+    def __init__(self, device: int = 0):
+        self._h = ctypes.c_void_p()
+        _check(lib().lpgpu_stepper_create(ctypes.c_int32(device), ctypes.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().lpgpu_stepper_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def launch(self, sessions):
+        """Enqueues the next round of every session in the list (no wait)."""
+        self._n = len(sessions)
+        arr = (ctypes.c_void_p * max(1, self._n))(*[x._h.value for x in sessions])
+        _check(lib().lpgpu_stepper_launch(self._h, arr, ctypes.c_int32(self._n)))
+
+    def wait(self):
+        """Waits for the launched round; one bool per session: its refinement is done."""
+        done = np.zeros(max(1, self._n), np.int32)
+        _check(lib().lpgpu_stepper_wait(self._h, _p(done, I32P)))
+        return done[:self._n].astype(bool)
+
+    def round(self, sessions):
+        self.launch(sessions)
+        return self.wait()
 
 
 def refine_km1(hg, k, part, eps=0.03, cfg: Config = None):

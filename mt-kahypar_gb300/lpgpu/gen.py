@@ -317,20 +317,22 @@ def random_small(seed, n=200, m=240, k=4, max_size=8, weighted=True, eps=0.03, r
     return Instance(f"random[{seed}]", hg, k, eps, part, rounds)
 
 
-def _one(name, seed, idx):
-    return globals()[name](seed, idx, incidence=False)
+def _one(name, seed, idx, kw=None):
+    return globals()[name](seed, idx, incidence=False, **(kw or {}))
 
 
-def generate_many(name, seed, count, processes=None):
-    """Instances idx = 0..count-1 of `batch_instance` / `served_request`, built in a
-    spawn-context process pool (safe after a CUDA context exists)."""
+def generate_many(name, seed, count, processes=None, **kw):
+    """Instances idx = 0..count-1 of `batch_instance` / `served_request` (extra
+    keyword arguments passed on), built in a spawn-context process pool (safe
+    after a CUDA context exists; the calling script needs a main guard)."""
     import multiprocessing as mp
     import os
     procs = processes or min(count, os.cpu_count() or 1)
     if procs <= 1:
-        return [_one(name, seed, i) for i in range(count)]
+        return [_one(name, seed, i, kw) for i in range(count)]
     with mp.get_context("spawn").Pool(procs) as pool:
-        return pool.starmap(_one, [(name, seed, i) for i in range(count)], chunksize=max(1, count // (4 * procs)))
+        return pool.starmap(_one, [(name, seed, i, kw) for i in range(count)],
+                            chunksize=max(1, count // (4 * procs)))
 
 
 WORKLOADS = {

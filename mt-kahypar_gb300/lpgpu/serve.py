@@ -1,31 +1,40 @@
-"""Continuous-batching refine server over batched lpgpu sessions.
+"""Continuous batching of refine requests at round granularity.
 
-Requests (hypergraph, partition, k, eps, rounds) arrive over time. The server
-keeps `slots` batched sessions, each with its own CUDA stream and driven by its
-own thread (the C calls release the GIL, so slots overlap on the device). A
-free slot takes every waiting request that fits the device-memory budget
-(admission by lpgpu_estimate_footprint against the budget minus what the other
-slots hold) and refines them together as one batch; requests that arrive while
-batches run wait for the next free slot. Each request's result is exactly what
-refining it alone gives, because a batched session assigns sub-rounds from
-instance-local ids and decides rollbacks per instance.
+Requests (hypergraph, partition, k, eps, rounds) arrive over time; a
+request's hypergraph and partition state stay on the device from admission to
+completion.
+
+* Small requests (at most `large_pins` pins and k <= 64) each get a session
+  from a pool and join the stepper's running set at the next round boundary.
+  Every step runs one LP round of every running request in one persistent
+  launch (lpgpu_stepper_launch). While a step runs, the requests admitted for
+  the next one are uploaded on their own streams; after it, finished requests
+  leave and their partitions are read back. A request never waits for the
+  remaining rounds of another: it joins after at most one round and leaves as
+  soon as its own rounds are done.
+* Large requests go to `solo_slots` lanes that refine one request at a time
+  with the multi-launch pipeline on their own streams, concurrently with the
+  stepper.
+
+Admission is by device-memory footprint (lpgpu_estimate_footprint) against the
+budget: admitted requests count with their estimate, idle pooled sessions with
+the memory they still hold (they are released when a request needs it).
+Each request's result is exactly what refining it alone gives (tested).
 
 `plain_loop` is the baseline: one request at a time, in arrival order, one
 session call sequence per request.
-
-Every request has its own shape, so a captured CUDA graph would be used once:
-both the server and the plain loop default to direct launches
-(LPGPU_FLAG_NO_GRAPH).
 """
 from __future__ import annotations
 
+import json
 import threading
 import time
 from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import FLAG_NO_GRAPH, Session, default_config, estimate_footprint
+from . import (FLAG_NO_GRAPH, PERSISTENT_MAX_K, TUNING_PATH, Session, Stepper, default_config,
+               estimate_footprint)
 
 
 @dataclass
@@ -42,8 +51,8 @@ class Request:
     finish: float = None
     result: np.ndarray = None
     km1: int = None
-    slot: int = None
-    batch_size: int = None
+    lane: str = None      # "stepped" or "solo"
+    batch_size: int = None  # requests in its first step (stepped) or 1 (solo)
 
     @property
     def latency(self):
@@ -60,6 +69,8 @@ class ServeStats:
     wall: float = 0.0
     pins: int = 0
     rejected: int = 0
+    steps: int = 0
+    solo: int = 0
 
     def summary(self):
         lat = np.array(self.latencies) if self.latencies else np.zeros(1)
@@ -68,60 +79,119 @@ class ServeStats:
                 "wall_s": self.wall, "pins_per_s": self.pins / self.wall if self.wall > 0 else 0.0,
                 "req_per_s": len(self.latencies) / self.wall if self.wall > 0 else 0.0,
                 "mean_batch": float(np.mean(self.batch_sizes)) if self.batch_sizes else 0.0,
-                "rejected": self.rejected}
+                "steps": self.steps, "solo": self.solo, "rejected": self.rejected}
 
 
-def _run_batch(session, reqs, subrounds, flags=FLAG_NO_GRAPH):
-    """Refines `reqs` together on one batched session; returns pins processed."""
-    session.upload_instances([r.hg for r in reqs])
-    session.set_partition_instances([r.k for r in reqs], [r.part for r in reqs],
-                                    eps=np.array([r.eps for r in reqs]))
-    res = session.refine(default_config(rounds=reqs[0].rounds, subrounds=subrounds, flags=flags))
-    parts = session.partition_instances()
-    km1 = session.instance_km1()
-    for i, r in enumerate(reqs):
-        r.result = parts[i]
-        r.km1 = int(km1[i])
-    return res.pins_processed
+def default_large_pins():
+    """Pins above which a request is refined alone: the largest mean instance
+    size for which the tuning table chose persistent rounds (1,000,000 without
+    a table)."""
+    try:
+        with open(TUNING_PATH) as f:
+            rows = [r for r in json.load(f)["entries"] if r["mode"] == 1]
+        return max(int(r["max_mean_pins"]) for r in rows) if rows else 0
+    except (OSError, ValueError, KeyError):
+        return 1_000_000
+
+
+class DeviceBackend:
+    """The device side of the server: a stepper, a pool of stepped sessions,
+    and one session per solo lane."""
+
+    def __init__(self, device=0, subrounds=7):
+        self.device = device
+        self.subrounds = subrounds
+        self.stepper = Stepper(device)
+        self._idle = []
+
+    def cfg(self, r, flags=FLAG_NO_GRAPH):
+        return default_config(rounds=r.rounds, subrounds=self.subrounds, flags=flags)
+
+    # stepped lane (one thread)
+    def acquire(self):
+        return self._idle.pop() if self._idle else Session(self.device)
+
+    def release(self, s):
+        self._idle.append(s)
+
+    def idle_bytes(self):
+        return sum(s.footprint() for s in self._idle)
+
+    def drop_idle(self):
+        while self._idle:
+            self._idle.pop().close()
+
+    def begin(self, s, r):
+        s.upload(r.hg)
+        s.set_partition(r.k, r.part, eps=r.eps)
+        s.begin_rounds(self.cfg(r))
+
+    def launch(self, sessions):
+        self.stepper.launch(sessions)
+
+    def wait(self):
+        return self.stepper.wait()
+
+    def finish(self, s, r):
+        res = s.end_rounds()
+        r.result = s.partition()
+        r.km1 = int(res.km1_after)
+        return res.pins_processed
+
+    # solo lanes (one session per lane thread)
+    def solo_session(self):
+        return Session(self.device)
+
+    def solo(self, s, r):
+        s.upload(r.hg)
+        s.set_partition(r.k, r.part, eps=r.eps)
+        res = s.refine(self.cfg(r))
+        r.result = s.partition()
+        r.km1 = int(res.km1_after)
+        return res.pins_processed
+
+    def close(self):
+        self.drop_idle()
+        self.stepper.close()
 
 
 class RefineServer:
-    """Continuous batching over `slots` concurrent batched sessions.
+    """Round-granular continuous batching; see the module docstring.
 
-    `session_factory(device)` and `runner(session, requests, subrounds)` default to
-    lpgpu sessions and `_run_batch`; `footprint(request, subrounds)` defaults to
-    lpgpu_estimate_footprint. Tests replace them to check the scheduling alone.
+    `backend` defaults to DeviceBackend and `footprint(request, subrounds)` to
+    lpgpu_estimate_footprint; tests replace both to check the scheduling alone.
     """
 
-    def __init__(self, device=0, slots=2, budget_bytes=150 << 30, subrounds=7, max_batch=4096,
-                 session_factory=Session, runner=_run_batch, footprint=None, max_batch_pins=None):
-        self.device = device
-        self.slots = slots
+    def __init__(self, device=0, budget_bytes=150 << 30, subrounds=7, solo_slots=1, large_pins=None,
+                 max_running=4096, backend=None, footprint=None):
         self.budget = budget_bytes
         self.subrounds = subrounds
-        self.max_batch = max_batch
-        # a batch stops growing once it holds this many pins (None: memory budget only);
-        # smaller batches finish their first requests sooner at some cost in throughput
-        self.max_batch_pins = max_batch_pins
-        self._runner = runner
+        self.solo_slots = solo_slots
+        self.large_pins = default_large_pins() if large_pins is None else large_pins
+        self.max_running = max_running
+        self.backend = backend or DeviceBackend(device, subrounds)
         self._footprint = footprint or (lambda r, s: r.footprint(s))
         self._cv = threading.Condition()
         self._queue = []
-        self._held = [0] * slots
+        self._held = 0         # estimated bytes of admitted requests
+        self._idle_bytes = 0   # bytes idle pooled sessions hold
         self._closed = False
         self.stats = ServeStats()
         self.errors = []
         self._t0 = None
         self._threads = []
-        self._sessions = [session_factory(device) for _ in range(slots)]
 
     def now(self):
         return time.perf_counter() - self._t0
 
+    def stepped(self, r):
+        return r.hg.num_pins <= self.large_pins and r.k <= PERSISTENT_MAX_K
+
     def start(self):
         self._t0 = time.perf_counter()
-        for s in range(self.slots):
-            t = threading.Thread(target=self._worker, args=(s,), daemon=True)
+        lanes = [self._stepper_lane] + [self._solo_lane] * self.solo_slots
+        for fn in lanes:
+            t = threading.Thread(target=fn, daemon=True)
             t.start()
             self._threads.append(t)
 
@@ -141,64 +211,141 @@ class RefineServer:
             self._cv.notify_all()
         for t in self._threads:
             t.join()
-        for s in self._sessions:
-            s.close()
+        self.backend.close()
 
-    def _admit(self, slot):
-        """Takes waiting requests in arrival order while they fit the memory left."""
-        free = self.budget - sum(h for i, h in enumerate(self._held) if i != slot)
-        take, used, pins = [], 0, 0
-        rounds = self._queue[0].rounds if self._queue else 0
+    # -------------------------------------------------------------- lanes
+
+    def _take(self, stepped, limit):
+        """Waiting requests of one lane, in arrival order, while they fit the
+        memory left (call with the lock held); a request that does not fit
+        waits, later ones may still be taken."""
+        take = []
+        free = self.budget - self._held - self._idle_bytes
         for r in list(self._queue):
-            if r.rounds != rounds:  # a batch runs one round count for all its requests
+            if len(take) >= limit:
+                break
+            if self.stepped(r) != stepped:
                 continue
             f = self._footprint(r, self.subrounds)
-            if len(take) >= self.max_batch or used + f > free:
-                break
-            if take and self.max_batch_pins is not None and pins + r.hg.num_pins > self.max_batch_pins:
-                break
+            if f > free:
+                continue
             take.append(r)
-            used += f
-            pins += r.hg.num_pins
+            free -= f
+            self._held += f
         for r in take:
             self._queue.remove(r)
-        self._held[slot] = used
         return take
 
-    def _worker(self, slot):
-        session = self._sessions[slot]
+    def _waiting(self, stepped):
+        return any(self.stepped(r) == stepped for r in self._queue)
+
+    def _done(self, r, pins):
+        with self._cv:
+            r.finish = self.now()
+            self.stats.latencies.append(r.latency)
+            self.stats.pins += pins
+            self._held -= self._footprint(r, self.subrounds)
+            self._cv.notify_all()
+
+    def _fail(self, reqs, exc):
+        with self._cv:
+            self.errors.append((tuple(r.rid for r in reqs), exc))
+            for r in reqs:
+                r.finish = -1.0
+                self._held -= self._footprint(r, self.subrounds)
+            self._cv.notify_all()
+
+    def _stepper_lane(self):
+        be = self.backend
+        running = []  # (request, session)
         while True:
             with self._cv:
-                while not self._queue and not self._closed:
-                    self._cv.wait()
-                if not self._queue and self._closed:
-                    return
-                batch = self._admit(slot)
-                if not batch:  # the head request waits for memory held by other slots
-                    self._cv.wait(0.001)
+                admit = self._take(True, self.max_running - len(running))
+                if not admit and not running:
+                    if self._closed and not self._waiting(True):
+                        return
+                    if self._waiting(True) and self._idle_bytes > 0:
+                        be.drop_idle()  # waiting requests need the memory idle sessions hold
+                        self._idle_bytes = 0
+                        continue
+                    self._cv.wait(0.002)
                     continue
-            t = self.now()
-            for r in batch:
-                r.start, r.slot, r.batch_size = t, slot, len(batch)
             try:
-                pins = self._runner(session, batch, self.subrounds)
-            except Exception as exc:  # the batch fails as a whole; the slot keeps serving
-                with self._cv:
-                    self.errors.append((tuple(r.rid for r in batch), exc))
-                    for r in batch:
-                        r.finish = -1.0
-                    self._held[slot] = 0
-                    self._cv.notify_all()
-                continue
-            t = self.now()
+                if running:
+                    be.launch([s for _, s in running])
+            except Exception as exc:  # the step fails its requests; their sessions are dropped
+                self._fail([r for r, _ in running], exc)
+                running = []
+            joined = []
+            for r in admit:  # uploads overlap the running step on their own streams
+                r.start, r.lane = self.now(), "stepped"
+                s = be.acquire()
+                try:
+                    be.begin(s, r)
+                except Exception as exc:
+                    self._fail([r], exc)
+                    be.release(s)
+                    continue
+                joined.append((r, s))
+            if running:
+                try:
+                    done = be.wait()
+                    self.stats.steps += 1
+                except Exception as exc:
+                    self._fail([r for r, _ in running], exc)
+                    done, running = [], []
+                keep = []
+                for (r, s), d in zip(running, done):
+                    if not d:
+                        keep.append((r, s))
+                        continue
+                    try:
+                        pins = be.finish(s, r)
+                    except Exception as exc:
+                        self._fail([r], exc)
+                    else:
+                        self._done(r, pins)
+                    be.release(s)
+                running = keep
+            for r, s in joined:
+                r.batch_size = len(running) + len(joined)
+                self.stats.batch_sizes.append(r.batch_size)
+                if r.rounds > 0:
+                    running.append((r, s))
+                else:  # nothing to run
+                    self._done(r, be.finish(s, r))
+                    be.release(s)
             with self._cv:
-                for r in batch:
-                    r.finish = t
-                    self.stats.latencies.append(r.latency)
-                self.stats.batch_sizes.append(len(batch))
-                self.stats.pins += pins
-                self._held[slot] = 0
+                self._idle_bytes = be.idle_bytes()
                 self._cv.notify_all()
+
+    def _solo_lane(self):
+        be = self.backend
+        s = None
+        while True:
+            with self._cv:
+                while True:
+                    take = self._take(False, 1)
+                    if take or (self._closed and not self._waiting(False)):
+                        break
+                    self._cv.wait(0.002)
+            if not take:
+                if s is not None:
+                    s.close()
+                return
+            r = take[0]
+            r.start, r.lane, r.batch_size = self.now(), "solo", 1
+            try:
+                if s is None:
+                    s = be.solo_session()
+                pins = be.solo(s, r)
+            except Exception as exc:
+                self._fail([r], exc)
+                continue
+            with self._cv:
+                self.stats.solo += 1
+                self.stats.batch_sizes.append(1)
+            self._done(r, pins)
 
 
 def replay(server: RefineServer, requests):
@@ -242,3 +389,7 @@ def plain_loop(requests, device=0, subrounds=7, flags=FLAG_NO_GRAPH):
 def poisson_arrivals(count, rate, seed):
     rng = np.random.default_rng([seed, 7])
     return np.cumsum(rng.exponential(1.0 / rate, size=count))
+
+
+__all__ = ["Request", "ServeStats", "RefineServer", "DeviceBackend", "replay", "plain_loop",
+           "poisson_arrivals", "default_large_pins"]
