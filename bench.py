@@ -69,6 +69,8 @@ def parse_args():
     ap.add_argument("--slots", type=int, default=2, help="served: solo lanes for large requests")
     ap.add_argument("--no-systems", action="store_true",
                     help="default run: skip the batched and served measurements")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="batch / served: skip the plain one-at-a-time loop they are compared with")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--subrounds", type=int, default=7)
     ap.add_argument("--no-baseline", action="store_true", help="skip the CPU baseline leg")
@@ -489,7 +491,7 @@ def batch_measure(args, insts, plain_modes=(0, None)):
             dev[name] = {"ms_per_refine": ms / steps, "pins_per_s": r.pins_processed / (ms / steps / 1e3),
                          "km1_identical": bool(np.array_equal(km_d, km_b))}
     best_plain = None
-    for flags in plain_modes:
+    for flags in ([] if args.no_plain else plain_modes):
         if flags is None:
             flags = lpgpu.FLAG_NO_GRAPH
         pcfg = lpgpu.default_config(rounds=5, subrounds=args.subrounds, flags=flags | lpgpu.FLAG_MULTI_LAUNCH)
@@ -507,6 +509,8 @@ def batch_measure(args, insts, plain_modes=(0, None)):
             t_plain = time.perf_counter() - t0
         if best_plain is None or t_plain < best_plain[0]:
             best_plain = (t_plain, flags, km_p, pp)
+    if best_plain is None:
+        best_plain = (float("nan"), 0, km_b, 0)
     t_plain, flags, km_p, pp = best_plain
     same = bool(np.array_equal(km_b, km_p)) and all(d["km1_identical"] for d in dev.values())
     nominal = pins_total * 5
