@@ -904,11 +904,14 @@ static lpgpu_status need_part(lpgpu_session* s) {
 static std::mutex g_tuning_mutex;
 static std::vector<lpgpu_tuning_entry> g_tuning_table;
 
+// The multi-launch form; when the persistent form is forced by the flag, its
+// kernel parameters are the ones the autotuner picked on every size class
+// where it won (2 CTAs per SM, unroll 8, largest instance first).
 static lpgpu_tuning default_tuning() {
   lpgpu_tuning t{};
   t.mode = LPGPU_MODE_MULTI_LAUNCH;
-  t.ctas_per_sm = 1;
-  t.unroll = 4;
+  t.ctas_per_sm = 2;
+  t.unroll = 8;
   t.order = 0;
   return t;
 }

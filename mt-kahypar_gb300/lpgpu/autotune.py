@@ -106,7 +106,7 @@ def build_table(class_results, count_results):
         best = min(cr["results"], key=lambda r: r["ms"])
         nxt = class_results[i + 1]["mean_pins"] if i + 1 < len(class_results) else 2 * cr["mean_pins"]
         bound = int(math.sqrt(cr["mean_pins"] * nxt))
-        tu = best["tuning"] or {"mode": 0, "ctas_per_sm": 1, "unroll": 4, "order": 0}
+        tu = best["tuning"] or {"mode": 0, "ctas_per_sm": 2, "unroll": 8, "order": 0}
         rows.append({"class": cr["class"], "max_mean_pins": bound, "min_instances": int(min_inst), **tu})
     return rows
 
