@@ -57,9 +57,14 @@ __host__ __device__ inline int subround_of(int64_t v, int round, int S) {
                (uint32_t)S);
 }
 
-// Candidate ordering key: (gain, vertex) as one unsigned 64-bit integer.
+// Candidate ordering key: (gain, vertex) as one unsigned 64-bit integer. The
+// gain maps to (gain - 1) XOR 2^31, which keeps the order of every gain above
+// INT32_MIN (gains stay within +-INT32_MAX) and sends the non-positive gains of
+// LP candidates (-d .. 0) to 0x7FFFFFFF - d .. 0x7FFFFFFF: a segment mixing
+// improving and zero-gain moves then differs only in the gain's low byte(s),
+// and the radix selection skips the constant ones.
 __host__ __device__ inline uint64_t move_key(int32_t gain, int32_t v) {
-  return ((uint64_t)((uint32_t)gain ^ 0x80000000u) << 32) | (uint32_t)v;
+  return ((uint64_t)((uint32_t)((int64_t)gain - 1) ^ 0x80000000u) << 32) | (uint32_t)v;
 }
 
 // Indices into the device scalar block.

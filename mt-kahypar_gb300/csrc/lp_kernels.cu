@@ -2025,6 +2025,9 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_moves(RoundCtx c, int sub) 
 #ifndef LPGPU_SEL_STAGE
 #define LPGPU_SEL_STAGE 8192
 #endif
+#ifndef LPGPU_SEL_ONEHIST
+#define LPGPU_SEL_ONEHIST 4096  // segments of at most this many keys share one histogram
+#endif
 constexpr int kSelThreads = LPGPU_SEL_THREADS;
 constexpr int kSelStage = LPGPU_SEL_STAGE;  // keys (8 B) + weights (4 B) staged in shared memory
 constexpr size_t kSelSmem = (size_t)kSelStage * 12;
@@ -2115,6 +2118,10 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const i
   ka = s_and[0];
   ko = s_or[0];
   uint64_t prefix = 0, mask = 0;
+  // small segments bin into one shared histogram (atomics rarely collide),
+  // large ones into a private histogram per warp folded afterwards
+  const bool one = cnt <= LPGPU_SEL_ONEHIST;
+  const int rows = one ? 1 : NW;
   for (int byte = 7; byte >= 0; --byte) {
     const int shift = 8 * byte;
     if ((((ka ^ ko) >> shift) & 255) == 0) {  // every key has this byte
@@ -2122,17 +2129,16 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const i
       mask |= 255ull << shift;
       continue;
     }
-    for (int i = threadIdx.x; i < NW * 256; i += blockDim.x) (&hist[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < rows * 256; i += blockDim.x) (&hist[0][0])[i] = 0;
     __syncthreads();
     if (staged)
-      sel_hist<1>(skeys, sws, cnt, mask, prefix, shift, hist[wid]);
+      sel_hist<1>(skeys, sws, cnt, mask, prefix, shift, hist[one ? 0 : wid]);
     else
-      sel_hist<8>(gkeys, gws, cnt, mask, prefix, shift, hist[wid]);
+      sel_hist<8>(gkeys, gws, cnt, mask, prefix, shift, hist[one ? 0 : wid]);
     __syncthreads();
     for (int bin = threadIdx.x; bin < 256; bin += blockDim.x) {
       unsigned t = 0;
-#pragma unroll
-      for (int w = 0; w < NW; ++w) t += hist[w][bin];
+      for (int w = 0; w < rows; ++w) t += hist[w][bin];
       tot[bin] = t;
     }
     __syncthreads();
