@@ -279,9 +279,9 @@ struct PhaseTimer;
 cudaError_t launch_mark_all(const Launch& L, const RoundCtx& c, int rebalancing);
 cudaError_t launch_mark_list(const Launch& L, const RoundCtx& c, const int32_t* nodes,
                              int64_t count);
-cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int S,
-                              int64_t* tile_cnt, int64_t* tile_off, int64_t* scan_tmp,
-                              int64_t scan_tmp_elems, PhaseTimer* timer);
+// bin_cnt: 2 * kMaxSubrounds * kDegClasses entries, the first half zero
+cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int S, int64_t* bin_cnt,
+                              PhaseTimer* timer);
 cudaError_t launch_subround(const Launch& L, const RoundCtx& c, int round, int sub, PhaseTimer* timer);
 // End of a round that has a successor: activation of the kept moves
 // (moveVertex, label_propagation_refiner.h:112-128) and expansion of the

@@ -285,19 +285,26 @@ __global__ void k_degree_hist(int64_t n, const int64_t* __restrict__ cnt, int64_
 }
 
 // Every pin writes its net id into its slot of its vertex's incident-net list
-// (list start + the rank k_count_pins returned). A warp takes 32 nets and
-// walks their pins in packed 32-pin groups (nets of more than 32 pins alone,
-// 32 pins at a time), so small nets keep every lane busy.
+// (list start + the rank k_count_pins returned). A warp takes the next 32 nets
+// from a counter and walks their pins in packed 32-pin groups (nets of more
+// than 32 pins alone, 32 pins at a time), so small nets keep every lane busy.
+// Taking nets in order keeps the nets in flight close together, so the
+// partly written 32-byte sectors of their vertices' lists stay in L2 until
+// they are complete (a grid-stride loop lets warps drift apart over nets of
+// uneven size, and the sectors were written back many times).
 __global__ void __launch_bounds__(256) k_scatter_incidence(int64_t m, const int64_t* __restrict__ net_off,
                                                            const int32_t* __restrict__ pins,
                                                            const int64_t* __restrict__ vtx_off,
                                                            const int32_t* __restrict__ rank,
-                                                           int32_t* __restrict__ inets) {
+                                                           int32_t* __restrict__ inets, ull* next_net) {
   __shared__ unsigned char s_own[256];
   const int lane = lane_id();
   unsigned char* own = s_own + (threadIdx.x & ~31);
-  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < m;
-       base += (int64_t)gridDim.x * blockDim.x) {
+  for (;;) {
+    ull b = 0;
+    if (lane == 0) b = atomicAdd(next_net, 32ull);
+    const int64_t base = (int64_t)__shfl_sync(FULLMASK, b, 0);
+    if (base >= m) break;
     const int64_t e = base + lane;
     const bool sel = e < m;
     const int64_t o0 = sel ? net_off[e] : 0;
@@ -329,7 +336,9 @@ cudaError_t launch_build_incidence(const Launch& L, int64_t n, int64_t m, int64_
   if ((e = scan_exclusive_i64(vtx_off, vtx_off, n + 1, scan_tmp, scan_tmp_elems, L.st)) != cudaSuccess)
     return e;
   if (m > 0) {
-    k_scatter_incidence<<<grid_for(L, m, 256, 8), 256, 0, L.st>>>(m, net_off, pins, vtx_off, rank, inets);
+    ull* next_net = reinterpret_cast<ull*>(scan_tmp);  // free again after the scan
+    if ((e = cudaMemsetAsync(next_net, 0, sizeof(ull), L.st)) != cudaSuccess) return e;
+    k_scatter_incidence<<<grid_for(L, m, 256, 8), 256, 0, L.st>>>(m, net_off, pins, vtx_off, rank, inets, next_net);
     LAUNCHED("k_scatter_incidence");
   }
   return cudaGetLastError();
@@ -375,8 +384,8 @@ __global__ void k_block_weights(RoundCtx c) {
 
 
 // Φ, Λ and Λ1 (blocks holding exactly one pin of the net) from scratch
-// (initializePinCountInPart, h:1086-1110), fused with the km1 / cut sums, on
-// zeroed Φ and Λ / Λ1. A warp takes 32 nets. Nets of up to 32 pins are packed
+// (initializePinCountInPart, h:1086-1110), fused with the km1 / cut sums. A
+// warp takes 32 nets and zeroes their Φ rows and records before filling them. Nets of up to 32 pins are packed
 // into 32-pin groups (lane = pin): lanes with the same (net, block) find each
 // other with a match, and the lowest writes Φ(e, b) and sets the Λ / Λ1 bits;
 // λ(e) is the number of such lanes. Larger nets are counted one at a time in a
@@ -394,6 +403,20 @@ __global__ void __launch_bounds__(256) k_pin_counts(RoundCtx c) {
   int64_t km1 = 0, cut = 0;
   for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < c.m;
        base += (int64_t)gridDim.x * blockDim.x) {
+    // The warp first zeroes the Φ rows and Λ records of its 32 nets (one
+    // contiguous range each), so every sector it then changes is complete in
+    // L2 and no partly written sector is read back from DRAM.
+    {
+      const int64_t e_end = base + 32 < c.m ? base + 32 : c.m;
+      const int esz = c.phi16 ? 2 : 4;
+      unsigned char* p0 = reinterpret_cast<unsigned char*>(c.phi) + base * k * esz;
+      const int64_t bytes = ((e_end - base) * k * esz + 3) & ~(int64_t)3;  // Φ is allocated in whole words
+      const int64_t n16 = bytes >> 4;
+      for (int64_t i = lane; i < n16; i += 32) reinterpret_cast<uint4*>(p0)[i] = make_uint4(0, 0, 0, 0);
+      for (int64_t i = (n16 << 2) + lane; i < (bytes >> 2); i += 32) reinterpret_cast<uint32_t*>(p0)[i] = 0;
+      for (int64_t i = base * 2 * W + lane; i < e_end * 2 * W; i += 32) c.conn[i] = 0;
+      __syncwarp();
+    }
     const int64_t e = base + lane;
     int64_t b0 = 0;
     int deg = 0, bo = 0;
@@ -481,10 +504,7 @@ cudaError_t launch_init_partition(const Launch& L, const RoundCtx& c) {
     LAUNCHED("k_block_weights");
   }
   if (c.m > 0) {
-    const size_t entries = (size_t)c.m * c.kmax;
-    const size_t phi_bytes = c.phi16 ? sizeof(uint32_t) * ((entries + 1) / 2) : sizeof(int32_t) * entries;
-    if ((e = cudaMemsetAsync(c.phi, 0, phi_bytes, L.st)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(c.conn, 0, sizeof(uint32_t) * (size_t)c.m * 2 * c.W, L.st)) != cudaSuccess) return e;
+    // k_pin_counts writes all of Φ and the Λ records, zeros included
     const size_t smem = sizeof(int) * c.kmax * 8;
     k_pin_counts<<<grid_for(L, c.m, 256, occupancy((const void*)k_pin_counts, 256, smem)), 256, smem, L.st>>>(c);
     LAUNCHED("k_pin_counts");
@@ -1588,7 +1608,6 @@ cudaError_t launch_apply_moves(const Launch& L, const RoundCtx& c, int64_t count
 
 // ========================================================= active lists
 
-constexpr int kTile = 1024;  // vertices per binning tile = 32 chunks of 32
 
 __global__ void k_mark_all(uint8_t* flag, int64_t n) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
@@ -1644,11 +1663,16 @@ cudaError_t launch_mark_list(const Launch& L, const RoundCtx& c, const int32_t* 
 
 // Active-list binning. Each round's active vertices are grouped by sub-round
 // and, inside a sub-round, by class (vertex_class): the heavy vertices first,
-// which the sweep gives to whole CTAs, then four degree classes, since the
+// which the sweep gives to whole CTAs, then the degree classes, since the
 // lane-per-vertex sweep runs a warp until its longest incidence list is done.
-// Bin b = sub-round * kDegClasses + class; tile_cnt[b * tiles + tile] counts
-// the tile's flagged vertices per bin. Which position a vertex takes inside
-// its sub-round changes no result.
+// Bin b = sub-round * kDegClasses + class. k_bin_count adds each CTA's
+// flagged vertices per bin to cnt[b] and keeps each flagged vertex's class in
+// its flag (1 + class); k_bin_offsets turns the counts into the bins' start
+// positions (cursors) and clears the counts for the next round; k_bin_scatter
+// places batches of 32-vertex chunks with one cursor atomic per bin and batch
+// and clears the flags. A warp's vertices of one bin stay together in id
+// order; the order of the batches inside a bin is the order of their atomics,
+// and which position a vertex takes inside its sub-round changes no result.
 //
 // All 32 vertices of an aligned chunk share one sub-round. Batched sessions
 // hash instance-local ids (so that an instance gets the same sub-rounds alone
@@ -1673,101 +1697,145 @@ __device__ __forceinline__ int vertex_class(const ClassRule& r, int64_t v) {
   return g <= 1 ? 1 : (g >= kDegClasses - 1 ? kDegClasses - 1 : (int)g);  // D = 2: always 1
 }
 
-__global__ void __launch_bounds__(1024) k_bin_count(const uint8_t* __restrict__ flag, int64_t n,
-                                                    int round, int S, int64_t tiles,
-                                                    int64_t* __restrict__ tile_cnt, ClassRule rule,
-                                                    const int32_t* __restrict__ vinst,
-                                                    const int64_t* __restrict__ inst_voff) {
-  __shared__ int s_cnt[kMaxSubrounds * kDegClasses];
+constexpr int kBinBins = kMaxSubrounds * kDegClasses;
+constexpr int kBinThreadsA = 1024;  // binning CTAs
+constexpr int kBinBatch = 4;        // chunks per warp and batch (independent loads in flight)
+constexpr int kBinBatchChunks = (kBinThreadsA / 32) * kBinBatch;
+
+__global__ void __launch_bounds__(kBinThreadsA) k_bin_count(uint8_t* __restrict__ flag, int64_t n, int round, int S,
+                                                            int64_t* __restrict__ cnt, ClassRule rule,
+                                                            const int32_t* __restrict__ vinst,
+                                                            const int64_t* __restrict__ inst_voff) {
+  __shared__ int s_cnt[kBinBins];
   const int bins = S * kDegClasses;
+  const int w = threadIdx.x >> 5, lane = lane_id();
   for (int i = threadIdx.x; i < bins; i += blockDim.x) s_cnt[i] = 0;
   __syncthreads();
-  const int64_t v = blockIdx.x * (int64_t)kTile + threadIdx.x;
-  const bool f = v < n && flag[v];
-  const int cls = f ? vertex_class(rule, v) : 0;
-  if (vinst) {
-    if (f) atomicAdd(&s_cnt[vertex_subround(vinst, inst_voff, v, round, S) * kDegClasses + cls], 1);
-  } else {
-    const int sub = subround_of(v, round, S);
+  const int64_t chunks = (n + 31) >> 5;
+  for (int64_t c0 = (int64_t)blockIdx.x * kBinBatchChunks; c0 < chunks; c0 += (int64_t)gridDim.x * kBinBatchChunks) {
+    bool f[kBinBatch];
 #pragma unroll
-    for (int q = 0; q < kDegClasses; ++q) {
-      const unsigned bal = __ballot_sync(FULLMASK, f && cls == q);
-      if (lane_id() == 0 && bal) atomicAdd(&s_cnt[sub * kDegClasses + q], __popc(bal));
+    for (int j = 0; j < kBinBatch; ++j) {
+      const int64_t v = ((c0 + j * 32 + w) << 5) + lane;
+      f[j] = v < n && flag[v];
+    }
+    int cls[kBinBatch];
+#pragma unroll
+    for (int j = 0; j < kBinBatch; ++j) cls[j] = f[j] ? vertex_class(rule, ((c0 + j * 32 + w) << 5) + lane) : 0;
+#pragma unroll
+    for (int j = 0; j < kBinBatch; ++j) {
+      const int64_t v = ((c0 + j * 32 + w) << 5) + lane;
+      if (f[j]) flag[v] = (uint8_t)(1 + cls[j]);
+      if (vinst) {
+        if (f[j]) atomicAdd(&s_cnt[vertex_subround(vinst, inst_voff, v, round, S) * kDegClasses + cls[j]], 1);
+      } else {
+        const int sub = subround_of(v, round, S);
+#pragma unroll
+        for (int q = 0; q < kDegClasses; ++q) {
+          const unsigned bal = __ballot_sync(FULLMASK, f[j] && cls[j] == q);
+          if (lane == 0 && bal) atomicAdd(&s_cnt[sub * kDegClasses + q], __popc(bal));
+        }
+      }
     }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < bins; i += blockDim.x) tile_cnt[i * tiles + blockIdx.x] = s_cnt[i];
+  for (int i = threadIdx.x; i < bins; i += blockDim.x)
+    if (s_cnt[i]) atomicAdd(reinterpret_cast<ull*>(&cnt[i]), (ull)s_cnt[i]);
 }
 
-// Writes each bin's flagged vertices (in increasing id order for one
-// instance) and clears the flags. Sub-round s occupies
-// list[tile_off[s * kDegClasses * tiles] .. tile_off[(s + 1) * kDegClasses * tiles]).
-__global__ void __launch_bounds__(1024) k_bin_scatter(uint8_t* __restrict__ flag, int64_t n, int round,
-                                                      int S, int64_t tiles,
-                                                      const int64_t* __restrict__ tile_off,
-                                                      int32_t* __restrict__ list, ClassRule rule,
-                                                      const int32_t* __restrict__ vinst,
-                                                      const int64_t* __restrict__ inst_voff) {
-  __shared__ int s_cnt[32][kDegClasses];    // per warp and class: flagged vertices
-  __shared__ int64_t s_base[32][kDegClasses];
-  __shared__ int s_sub[32];
-  __shared__ unsigned long long s_cur[kMaxSubrounds * kDegClasses];
+// One CTA: the bins' start positions (cnt[kBinBins + b]) from their counts,
+// which are cleared for the next round; the sub-round offsets (sub-round s
+// occupies list[sub_off[s] .. sub_off[s + 1]), its heavy vertices the first
+// sub_off[kMaxSubrounds + 1 + s] - sub_off[s]) and the round's activation
+// epoch.
+constexpr int kBinOffThreads = (kBinBins + 31) / 32 * 32;
+__global__ void __launch_bounds__(kBinOffThreads) k_bin_offsets(int64_t* __restrict__ cnt, int S,
+                                                                int64_t* __restrict__ sub_off, int64_t* scal) {
+  __shared__ int64_t s_off[kBinBins];
+  const int bins = S * kDegClasses, i = threadIdx.x;
+  const int64_t x = i < bins ? cnt[i] : 0;
+  int64_t total;
+  const int64_t off = block_scan_excl_i64(x, &total);
+  if (i < bins) {
+    cnt[kBinBins + i] = off;
+    cnt[i] = 0;
+    s_off[i] = off;
+  }
+  __syncthreads();
+  if (i < S) {
+    sub_off[i] = s_off[i * kDegClasses];
+    sub_off[kMaxSubrounds + 1 + i] = s_off[i * kDegClasses + 1];  // end of the heavy class
+  }
+  if (i == 0) {
+    sub_off[S] = total;
+    scal[kEpoch] += 1;  // new round: fresh activation stamp
+  }
+}
+
+__global__ void __launch_bounds__(kBinThreadsA) k_bin_scatter(uint8_t* __restrict__ flag, int64_t n, int round,
+                                                              int S, int64_t* __restrict__ cnt,
+                                                              int32_t* __restrict__ list,
+                                                              const int32_t* __restrict__ vinst,
+                                                              const int64_t* __restrict__ inst_voff) {
+  __shared__ int s_cnt[kBinBins];
+  __shared__ int64_t s_base[kBinBins];
+  int64_t* cursor = cnt + kBinBins;
+  const int bins = S * kDegClasses;
   const int w = threadIdx.x >> 5, lane = lane_id();
-  const int64_t v = blockIdx.x * (int64_t)kTile + threadIdx.x;
-  const bool f = v < n && flag[v];
-  const int cls = f ? vertex_class(rule, v) : 0;
-  if (vinst) {
-    // per-vertex sub-rounds; positions inside a (tile, bin) segment are taken
-    // in arrival order
-    for (int i = threadIdx.x; i < S * kDegClasses; i += blockDim.x) {
-      const int sub = i / kDegClasses, q = i - sub * kDegClasses;
-      s_cur[i] = (unsigned long long)tile_off[(sub * kDegClasses + q) * tiles + blockIdx.x];
+  for (int i = threadIdx.x; i < bins; i += blockDim.x) s_cnt[i] = 0;
+  __syncthreads();
+  const int64_t chunks = (n + 31) >> 5;
+  for (int64_t c0 = (int64_t)blockIdx.x * kBinBatchChunks; c0 < chunks; c0 += (int64_t)gridDim.x * kBinBatchChunks) {
+    int fl[kBinBatch];
+#pragma unroll
+    for (int j = 0; j < kBinBatch; ++j) {
+      const int64_t v = ((c0 + j * 32 + w) << 5) + lane;
+      fl[j] = v < n ? flag[v] : 0;
+    }
+    // each vertex's bin and its place among the batch's vertices of that bin
+    int bin[kBinBatch], at[kBinBatch];
+#pragma unroll
+    for (int j = 0; j < kBinBatch; ++j) {
+      const int64_t v = ((c0 + j * 32 + w) << 5) + lane;
+      const bool f = fl[j] != 0;
+      const int cls = f ? fl[j] - 1 : 0;
+      bin[j] = -1;
+      at[j] = 0;
+      if (vinst) {
+        if (f) {
+          bin[j] = vertex_subround(vinst, inst_voff, v, round, S) * kDegClasses + cls;
+          at[j] = atomicAdd(&s_cnt[bin[j]], 1);
+        }
+      } else {
+        const int sub = subround_of(v, round, S);
+#pragma unroll
+        for (int q = 0; q < kDegClasses; ++q) {
+          const unsigned bal = __ballot_sync(FULLMASK, f && cls == q);
+          int o = 0;
+          if (lane == 0 && bal) o = atomicAdd(&s_cnt[sub * kDegClasses + q], __popc(bal));
+          o = __shfl_sync(FULLMASK, o, 0);
+          if (f && cls == q) {
+            bin[j] = sub * kDegClasses + q;
+            at[j] = o + __popc(bal & lanemask_lt());
+          }
+        }
+      }
     }
     __syncthreads();
-    if (f) {
-      const int b = vertex_subround(vinst, inst_voff, v, round, S) * kDegClasses + cls;
-      list[atomicAdd(&s_cur[b], 1ull)] = (int32_t)v;
-      flag[v] = 0;
+    for (int i = threadIdx.x; i < bins; i += blockDim.x) {
+      const int c = s_cnt[i];
+      if (c) s_base[i] = (int64_t)atomicAdd(reinterpret_cast<ull*>(&cursor[i]), (ull)c);
+      s_cnt[i] = 0;
     }
-    return;
-  }
-  unsigned mine = 0;
+    __syncthreads();
 #pragma unroll
-  for (int q = 0; q < kDegClasses; ++q) {
-    const unsigned bal = __ballot_sync(FULLMASK, f && cls == q);
-    if (q == cls) mine = bal;
-    if (lane == 0) s_cnt[w][q] = __popc(bal);
-  }
-  if (lane == 0) s_sub[w] = subround_of(blockIdx.x * (int64_t)kTile + w * 32, round, S);
-  __syncthreads();
-  if (threadIdx.x < 32 * kDegClasses) {
-    // base of (warp ww, class q): the bin's tile offset plus the class-q
-    // vertices of earlier warps of this tile in the same sub-round
-    const int ww = threadIdx.x & 31, q = threadIdx.x >> 5;
-    const int sub = s_sub[ww];
-    int64_t base = tile_off[(sub * kDegClasses + q) * tiles + blockIdx.x];
-    for (int x = 0; x < ww; ++x)
-      if (s_sub[x] == sub) base += s_cnt[x][q];
-    s_base[ww][q] = base;
-  }
-  __syncthreads();
-  if (f) {
-    list[s_base[w][cls] + __popc(mine & lanemask_lt())] = (int32_t)v;
-    flag[v] = 0;
-  }
-}
-
-__global__ void k_sub_offsets(const int64_t* __restrict__ tile_off, const int64_t* __restrict__ tile_cnt,
-                              int S, int64_t tiles, int64_t* __restrict__ sub_off, int64_t* scal) {
-  const int s = threadIdx.x;
-  if (s < S) {
-    sub_off[s] = tile_off[(int64_t)s * kDegClasses * tiles];
-    sub_off[kMaxSubrounds + 1 + s] = tile_off[((int64_t)s * kDegClasses + 1) * tiles];  // end of the heavy class
-  }
-  if (s == 0) {
-    const int64_t last = (int64_t)S * kDegClasses * tiles - 1;
-    sub_off[S] = tile_off[last] + tile_cnt[last];
-    scal[kEpoch] += 1;  // new round: fresh activation stamp
+    for (int j = 0; j < kBinBatch; ++j) {
+      if (bin[j] >= 0) {
+        const int64_t v = ((c0 + j * 32 + w) << 5) + lane;
+        list[s_base[bin[j]] + at[j]] = (int32_t)v;
+        flag[v] = 0;
+      }
+    }
   }
 }
 
@@ -1816,24 +1884,24 @@ struct Scope {
   }
 };
 
-cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int S,
-                              int64_t* tile_cnt, int64_t* tile_off, int64_t* scan_tmp,
-                              int64_t scan_tmp_elems, PhaseTimer* timer) {
+// CTAs of the binning kernels: two resident per SM, at most one per batch of chunks
+static int bin_ctas(int64_t n, int num_sms) {
+  const int64_t batches = std::max<int64_t>(1, ((n + 31) / 32 + kBinBatchChunks - 1) / kBinBatchChunks);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(batches, 2 * (int64_t)std::max(1, num_sms)));
+}
+
+cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int S, int64_t* bin_cnt,
+                              PhaseTimer* timer) {
   Scope sc(timer, "bin_active");
-  const int64_t tiles = std::max<int64_t>(1, (c.n + kTile - 1) / kTile);
+  const int G = bin_ctas(c.n, L.num_sms);
   const int32_t* vinst = c.batched ? c.vinst : nullptr;
   const ClassRule rule{c.vtx_off, c.W, c.unit_nets, c.max_we};
-  k_bin_count<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_cnt, rule, vinst,
-                                                   c.inst_voff);
+  k_bin_count<<<G, kBinThreadsA, 0, L.st>>>(c.next_flag, c.n, round, S, bin_cnt, rule, vinst, c.inst_voff);
   LAUNCHED("k_bin_count");
-  cudaError_t e =
-      scan_exclusive_i64(tile_cnt, tile_off, (int64_t)S * kDegClasses * tiles, scan_tmp, scan_tmp_elems, L.st);
-  if (e != cudaSuccess) return e;
-  k_bin_scatter<<<(unsigned)tiles, kTile, 0, L.st>>>(c.next_flag, c.n, round, S, tiles, tile_off, c.list, rule,
-                                                     vinst, c.inst_voff);
+  k_bin_offsets<<<1, kBinOffThreads, 0, L.st>>>(bin_cnt, S, c.sub_off, c.scal);
+  LAUNCHED("k_bin_offsets");
+  k_bin_scatter<<<G, kBinThreadsA, 0, L.st>>>(c.next_flag, c.n, round, S, bin_cnt, c.list, vinst, c.inst_voff);
   LAUNCHED("k_bin_scatter");
-  k_sub_offsets<<<1, 64, 0, L.st>>>(tile_off, tile_cnt, S, tiles, c.sub_off, c.scal);
-  LAUNCHED("k_sub_offsets");
   return cudaGetLastError();
 }
 

@@ -152,7 +152,7 @@ struct lpgpu_session_s {
   std::vector<int64_t> h_perfect;
   // refine scratch
   DevBuf<int32_t> list, net_epoch, seg_w, heavy, revl;
-  DevBuf<int64_t> sub_off, blk64, scal, stats, tile_cnt, tile_off, scan_tmp;
+  DevBuf<int64_t> sub_off, blk64, scal, stats, bin_cnt, scan_tmp;
   DevBuf<uint8_t> next_flag, status, over;
   DevBuf<int4> rec;
   DevBuf<uint64_t> seg_key, thr;
@@ -327,7 +327,7 @@ struct lpgpu_session_s {
 
   void release_all() {
     release_partition();
-    DevBuf<int64_t>* b64[] = {&net_off, &vtx_off, &sub_off, &stats, &tile_cnt, &tile_off, &scan_tmp};
+    DevBuf<int64_t>* b64[] = {&net_off, &vtx_off, &sub_off, &stats, &bin_cnt, &scan_tmp};
     for (auto* b : b64) b->release(&mem);
     DevBuf<int32_t>* b32[] = {&pins, &inets, &w_v, &w_e, &list, &net_epoch, &seg_w, &heavy, &revl};
     for (auto* b : b32) b->release(&mem);
@@ -363,8 +363,6 @@ struct DeviceGuard {
     if (prev >= 0) cudaSetDevice(prev);
   }
 };
-
-int64_t tiles_for(int64_t n) { return std::max<int64_t>(1, (n + 1023) / 1024); }
 
 // Structural checks of the upload arguments on the host (O(instances)); the
 // per-net, per-pin and per-vertex checks run on the device after the copy
@@ -525,11 +523,8 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
   CK(s->revl.alloc(n, fp));
   CK(s->vout.alloc(std::max<int64_t>(kVSums + 2 * (int64_t)I, kDegBuckets), fp));
   CK(s->sub_off.alloc(2 * kMaxSubrounds + 1, fp));
-  const int64_t tiles = tiles_for(n);
-  CK(s->tile_cnt.alloc(kMaxSubrounds * kDegClasses * tiles, fp));
-  CK(s->tile_off.alloc(kMaxSubrounds * kDegClasses * tiles, fp));
-  s->scan_tmp_n =
-      std::max<int64_t>(1, std::max(scan_tmp_elems(n + 1), scan_tmp_elems(kMaxSubrounds * kDegClasses * tiles)));
+  CK(s->bin_cnt.alloc(2 * kMaxSubrounds * kDegClasses, fp));
+  s->scan_tmp_n = std::max<int64_t>(1, scan_tmp_elems(n + 1));
   CK(s->scan_tmp.alloc(s->scan_tmp_n, fp));
   cudaStream_t st = s->st;
   const Launch L = s->launch();
@@ -1119,6 +1114,8 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
     if ((e = cudaMemsetAsync(s->blk64.p, 0, sizeof(int64_t) * (7 * s->k + 1), st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(s->scal.p, 0, sizeof(int64_t) * kScalars, st)) != cudaSuccess) return e;
     if (s->m > 0 && (e = cudaMemsetAsync(s->net_epoch.p, 0, sizeof(int32_t) * s->m, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(s->bin_cnt.p, 0, sizeof(int64_t) * kMaxSubrounds * kDegClasses, st)) != cudaSuccess)
+      return e;
     if (s->batched && (e = cudaMemsetAsync(s->inst_delta.p, 0, sizeof(int64_t) * s->num_inst, st)) != cudaSuccess)
       return e;
     if (num_nodes > 0) {
@@ -1138,8 +1135,7 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
       return cudaSuccess;
     }
     for (int r = 0; r < R; ++r) {
-      if ((e = launch_bin_active(L, c, r, S, s->tile_cnt.p, s->tile_off.p, s->scan_tmp.p, s->scan_tmp_n, tm)) != cudaSuccess)
-        return e;
+      if ((e = launch_bin_active(L, c, r, S, s->bin_cnt.p, tm)) != cudaSuccess) return e;
       for (int sub = 0; sub < S; ++sub)
         if ((e = launch_subround(L, c, r, sub, tm)) != cudaSuccess) return e;
       if (r + 1 < R && (e = launch_expand_nets(L, c, S, tm)) != cudaSuccess) return e;
@@ -1157,8 +1153,7 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
     struct Key {
       RoundCtx c;
       int R, S, timing, px;
-      int64_t* p[3];
-      int64_t scan_n;
+      int64_t* p[1];
       lpgpu_tuning tu;
       const void* px_ptr[2];
       int32_t px_count;
@@ -1175,10 +1170,7 @@ lpgpu_status lpgpu_session_refine(lpgpu_session* s, const lpgpu_config* cfg_in,
       key.px_ptr[1] = s->px_order.p;
       key.px_count = px_count;
     }
-    key.p[0] = s->tile_cnt.p;
-    key.p[1] = s->tile_off.p;
-    key.p[2] = s->scan_tmp.p;
-    key.scan_n = s->scan_tmp_n;
+    key.p[0] = s->bin_cnt.p;
     std::vector<unsigned char> kb(reinterpret_cast<unsigned char*>(&key),
                                   reinterpret_cast<unsigned char*>(&key) + sizeof(key));
     if (!s->graph || s->graph_key != kb) {
@@ -1711,12 +1703,11 @@ lpgpu_status lpgpu_session_footprint(lpgpu_session* s, int64_t* bytes) {
 int64_t lpgpu_estimate_footprint(int64_t n, int64_t m, int64_t P, int32_t k, int32_t subrounds) {
   (void)subrounds;
   const int64_t W = word_class_of(std::max(1, k));
-  const int64_t tiles = tiles_for(n);
   int64_t b = 0;
   b += 8 * (m + 1) + 8 * (n + 1) + 4 * P * 2 + 4 * n + 4 * m;          // CSR + weights
   b += 4 * m + 4 * n + n + n + 16 * n + 8 * n + 4 * n + 8 * n;         // epoch, list, flags, status, rec, seg, queues
-  b += 8 * (2 * kMaxSubrounds + 1) + 2 * 8 * kMaxSubrounds * kDegClasses * tiles;  // sub-round bins
-  b += 8 * (scan_tmp_elems(std::max(n + 1, kMaxSubrounds * kDegClasses * tiles)) + 1);
+  b += 8 * (2 * kMaxSubrounds + 1) + 8 * 2 * kMaxSubrounds * kDegClasses;  // sub-round bins
+  b += 8 * (scan_tmp_elems(n + 1) + 1);
   b += 4 * n + 4 * m * (int64_t)k + 8 * m * W;                         // part, Φ, Λ + Λ1
   b += 8 * (3 * k + 7 * k + 1 + 2 * k) + 2 * k + 8 * 64 + 8 * 8;       // per-block, stats, scalars
   return b;
