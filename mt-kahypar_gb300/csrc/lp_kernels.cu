@@ -288,10 +288,10 @@ __global__ void k_degree_hist(int64_t n, const int64_t* __restrict__ cnt, int64_
 // (list start + the rank k_count_pins returned). A warp takes the next 32 nets
 // from a counter and walks their pins in packed 32-pin groups (nets of more
 // than 32 pins alone, 32 pins at a time), so small nets keep every lane busy.
-// Taking nets in order keeps the nets in flight close together, so the
-// partly written 32-byte sectors of their vertices' lists stay in L2 until
-// they are complete (a grid-stride loop lets warps drift apart over nets of
-// uneven size, and the sectors were written back many times).
+// Taking nets in order keeps the nets in flight close together, so where a
+// hypergraph's pins are local, the partly written 32-byte sectors of their
+// vertices' lists stay in L2 until they are complete (a grid-stride loop lets
+// warps drift apart over nets of uneven size).
 __global__ void __launch_bounds__(256) k_scatter_incidence(int64_t m, const int64_t* __restrict__ net_off,
                                                            const int32_t* __restrict__ pins,
                                                            const int64_t* __restrict__ vtx_off,

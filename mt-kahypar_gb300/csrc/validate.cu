@@ -112,6 +112,10 @@ __global__ void k_check_nets_flat(int64_t m, int64_t P, const int64_t* __restric
     nonunit |= we != 1;
     gsum += (b - a) * (int64_t)we;
   }
+  // one set of atomics per CTA: the sums meet in shared memory
+  __shared__ int64_t s_sum[32], s_maxs[32];
+  __shared__ int s_maxw[32], s_nonunit[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     gsum += __shfl_xor_sync(FULL, gsum, o);
@@ -119,7 +123,20 @@ __global__ void k_check_nets_flat(int64_t m, int64_t P, const int64_t* __restric
     maxs = max(maxs, __shfl_xor_sync(FULL, maxs, o));
     nonunit |= __shfl_xor_sync(FULL, nonunit, o);
   }
-  if ((threadIdx.x & 31) == 0) {
+  if (lane == 0) {
+    s_sum[w] = gsum;
+    s_maxw[w] = maxw;
+    s_maxs[w] = maxs;
+    s_nonunit[w] = nonunit;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int x = 1; x < (int)(blockDim.x >> 5); ++x) {
+      gsum += s_sum[x];
+      maxw = max(maxw, s_maxw[x]);
+      maxs = max(maxs, s_maxs[x]);
+      nonunit |= s_nonunit[x];
+    }
     if (gsum) atomicAdd(reinterpret_cast<ull*>(&out[kVSums]), (ull)gsum);
     if (maxw) atomicMax(reinterpret_cast<unsigned long long*>(&out[kVMaxWe]), (ull)maxw);
     if (maxs) atomicMax(reinterpret_cast<unsigned long long*>(&out[kVMaxSize]), (ull)maxs);
@@ -138,12 +155,26 @@ __global__ void k_check_pins_flat(int64_t P, const int32_t* __restrict__ pins, i
 }
 
 // Thread per vertex: w(v) >= 0, the vertex's instance (written to vinst when
-// given, i.e. for every batched session), Σ w(v) per instance (warp sums when
+// given, i.e. for every batched session), Σ w(v) per instance (one instance:
+// per-thread sums, one atomic per warp at the end; several: warp sums when
 // the warp's vertices share an instance).
 __global__ void k_check_vertices(int64_t n, const int32_t* __restrict__ w_v, int I,
                                  const int64_t* __restrict__ inst_voff, int32_t* __restrict__ vinst,
                                  int64_t* out) {
   const int lane = threadIdx.x & 31;
+  if (I <= 1) {
+    int64_t acc = 0;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t w = w_v ? w_v[v] : 1;
+      if (w < 0) fail(out, kVNegVertexWeight);
+      if (vinst) vinst[v] = 0;
+      acc += w;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
+    if (lane == 0 && acc) atomicAdd(reinterpret_cast<ull*>(&out[kVSums + I]), (ull)acc);
+    return;
+  }
   for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < n;
        base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t v = base + lane;
