@@ -246,12 +246,13 @@ cudaError_t launch_apply_moves(const Launch& L, const RoundCtx& c, int64_t count
                                const int32_t* v, const int32_t* from, const int32_t* to, const GainCache& g);
 
 // Device-side input checks (validate.cu). `out` holds kVSums + 2 I words;
-// `inst_voff`, `inst_noff` are read when I > 1; `vinst` (batched sessions,
-// null otherwise) receives every vertex's instance.
+// `inst_voff`, `inst_noff` and `inst_poff` (each instance's pin range,
+// non-decreasing from 0 to P) are read when I > 1; `vinst` (batched
+// sessions, null otherwise) receives every vertex's instance.
 cudaError_t launch_validate_csr(const Launch& L, int64_t n, int64_t m, int64_t P, const int64_t* net_off,
                                 const int32_t* pins, const int32_t* w_v, const int32_t* w_e, int I,
-                                const int64_t* inst_voff, const int64_t* inst_noff, int32_t* vinst,
-                                int64_t* out);
+                                const int64_t* inst_voff, const int64_t* inst_noff, const int64_t* inst_poff,
+                                int32_t* vinst, int64_t* out);
 // Checks the partition ids in `part` (device) against k, or per instance when
 // `vinst` is given, and turns local ids into global ones.
 cudaError_t launch_check_partition(const Launch& L, int64_t n, int32_t* part, int k, const int32_t* vinst,

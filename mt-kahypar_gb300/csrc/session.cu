@@ -494,6 +494,18 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
                                 const int32_t* pins, const int32_t* w_v, const int32_t* w_e,
                                 int32_t num_inst, const int64_t* inst_voff, const int64_t* inst_noff,
                                 const lpgpu_instance* insts = nullptr, const int64_t* inst_poff = nullptr) {
+  // each instance's pin range of a batch (host-computed for per-instance
+  // buffers, from the union's offsets otherwise), checked before any copy
+  const bool batch = inst_voff != nullptr;
+  std::vector<int64_t> hpoff;
+  if (batch) {
+    hpoff.resize(num_inst + 1);
+    for (int32_t i = 0; i < num_inst; ++i) hpoff[i] = insts ? inst_poff[i] : net_off[inst_noff[i]];
+    hpoff[num_inst] = P;
+    for (int32_t i = 0; i < num_inst; ++i)
+      if (hpoff[i] < 0 || hpoff[i] > hpoff[i + 1])
+        return invalid("net_offsets must be non-decreasing and within the pin array");
+  }
   DeviceGuard g(s->device);
   CK(cudaStreamSynchronize(s->st));
   // buffers of the same size are reused; the partition must be set again
@@ -579,18 +591,18 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
   s->h_inst_noff.assign(2, 0);
   s->h_inst_voff[1] = n;
   s->h_inst_noff[1] = m;
+  TmpBuf<int64_t> poff(s->mem);  // hpoff on the device, alive through the checks
   if (s->batched) {
     s->h_inst_voff.assign(inst_voff, inst_voff + I + 1);
     s->h_inst_noff.assign(inst_noff, inst_noff + I + 1);
     CK(s->vinst.alloc(n, fp));
     CK(s->inst_voff.alloc(I + 1, fp));
     CK(s->inst_noff.alloc(I + 1, fp));
+    CK(poff.alloc(I + 1));
     CK(cudaMemcpyAsync(s->inst_voff.p, inst_voff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(s->inst_noff.p, inst_noff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(poff.p(), hpoff.data(), sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
     if (insts) {  // local ids to union ids
-      TmpBuf<int64_t> poff(s->mem);
-      CK(poff.alloc(I + 1));
-      CK(cudaMemcpyAsync(poff.p(), inst_poff, sizeof(int64_t) * (I + 1), cudaMemcpyHostToDevice, st));
       CK(launch_rebase_instances(L, I, s->inst_voff.p, s->inst_noff.p, poff.p(), s->net_off.p, s->pins.p,
                                  staged.p()));
       CK(cudaStreamSynchronize(st));
@@ -602,7 +614,7 @@ static lpgpu_status upload_impl(lpgpu_session* s, int64_t n, int64_t m, int64_t 
   }
   // device-side checks; one copy back of the result words and the per-instance sums
   CK(launch_validate_csr(s->launch(), n, m, P, s->net_off.p, s->pins.p, s->w_v.p, s->w_e.p, I,
-                         s->inst_voff.p, s->inst_noff.p, s->vinst.p, s->vout.p));
+                         s->inst_voff.p, s->inst_noff.p, poff.p(), s->vinst.p, s->vout.p));
   std::vector<int64_t> h(kVSums + 2 * (size_t)I);
   CK(cudaMemcpyAsync(h.data(), s->vout.p, sizeof(int64_t) * h.size(), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));

@@ -28,66 +28,76 @@ __device__ __forceinline__ int find_instance(const int64_t* __restrict__ off, in
   return lo;
 }
 
-// Warp per net: offsets inside [0, P] and non-decreasing, w(e) >= 0, every
-// pin inside its instance's vertex range; Σ |e|·w(e) per instance, the
-// largest net weight and size, and whether some weight differs from 1.
-__global__ void k_check_nets(int64_t m, int64_t P, const int64_t* __restrict__ net_off,
-                             const int32_t* __restrict__ pins, const int32_t* __restrict__ w_e, int I,
-                             const int64_t* __restrict__ inst_voff, const int64_t* __restrict__ inst_noff,
-                             int64_t n, int64_t* out) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  int64_t gsum = 0;
-  int cur = -1;  // instance whose sum is held in gsum
-  int maxw = 0, nonunit = 0;
-  int64_t maxs = 0;
-  for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < m; e += warps) {
+// Batches: one CTA per instance. Its nets, thread per net: offsets inside
+// [0, P] and non-decreasing, w(e) >= 0; its pins (the instance's pin range
+// inst_poff[i] .. inst_poff[i + 1], non-decreasing and inside [0, P] by a
+// host check), thread per pin: inside the instance's vertex range. Then the
+// instance's Σ |e|·w(e), the largest net weight and size, and whether some
+// weight differs from 1. With the offsets non-decreasing over all nets, the
+// pins of instance i's nets are exactly its pin range, so this is the
+// per-net pin check.
+__global__ void __launch_bounds__(256) k_check_instances(int64_t P, const int64_t* __restrict__ net_off,
+                                                         const int32_t* __restrict__ pins,
+                                                         const int32_t* __restrict__ w_e,
+                                                         const int64_t* __restrict__ inst_voff,
+                                                         const int64_t* __restrict__ inst_noff,
+                                                         const int64_t* __restrict__ inst_poff, int64_t* out) {
+  __shared__ int64_t s_sum[8], s_maxs[8];
+  __shared__ int s_maxw[8], s_flags[8];
+  const int i = blockIdx.x;
+  const int64_t e1 = inst_noff[i + 1];
+  int64_t gsum = 0, maxs = 0;
+  int maxw = 0, flags = 0;  // bit 0: non-unit weight, 1: bad offsets, 2: negative weight, 3: pin range
+  for (int64_t e = inst_noff[i] + threadIdx.x; e < e1; e += blockDim.x) {
     const int64_t a = net_off[e], b = net_off[e + 1];
     if (a < 0 || b < a || b > P) {
-      if (lane == 0) fail(out, kVBadOffsets);
+      flags |= 2;
       continue;
     }
     const int we = w_e ? w_e[e] : 1;
     if (we < 0) {
-      if (lane == 0) fail(out, kVNegNetWeight);
+      flags |= 4;
       continue;
     }
     maxw = max(maxw, we);
     maxs = max(maxs, b - a);
-    nonunit |= we != 1;
-    int inst = 0;
-    int64_t v0 = 0, v1 = n;
-    if (I > 1) {
-      inst = find_instance(inst_noff, I, e);
-      v0 = inst_voff[inst];
-      v1 = inst_voff[inst + 1];
-    }
-    bool bad = false;
-    for (int64_t q = a + lane; q < b; q += 32) {
-      const int32_t p = pins[q];
-      bad |= p < v0 || p >= v1;
-    }
-    if (__any_sync(FULL, bad) && lane == 0) fail(out, kVPinRange);
-    if (lane == 0) {
-      if (inst != cur) {
-        if (cur >= 0 && gsum) atomicAdd(reinterpret_cast<ull*>(&out[kVSums + cur]), (ull)gsum);
-        cur = inst;
-        gsum = 0;
-      }
-      gsum += (b - a) * (int64_t)we;
-    }
+    flags |= we != 1;
+    gsum += (b - a) * (int64_t)we;
   }
-  if (lane == 0 && cur >= 0 && gsum) atomicAdd(reinterpret_cast<ull*>(&out[kVSums + cur]), (ull)gsum);
+  const int64_t v0 = inst_voff[i], v1 = inst_voff[i + 1], q1 = inst_poff[i + 1];
+  for (int64_t q = inst_poff[i] + threadIdx.x; q < q1; q += blockDim.x) {
+    const int32_t p = pins[q];
+    if (p < v0 || p >= v1) flags |= 8;
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
+    gsum += __shfl_xor_sync(FULL, gsum, o);
     maxw = max(maxw, __shfl_xor_sync(FULL, maxw, o));
     maxs = max(maxs, __shfl_xor_sync(FULL, maxs, o));
-    nonunit |= __shfl_xor_sync(FULL, nonunit, o);
+    flags |= __shfl_xor_sync(FULL, flags, o);
   }
   if (lane == 0) {
+    s_sum[w] = gsum;
+    s_maxw[w] = maxw;
+    s_maxs[w] = maxs;
+    s_flags[w] = flags;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int x = 1; x < (int)(blockDim.x >> 5); ++x) {
+      gsum += s_sum[x];
+      maxw = max(maxw, s_maxw[x]);
+      maxs = max(maxs, s_maxs[x]);
+      flags |= s_flags[x];
+    }
+    if (flags & 2) fail(out, kVBadOffsets);
+    if (flags & 4) fail(out, kVNegNetWeight);
+    if (flags & 8) fail(out, kVPinRange);
+    if (gsum) atomicAdd(reinterpret_cast<ull*>(&out[kVSums + i]), (ull)gsum);
     if (maxw) atomicMax(reinterpret_cast<unsigned long long*>(&out[kVMaxWe]), (ull)maxw);
     if (maxs) atomicMax(reinterpret_cast<unsigned long long*>(&out[kVMaxSize]), (ull)maxs);
-    if (nonunit) atomicOr(reinterpret_cast<ull*>(&out[kVNonUnit]), 1ull);
+    if (flags & 1) atomicOr(reinterpret_cast<ull*>(&out[kVNonUnit]), 1ull);
   }
 }
 
@@ -278,19 +288,19 @@ int grid(const Launch& L, int64_t items, int threads) {
 
 cudaError_t launch_validate_csr(const Launch& L, int64_t n, int64_t m, int64_t P, const int64_t* net_off,
                                 const int32_t* pins, const int32_t* w_v, const int32_t* w_e, int I,
-                                const int64_t* inst_voff, const int64_t* inst_noff, int32_t* vinst,
-                                int64_t* out) {
+                                const int64_t* inst_voff, const int64_t* inst_noff, const int64_t* inst_poff,
+                                int32_t* vinst, int64_t* out) {
   cudaError_t e = cudaMemsetAsync(out, 0, sizeof(int64_t) * (kVSums + 2 * (int64_t)I), L.st);
   if (e != cudaSuccess) return e;
   if (I > 1) {
-    if (m > 0) k_check_nets<<<grid(L, m * 32, 256), 256, 0, L.st>>>(m, P, net_off, pins, w_e, I, inst_voff,
-                                                                      inst_noff, n, out);
+    if (m > 0 || P > 0)
+      k_check_instances<<<I, 256, 0, L.st>>>(P, net_off, pins, w_e, inst_voff, inst_noff, inst_poff, out);
   } else {
     if (m > 0) k_check_nets_flat<<<grid(L, m, 256), 256, 0, L.st>>>(m, P, net_off, w_e, out);
     if (P > 0) k_check_pins_flat<<<grid(L, P, 256), 256, 0, L.st>>>(P, pins, n, out);
   }
   if (n > 0) k_check_vertices<<<grid(L, n, 256), 256, 0, L.st>>>(n, w_v, I, inst_voff, vinst, out);
-  add_kernel_launches((m > 0) + (n > 0) + (I == 1 && P > 0));
+  add_kernel_launches((I > 1 ? (m > 0 || P > 0) : (m > 0) + (P > 0)) + (n > 0));
   return cudaGetLastError();
 }
 
