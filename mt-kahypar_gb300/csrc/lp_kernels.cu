@@ -1697,33 +1697,33 @@ __device__ __forceinline__ int vertex_class(const ClassRule& r, int64_t v) {
   return g <= 1 ? 1 : (g >= kDegClasses - 1 ? kDegClasses - 1 : (int)g);  // D = 2: always 1
 }
 
-constexpr int kBinBins = kMaxSubrounds * kDegClasses;
-constexpr int kBinThreadsA = 1024;  // binning CTAs
-constexpr int kBinBatch = 4;        // chunks per warp and batch (independent loads in flight)
-constexpr int kBinBatchChunks = (kBinThreadsA / 32) * kBinBatch;
+constexpr int kListBins = kMaxSubrounds * kDegClasses;  // (sub-round, class) bins
+constexpr int kListBinThreads = 1024;                     // binning CTAs
+constexpr int kListBinBatch = 4;  // chunks per warp and batch (independent loads in flight)
+constexpr int kListBinChunks = (kListBinThreads / 32) * kListBinBatch;
 
-__global__ void __launch_bounds__(kBinThreadsA) k_bin_count(uint8_t* __restrict__ flag, int64_t n, int round, int S,
-                                                            int64_t* __restrict__ cnt, ClassRule rule,
-                                                            const int32_t* __restrict__ vinst,
-                                                            const int64_t* __restrict__ inst_voff) {
-  __shared__ int s_cnt[kBinBins];
+__global__ void __launch_bounds__(kListBinThreads) k_bin_count(uint8_t* __restrict__ flag, int64_t n, int round,
+                                                               int S, int64_t* __restrict__ cnt, ClassRule rule,
+                                                               const int32_t* __restrict__ vinst,
+                                                               const int64_t* __restrict__ inst_voff) {
+  __shared__ int s_cnt[kListBins];
   const int bins = S * kDegClasses;
   const int w = threadIdx.x >> 5, lane = lane_id();
   for (int i = threadIdx.x; i < bins; i += blockDim.x) s_cnt[i] = 0;
   __syncthreads();
   const int64_t chunks = (n + 31) >> 5;
-  for (int64_t c0 = (int64_t)blockIdx.x * kBinBatchChunks; c0 < chunks; c0 += (int64_t)gridDim.x * kBinBatchChunks) {
-    bool f[kBinBatch];
+  for (int64_t c0 = (int64_t)blockIdx.x * kListBinChunks; c0 < chunks; c0 += (int64_t)gridDim.x * kListBinChunks) {
+    bool f[kListBinBatch];
 #pragma unroll
-    for (int j = 0; j < kBinBatch; ++j) {
+    for (int j = 0; j < kListBinBatch; ++j) {
       const int64_t v = ((c0 + j * 32 + w) << 5) + lane;
       f[j] = v < n && flag[v];
     }
-    int cls[kBinBatch];
+    int cls[kListBinBatch];
 #pragma unroll
-    for (int j = 0; j < kBinBatch; ++j) cls[j] = f[j] ? vertex_class(rule, ((c0 + j * 32 + w) << 5) + lane) : 0;
+    for (int j = 0; j < kListBinBatch; ++j) cls[j] = f[j] ? vertex_class(rule, ((c0 + j * 32 + w) << 5) + lane) : 0;
 #pragma unroll
-    for (int j = 0; j < kBinBatch; ++j) {
+    for (int j = 0; j < kListBinBatch; ++j) {
       const int64_t v = ((c0 + j * 32 + w) << 5) + lane;
       if (f[j]) flag[v] = (uint8_t)(1 + cls[j]);
       if (vinst) {
@@ -1743,21 +1743,21 @@ __global__ void __launch_bounds__(kBinThreadsA) k_bin_count(uint8_t* __restrict_
     if (s_cnt[i]) atomicAdd(reinterpret_cast<ull*>(&cnt[i]), (ull)s_cnt[i]);
 }
 
-// One CTA: the bins' start positions (cnt[kBinBins + b]) from their counts,
+// One CTA: the bins' start positions (cnt[kListBins + b]) from their counts,
 // which are cleared for the next round; the sub-round offsets (sub-round s
 // occupies list[sub_off[s] .. sub_off[s + 1]), its heavy vertices the first
 // sub_off[kMaxSubrounds + 1 + s] - sub_off[s]) and the round's activation
 // epoch.
-constexpr int kBinOffThreads = (kBinBins + 31) / 32 * 32;
-__global__ void __launch_bounds__(kBinOffThreads) k_bin_offsets(int64_t* __restrict__ cnt, int S,
-                                                                int64_t* __restrict__ sub_off, int64_t* scal) {
-  __shared__ int64_t s_off[kBinBins];
+constexpr int kListOffThreads = (kListBins + 31) / 32 * 32;
+__global__ void __launch_bounds__(kListOffThreads) k_bin_offsets(int64_t* __restrict__ cnt, int S,
+                                                                 int64_t* __restrict__ sub_off, int64_t* scal) {
+  __shared__ int64_t s_off[kListBins];
   const int bins = S * kDegClasses, i = threadIdx.x;
   const int64_t x = i < bins ? cnt[i] : 0;
   int64_t total;
   const int64_t off = block_scan_excl_i64(x, &total);
   if (i < bins) {
-    cnt[kBinBins + i] = off;
+    cnt[kListBins + i] = off;
     cnt[i] = 0;
     s_off[i] = off;
   }
@@ -1772,30 +1772,30 @@ __global__ void __launch_bounds__(kBinOffThreads) k_bin_offsets(int64_t* __restr
   }
 }
 
-__global__ void __launch_bounds__(kBinThreadsA) k_bin_scatter(uint8_t* __restrict__ flag, int64_t n, int round,
-                                                              int S, int64_t* __restrict__ cnt,
-                                                              int32_t* __restrict__ list,
-                                                              const int32_t* __restrict__ vinst,
-                                                              const int64_t* __restrict__ inst_voff) {
-  __shared__ int s_cnt[kBinBins];
-  __shared__ int64_t s_base[kBinBins];
-  int64_t* cursor = cnt + kBinBins;
+__global__ void __launch_bounds__(kListBinThreads) k_bin_scatter(uint8_t* __restrict__ flag, int64_t n, int round,
+                                                                 int S, int64_t* __restrict__ cnt,
+                                                                 int32_t* __restrict__ list,
+                                                                 const int32_t* __restrict__ vinst,
+                                                                 const int64_t* __restrict__ inst_voff) {
+  __shared__ int s_cnt[kListBins];
+  __shared__ int64_t s_base[kListBins];
+  int64_t* cursor = cnt + kListBins;
   const int bins = S * kDegClasses;
   const int w = threadIdx.x >> 5, lane = lane_id();
   for (int i = threadIdx.x; i < bins; i += blockDim.x) s_cnt[i] = 0;
   __syncthreads();
   const int64_t chunks = (n + 31) >> 5;
-  for (int64_t c0 = (int64_t)blockIdx.x * kBinBatchChunks; c0 < chunks; c0 += (int64_t)gridDim.x * kBinBatchChunks) {
-    int fl[kBinBatch];
+  for (int64_t c0 = (int64_t)blockIdx.x * kListBinChunks; c0 < chunks; c0 += (int64_t)gridDim.x * kListBinChunks) {
+    int fl[kListBinBatch];
 #pragma unroll
-    for (int j = 0; j < kBinBatch; ++j) {
+    for (int j = 0; j < kListBinBatch; ++j) {
       const int64_t v = ((c0 + j * 32 + w) << 5) + lane;
       fl[j] = v < n ? flag[v] : 0;
     }
     // each vertex's bin and its place among the batch's vertices of that bin
-    int bin[kBinBatch], at[kBinBatch];
+    int bin[kListBinBatch], at[kListBinBatch];
 #pragma unroll
-    for (int j = 0; j < kBinBatch; ++j) {
+    for (int j = 0; j < kListBinBatch; ++j) {
       const int64_t v = ((c0 + j * 32 + w) << 5) + lane;
       const bool f = fl[j] != 0;
       const int cls = f ? fl[j] - 1 : 0;
@@ -1829,7 +1829,7 @@ __global__ void __launch_bounds__(kBinThreadsA) k_bin_scatter(uint8_t* __restric
     }
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < kBinBatch; ++j) {
+    for (int j = 0; j < kListBinBatch; ++j) {
       if (bin[j] >= 0) {
         const int64_t v = ((c0 + j * 32 + w) << 5) + lane;
         list[s_base[bin[j]] + at[j]] = (int32_t)v;
@@ -1886,7 +1886,7 @@ struct Scope {
 
 // CTAs of the binning kernels: two resident per SM, at most one per batch of chunks
 static int bin_ctas(int64_t n, int num_sms) {
-  const int64_t batches = std::max<int64_t>(1, ((n + 31) / 32 + kBinBatchChunks - 1) / kBinBatchChunks);
+  const int64_t batches = std::max<int64_t>(1, ((n + 31) / 32 + kListBinChunks - 1) / kListBinChunks);
   return (int)std::max<int64_t>(1, std::min<int64_t>(batches, 2 * (int64_t)std::max(1, num_sms)));
 }
 
@@ -1896,11 +1896,11 @@ cudaError_t launch_bin_active(const Launch& L, const RoundCtx& c, int round, int
   const int G = bin_ctas(c.n, L.num_sms);
   const int32_t* vinst = c.batched ? c.vinst : nullptr;
   const ClassRule rule{c.vtx_off, c.W, c.unit_nets, c.max_we};
-  k_bin_count<<<G, kBinThreadsA, 0, L.st>>>(c.next_flag, c.n, round, S, bin_cnt, rule, vinst, c.inst_voff);
+  k_bin_count<<<G, kListBinThreads, 0, L.st>>>(c.next_flag, c.n, round, S, bin_cnt, rule, vinst, c.inst_voff);
   LAUNCHED("k_bin_count");
-  k_bin_offsets<<<1, kBinOffThreads, 0, L.st>>>(bin_cnt, S, c.sub_off, c.scal);
+  k_bin_offsets<<<1, kListOffThreads, 0, L.st>>>(bin_cnt, S, c.sub_off, c.scal);
   LAUNCHED("k_bin_offsets");
-  k_bin_scatter<<<G, kBinThreadsA, 0, L.st>>>(c.next_flag, c.n, round, S, bin_cnt, c.list, vinst, c.inst_voff);
+  k_bin_scatter<<<G, kListBinThreads, 0, L.st>>>(c.next_flag, c.n, round, S, bin_cnt, c.list, vinst, c.inst_voff);
   LAUNCHED("k_bin_scatter");
   return cudaGetLastError();
 }
