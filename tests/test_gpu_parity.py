@@ -437,6 +437,55 @@ def test_device_side_input_checks(lp, orc):
         assert s.instance_km1().shape == (3,)
 
 
+@pytest.mark.parametrize("form", ["union", "instances"])
+def test_batched_input_checks(lp, form):
+    """Batched uploads are checked per instance on the device: a pin outside
+    its instance's vertex range, a negative net weight and decreasing offsets
+    inside one instance are each rejected with INVALID_ARG, and the session then
+    refines a valid batch exactly as one session per instance does."""
+    from lpgpu import gen
+    insts = [gen.random_small(40 + i, n=150 + 20 * i, m=170, k=3) for i in range(3)]
+
+    def broken(kind):
+        hgs = [x.hg for x in insts]
+        h = hgs[1]
+        if kind == "pin":
+            pins = h.pins.copy()
+            pins[5] = h.n  # local id one past the instance's last vertex
+            hgs[1] = gen.Hypergraph(h.n, h.m, h.net_off, pins, h.w_v, h.w_e)
+        elif kind == "net weight":
+            w_e = h.w_e.copy()
+            w_e[3] = -1
+            hgs[1] = gen.Hypergraph(h.n, h.m, h.net_off, h.pins, h.w_v, w_e)
+        else:  # decreasing offsets inside the instance
+            off = h.net_off.copy()
+            off[4] = off[6]
+            off[5] = off[3]
+            hgs[1] = gen.Hypergraph(h.n, h.m, off, h.pins, h.w_v, h.w_e)
+        return hgs
+
+    def upload(s, hgs):
+        return s.upload_batch(hgs) if form == "union" else s.upload_instances(hgs)
+
+    cfg = lp.default_config(rounds=3)
+    with lp.Session(0) as s:
+        for kind in ("pin", "net weight", "offsets"):
+            with pytest.raises(lp.LpgpuError) as e:
+                upload(s, broken(kind))
+            assert e.value.status == lp.ERR_INVALID_ARG, kind
+        upload(s, [x.hg for x in insts])
+        s.set_partition_batch([x.k for x in insts], [x.part for x in insts])
+        s.refine(cfg)
+        got = s.instance_km1()
+    want = []
+    for x in insts:
+        with lp.Session(0) as t:
+            t.upload(x.hg)
+            t.set_partition(x.k, x.part)
+            want.append(t.refine(cfg).km1_after)
+    assert list(got) == want
+
+
 def test_one_shot_entry_point(lp, orc):
     from lpgpu import gen
     inst = gen.plain_small(seed=2)
