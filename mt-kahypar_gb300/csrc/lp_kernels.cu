@@ -2246,14 +2246,107 @@ __device__ uint64_t cta_radix_select(const uint64_t* __restrict__ gkeys, const i
   return prefix;
 }
 
-// Target-side selection: CTAs stride over the overflowing blocks.
+// Warp-wide radix selection over the cnt keys at `keys` (written earlier in
+// this kernel, so read through plain loads): the same threshold as
+// cta_radix_select (the first key whose weighted prefix exceeds `budget`, all
+// ones when the total stays within it), with only warp barriers between the
+// byte passes. `hist`: 256 words of this warp's shared scratch.
+__device__ uint64_t warp_radix_select(const uint64_t* keys, const int32_t* ws, int cnt, int64_t budget,
+                                      unsigned* hist) {
+  const int lane = lane_id();
+  uint64_t ka = ~0ull, ko = 0;
+  for (int i = lane; i < cnt; i += 32) {
+    const uint64_t key = keys[i];
+    ka &= key;
+    ko |= key;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ka &= __shfl_xor_sync(FULLMASK, ka, o);
+    ko |= __shfl_xor_sync(FULLMASK, ko, o);
+  }
+  uint64_t prefix = 0, mask = 0;
+  for (int byte = 7; byte >= 0; --byte) {
+    const int shift = 8 * byte;
+    if ((((ka ^ ko) >> shift) & 255) == 0) {  // every key has this byte
+      prefix |= ka & (255ull << shift);
+      mask |= 255ull << shift;
+      continue;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) hist[32 * j + lane] = 0;
+    __syncwarp();
+    for (int i = lane; i < cnt; i += 32) {
+      const uint64_t key = keys[i];
+      if ((key & mask) == prefix) atomicAdd(&hist[(unsigned)(key >> shift) & 255u], (unsigned)ws[i]);
+    }
+    __syncwarp();
+    // lane l owns bins 8l .. 8l+7: first bin whose running sum exceeds the budget
+    int64_t h[8], sum = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      h[j] = hist[8 * lane + j];
+      sum += h[j];
+    }
+    int64_t run = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(FULLMASK, run, o);
+      if (lane >= o) run += y;
+    }
+    int sel = -1;
+    int64_t below = 0, acc = run - sum;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      if (sel < 0 && acc + h[j] > budget) {
+        sel = 8 * lane + j;
+        below = acc;
+      }
+      acc += h[j];
+    }
+    const unsigned found = __ballot_sync(FULLMASK, sel >= 0);
+    const int first = found ? __ffs(found) - 1 : 31;
+    const int pick = __shfl_sync(FULLMASK, found ? sel : 255, first);
+    budget = __shfl_sync(FULLMASK, budget - (found ? below : acc), first);
+    prefix |= (uint64_t)pick << shift;
+    mask |= 255ull << shift;
+    __syncwarp();  // the histogram is cleared by the next pass
+  }
+  return prefix;
+}
+
+#ifndef LPGPU_SEL_WARP
+#define LPGPU_SEL_WARP 512  // segments of at most this many keys are selected by one warp
+#endif
+constexpr int kSelWarpKeys = LPGPU_SEL_WARP;
+static_assert(kSelSmem >= (size_t)(kSelThreads / 32) * 256 * sizeof(unsigned),
+              "every warp's selection histogram fits the staging area");
+
+// Target-side selection. With more overflowing blocks than CTAs, warps
+// first stride over the blocks with small segments (histograms in the staging
+// area, not in use then), which CTAs would otherwise take one after another;
+// CTAs take the others (all blocks when each gets a CTA of its own).
 __device__ void from_side(const RoundCtx& c, int sub);
 
 // Its last CTA then runs the source-side selection (from_side).
 __global__ void __launch_bounds__(kSelThreads) k_select(RoundCtx c, int sub) {
+  extern __shared__ __align__(16) unsigned char sel_smem[];
   const int64_t nover = c.scal[kOverCount];
+  const int64_t warp_keys = nover > gridDim.x ? kSelWarpKeys : -1;
+  const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned* whist = reinterpret_cast<unsigned*>(sel_smem) + 256 * wid;
+  for (int64_t i = (int64_t)blockIdx.x * nw + wid; warp_keys >= 0 && i < nover; i += (int64_t)gridDim.x * nw) {
+    const int b = c.over_ids[i];
+    const int64_t cnt = c.in_cnt[b];
+    if (cnt > warp_keys) continue;
+    const int64_t off = c.seg_off[b];
+    const uint64_t thr = warp_radix_select(c.seg_key + off, c.seg_w + off, (int)cnt, c.lmax[b] - c.bw[b], whist);
+    if (lane_id() == 0) c.thr_to[b] = thr;
+  }
+  __syncthreads();
   for (int64_t i = blockIdx.x; i < nover; i += gridDim.x) {
     const int b = c.over_ids[i];
+    if (c.in_cnt[b] <= warp_keys) continue;  // the same for the whole CTA
     const int64_t off = c.seg_off[b];
     const uint64_t thr = cta_radix_select(c.seg_key + off, c.seg_w + off, c.in_cnt[b],
                                           c.lmax[b] - c.bw[b]);
@@ -3375,13 +3468,20 @@ __device__ void px_heavy(const PxInst& I, const PxParams& P, PxShared& s, int64_
   __syncwarp();
 }
 
+constexpr int kPxStage = 2048;  // selection keys staged in the CTA-flat area (not in use then)
+static_assert(sizeof(FlatSmem) >= (size_t)kPxStage * 12, "staged keys and weights fit the CTA-flat area");
+
+#ifndef LPGPU_PX_WARP_SEL
+#define LPGPU_PX_WARP_SEL 512  // segments of at most this many keys get one warp each
+#endif
+constexpr int kPxWarpSelKeys = LPGPU_PX_WARP_SEL;
+static_assert(sizeof(FlatSmem) >= (size_t)(kPxThreads / 32) * 256 * sizeof(unsigned),
+              "every warp's selection histogram fits the CTA-flat area");
+
 // Thresholds of the blocks flagged in `over` (bit b): the first key of the
 // block's segment whose weighted prefix exceeds budget(b). The segments are
 // filled from the candidate list by member(rec, lv) (the block a candidate
 // belongs to, or -1); cnt[b] is the size of block b's segment.
-constexpr int kPxStage = 2048;  // selection keys staged in the CTA-flat area (not in use then)
-static_assert(sizeof(FlatSmem) >= (size_t)kPxStage * 12, "staged keys and weights fit the CTA-flat area");
-
 template <typename Member, typename Budget>
 __device__ void px_select(const PxInst& I, PxShared& s, FlatSmem& f, uint64_t over, const unsigned* cnt,
                           uint64_t* thr, Member member, Budget budget) {
@@ -3406,8 +3506,22 @@ __device__ void px_select(const PxInst& I, PxShared& s, FlatSmem& f, uint64_t ov
     }
   }
   __syncthreads();
+  // with several blocks to select, small segments get one warp each, all at
+  // once (histograms in the CTA-flat area, not in use here); the others take
+  // the whole CTA, one after another
+  const int64_t warp_keys = __popcll(over) > 1 ? kPxWarpSelKeys : -1;
+  const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned* whist = reinterpret_cast<unsigned*>(&f) + 256 * wid;
+  for (int b = wid; b < I.k; b += nw) {
+    const int64_t nb = s.seg[b + 1] - s.seg[b];
+    if (((over >> b) & 1) && nb <= warp_keys) {
+      const uint64_t t = warp_radix_select(I.keys + s.seg[b], I.kw + s.seg[b], (int)nb, budget(b), whist);
+      if (lane_id() == 0) thr[b] = t;
+    }
+  }
+  __syncthreads();
   for (int b = 0; b < I.k; ++b) {
-    if (!((over >> b) & 1)) continue;
+    if (!((over >> b) & 1) || s.seg[b + 1] - s.seg[b] <= warp_keys) continue;
     const uint64_t t = cta_radix_select(I.keys + s.seg[b], I.kw + s.seg[b], s.seg[b + 1] - s.seg[b], budget(b),
                                         reinterpret_cast<unsigned char*>(&f), kPxStage);
     if (threadIdx.x == 0) thr[b] = t;
