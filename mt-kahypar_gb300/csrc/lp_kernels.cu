@@ -2415,8 +2415,24 @@ __device__ void from_side(const RoundCtx& c, int sub) {
     }
   }
   __syncthreads();
+  // several blocks: small segments one warp each, all at once (histograms in
+  // the staging area); the others the whole CTA, one after another
+  int nof = 0;
+  for (int b0 = 0; b0 < k; b0 += blockDim.x)
+    nof += __syncthreads_count(b0 + (int)threadIdx.x < k && c.over_from[b0 + threadIdx.x]);
+  const int64_t warp_keys = nof > 1 ? kSelWarpKeys : -1;
+  extern __shared__ __align__(16) unsigned char sel_smem[];
+  const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned* whist = reinterpret_cast<unsigned*>(sel_smem) + 256 * wid;
+  for (int b = wid; b < k; b += nw) {
+    if (!c.over_from[b] || c.acc_cnt[b] > warp_keys) continue;
+    const int64_t off = c.seg_off[b];
+    const uint64_t thr = warp_radix_select(c.seg_key + off, c.seg_w + off, (int)c.acc_cnt[b], c.bw[b] - 1, whist);
+    if (lane_id() == 0) c.thr_from[b] = thr;
+  }
+  __syncthreads();
   for (int b = 0; b < k; ++b) {
-    if (!c.over_from[b]) continue;  // uniform across the CTA
+    if (!c.over_from[b] || c.acc_cnt[b] <= warp_keys) continue;  // uniform across the CTA
     const int64_t off = c.seg_off[b];
     const uint64_t thr = cta_radix_select(c.seg_key + off, c.seg_w + off, c.acc_cnt[b], c.bw[b] - 1);
     if (threadIdx.x == 0) c.thr_from[b] = thr;
